@@ -1,0 +1,199 @@
+/*
+ * ksj_gpu.h -- the thin C ABI over the sm_103a kernels of the non-Cartesian
+ * reconstruction path.  Plain pointers and sizes only; every pointer named
+ * `d_*` is device memory of the current CUDA device, `stream` is a
+ * cudaStream_t (NULL = legacy default stream).  Nothing here allocates device
+ * memory except the ksj_gpu_context helpers, which are a convenience for hosts
+ * (the Provider plug-ins) that do not manage their own workspace.
+ *
+ * Every function returns a ksj_gpu_status.  There is no CPU fallback: a
+ * missing or failing device is reported, never emulated.
+ *
+ * Reference interfaces replaced (paths relative to the KSpaceJet tree):
+ *   ksj_gpu_gridding_adjoint with KSJ_GPU_KERNEL_LINEAR
+ *       <- ksj::nufft::radial_analytic_ramp_dcf2 +
+ *          ksj::nufft::radial_linear_gridding2_adjoint, per channel
+ *          (libs/numerics/kspacejet-nufft/include/kspacejet/nufft/radial_gridding.hpp:33-37, 59-70)
+ *          and the per-channel loop + coil-last scatter of
+ *          providers/kspacejet-noncartesian-recon/src/operators/radial_gridding_reconstruct.cpp:394-413
+ *   ksj_gpu_gridding_adjoint with KSJ_GPU_KERNEL_KAISER_BESSEL
+ *       <- no reference counterpart (new operator radial_kb_gridding_reconstruct)
+ *   ksj_gpu_direct_adjoint
+ *       <- ksj::nufft::direct_nudft2_adjoint, per channel
+ *          (libs/numerics/kspacejet-nufft/include/kspacejet/nufft/direct_nudft.hpp:62-69) and
+ *          providers/kspacejet-noncartesian-recon/src/operators/noncartesian_adjoint_reconstruct.cpp:352-368
+ *   ksj_gpu_rss_coil_last
+ *       <- ksj::stats::root_sum_of_squares_across(cube, image, Dim::dim2)
+ *          (libs/numerics/kspacejet-stats/include/kspacejet/stats/norms.hpp:207-218) as called by
+ *          providers/kspacejet-coil-combine/src/operators/coil_combine_rss.cpp:303-308
+ */
+#ifndef KSJ_GPU_H_
+#define KSJ_GPU_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define KSJ_GPU_API __attribute__((visibility("default")))
+#else
+#define KSJ_GPU_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t ksj_gpu_status;
+#define KSJ_GPU_OK 0
+#define KSJ_GPU_ERROR_INVALID_ARGUMENT 1  /* a size, pointer or mode outside the documented envelope */
+#define KSJ_GPU_ERROR_UNSUPPORTED 2       /* a combination this build does not implement */
+#define KSJ_GPU_ERROR_CUDA 3              /* a CUDA runtime call or launch failed */
+#define KSJ_GPU_ERROR_WORKSPACE 4         /* workspace pointer null, misaligned or too small */
+#define KSJ_GPU_ERROR_OUT_OF_MEMORY 5     /* a ksj_gpu_context allocation failed */
+#define KSJ_GPU_ERROR_NONFINITE_INPUT 6   /* device check: a sample, trajectory or DCF value was rejected */
+
+/* Device-side input checks, reported through ksj_gpu_read_flags(). */
+#define KSJ_GPU_FLAG_NONFINITE_SAMPLE (1u << 0)
+#define KSJ_GPU_FLAG_BAD_TRAJECTORY (1u << 1)   /* non-finite, or outside [-pi, pi] where required */
+#define KSJ_GPU_FLAG_BAD_DCF (1u << 2)          /* non-finite or negative external weight */
+
+/* ------------------------------------------------------------- gridding */
+
+#define KSJ_GPU_KERNEL_LINEAR 0u        /* the reference's periodic 2x2 linear stencil, grid == image */
+#define KSJ_GPU_KERNEL_KAISER_BESSEL 1u /* W-tap Kaiser-Bessel on an oversampled grid, deapodised and cropped */
+
+#define KSJ_GPU_DCF_NONE 0u           /* weight 1 */
+#define KSJ_GPU_DCF_ANALYTIC_RAMP 1u  /* hypot(k_row, k_col), radians per pixel (Ram-Lak) */
+#define KSJ_GPU_DCF_EXTERNAL 2u       /* caller weights d_dcf[frame][sample], finite and >= 0 */
+
+#define KSJ_GPU_OUTPUT_COIL_LAST 0u   /* complex64 [frame][row][col][channel] (ksj.coil-image-frame) */
+#define KSJ_GPU_OUTPUT_RSS 1u         /* float32 [frame][row][col], root-sum-of-squares over channels */
+#define KSJ_GPU_OUTPUT_COIL_MAJOR 2u  /* complex64 [frame][channel][row][col] */
+
+#define KSJ_GPU_SAMPLES_CF32 0u       /* interleaved float32 (re, im) */
+#define KSJ_GPU_SAMPLES_BF16 1u       /* interleaved bfloat16 (re, im); arithmetic stays float32 */
+
+typedef struct ksj_gpu_gridding_desc {
+  uint32_t struct_size;     /* sizeof(ksj_gpu_gridding_desc) */
+  uint32_t kernel;          /* KSJ_GPU_KERNEL_* */
+  uint32_t image_rows;      /* output image, 2..1024 */
+  uint32_t image_cols;
+  uint32_t grid_rows;       /* oversampled grid; == image for LINEAR; 2^a * 3^b, a+b >= 1, <= 1024 */
+  uint32_t grid_cols;
+  uint32_t kernel_width;    /* LINEAR: 2.  KAISER_BESSEL: even, 2..8 */
+  float kb_beta;            /* KAISER_BESSEL shape; <= 0 selects Beatty et al. 2005 for (width, grid/image) */
+  double row_origin;        /* image origin in pixels; the reference uses (rows-1)/2 */
+  double col_origin;
+  uint32_t channels;        /* coils, >= 1 */
+  uint32_t samples;         /* samples per frame and channel, >= 1 */
+  uint32_t frames;          /* independent frames in this call, >= 1 */
+  uint32_t dcf_mode;        /* KSJ_GPU_DCF_* */
+  uint32_t output;          /* KSJ_GPU_OUTPUT_* */
+  uint32_t sample_format;   /* KSJ_GPU_SAMPLES_* */
+  uint32_t require_nyquist; /* nonzero: reject |k| > pi (the reference operator's trajectory contract) */
+  uint32_t reserved0;
+} ksj_gpu_gridding_desc;
+
+/* Tuning knobs chosen per shape by ksj_gpu_gridding_tune() (or by hand).
+ * Zero fields select the built-in heuristic. */
+typedef struct ksj_gpu_gridding_tuning {
+  uint32_t struct_size;
+  uint32_t coil_group;      /* channels accumulated per row CTA: 1, 2, 4, 8, 16 or 32 */
+  uint32_t column_block;    /* columns per column-pass CTA: 4, 8, 16 or 32 */
+  uint32_t list_capacity;   /* per-warp sorted-list buffer, entries (power of two, 64..2048) */
+} ksj_gpu_gridding_tuning;
+
+/* Workspace bytes ksj_gpu_gridding_adjoint needs for `desc` (0 on a bad desc). */
+KSJ_GPU_API size_t ksj_gpu_gridding_workspace_bytes(const ksj_gpu_gridding_desc* desc);
+
+/* Adjoint gridding reconstruction of `frames` independent frames.
+ *   d_kspace  [frame][channel][sample] samples (channel-major, ksj.noncartesian-kspace-frame per frame)
+ *   d_traj    [frame][sample][2] float32, (k_row, k_col) in radians per pixel (ksj.trajectory-frame)
+ *   d_dcf     [frame][sample] float32 for KSJ_GPU_DCF_EXTERNAL, else ignored (may be NULL)
+ *   d_out     per desc->output
+ *   d_workspace >= ksj_gpu_gridding_workspace_bytes(desc) bytes, 256-byte aligned; its
+ *               contents need not be initialised and are overwritten.
+ * Asynchronous on `stream`.  Input checks run on the device; read them with
+ * ksj_gpu_read_flags() after the stream has completed.
+ * Deterministic: repeated calls on the same inputs give byte-identical output. */
+KSJ_GPU_API ksj_gpu_status ksj_gpu_gridding_adjoint(const ksj_gpu_gridding_desc* desc,
+                                                    const ksj_gpu_gridding_tuning* tuning, const void* d_kspace,
+                                                    const float* d_traj, const float* d_dcf, void* d_out,
+                                                    void* d_workspace, size_t workspace_bytes, void* stream);
+
+/* The sorted binning lists of the last call that used `d_workspace`, copied to
+ * host memory: for every frame, list (grid_row, column_chunk) in row-major
+ * order, the sample indices that touch it in increasing order.  out_offsets
+ * receives frames * lists + 1 entries (lists = grid_rows * chunks), out_samples
+ * the concatenated indices.  Pass NULL arrays to query the sizes. */
+KSJ_GPU_API ksj_gpu_status ksj_gpu_gridding_binning(const ksj_gpu_gridding_desc* desc,
+                                                    const ksj_gpu_gridding_tuning* tuning, const void* d_workspace,
+                                                    uint32_t* out_chunk_width, uint64_t* out_list_count,
+                                                    uint64_t* out_entry_count, uint64_t* out_offsets,
+                                                    uint32_t* out_samples);
+
+/* Device-side check flags (KSJ_GPU_FLAG_*) of the last call that used
+ * `d_workspace`.  Synchronises `stream`. */
+KSJ_GPU_API ksj_gpu_status ksj_gpu_read_flags(const void* d_workspace, void* stream, uint32_t* out_flags);
+
+/* Fill `tuning` with the autotuner's choice for `desc`: every admissible
+ * (coil_group, column_block) pair is timed with CUDA events on `stream`, the
+ * fastest kept and cached per shape for the life of the process.  The buffers
+ * are those a real call would use. */
+KSJ_GPU_API ksj_gpu_status ksj_gpu_gridding_tune(const ksj_gpu_gridding_desc* desc, const void* d_kspace,
+                                                 const float* d_traj, const float* d_dcf, void* d_out,
+                                                 void* d_workspace, size_t workspace_bytes, void* stream,
+                                                 ksj_gpu_gridding_tuning* tuning);
+
+/* ----------------------------------------------------------- direct NUDFT */
+
+/* Exact direct adjoint NUDFT, no DCF:
+ *   img(c)(r, col) = sum_s y(c)(s) exp(i (k_row,s (r - row_origin) + k_col,s (col - col_origin)))
+ * d_kspace [channel][sample] complex64, d_traj [sample][2], d_out coil-last
+ * complex64 [row][col][channel].  Workspace: ksj_gpu_direct_workspace_bytes. */
+KSJ_GPU_API size_t ksj_gpu_direct_workspace_bytes(uint32_t rows, uint32_t cols, uint32_t channels);
+KSJ_GPU_API ksj_gpu_status ksj_gpu_direct_adjoint(uint32_t rows, uint32_t cols, double row_origin, double col_origin,
+                                                  uint32_t channels, uint32_t samples, const void* d_kspace,
+                                                  const float* d_traj, void* d_out, void* d_workspace,
+                                                  size_t workspace_bytes, void* stream);
+
+/* --------------------------------------------------------------- combine */
+
+/* Root-sum-of-squares over the channel (last) axis:
+ *   d_out[p] = sqrt(sum_c re^2 + im^2), summed in channel order in float32,
+ * d_coil_last complex64 [pixels][channels] -> d_out float32 [pixels]. */
+KSJ_GPU_API ksj_gpu_status ksj_gpu_rss_coil_last(uint64_t pixels, uint32_t channels, const void* d_coil_last,
+                                                 float* d_out, void* stream);
+
+/* --------------------------------------------------------------- context */
+
+/* A device, a non-blocking stream and a grow-only device workspace; used by
+ * the Provider plug-ins.  Not thread-safe: one context per serial instance. */
+typedef struct ksj_gpu_context ksj_gpu_context;
+
+KSJ_GPU_API ksj_gpu_status ksj_gpu_context_create(int device, ksj_gpu_context** out_context);
+KSJ_GPU_API void ksj_gpu_context_destroy(ksj_gpu_context* context);
+KSJ_GPU_API void* ksj_gpu_context_stream(ksj_gpu_context* context);
+/* Ensure `bytes` of device memory, keyed by `slot` (0..7); returns the pointer. */
+KSJ_GPU_API ksj_gpu_status ksj_gpu_context_buffer(ksj_gpu_context* context, uint32_t slot, size_t bytes,
+                                                  void** out_pointer);
+/* Host staging: pinned host memory, keyed by slot (0..3). */
+KSJ_GPU_API ksj_gpu_status ksj_gpu_context_pinned(ksj_gpu_context* context, uint32_t slot, size_t bytes,
+                                                  void** out_pointer);
+/* Async copies on the context stream (kind: 0 host->device, 1 device->host). */
+KSJ_GPU_API ksj_gpu_status ksj_gpu_context_copy(ksj_gpu_context* context, void* dst, const void* src, size_t bytes,
+                                                int kind);
+KSJ_GPU_API ksj_gpu_status ksj_gpu_context_sync(ksj_gpu_context* context);
+/* Total device bytes and streams the context holds (the Provider declares them). */
+KSJ_GPU_API uint64_t ksj_gpu_context_device_bytes(const ksj_gpu_context* context);
+
+/* Human-readable status text (static storage). */
+KSJ_GPU_API const char* ksj_gpu_status_string(ksj_gpu_status status);
+/* Number of kernel launches this process issued through the library. */
+KSJ_GPU_API uint64_t ksj_gpu_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* KSJ_GPU_H_ */

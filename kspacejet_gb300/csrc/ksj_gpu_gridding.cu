@@ -1,0 +1,1038 @@
+// ksj_gpu_gridding.cu -- adjoint gridding reconstruction on sm_103a.
+//
+// One call reconstructs `frames` independent frames of `channels` coils:
+//
+//   k_tables   quarter-turn-reduced FFT twiddles, FP64 Kaiser-Bessel
+//              deapodisation factors (per call, tiny)
+//   k_prepare  per (frame, sample): error-free grid coordinate, taps and
+//              weights (linear or Kaiser-Bessel), accurately reduced origin
+//              phase times the DCF, and a count per binning list
+//   k_scan     per frame: exclusive scan of the list counts
+//   k_scatter  per (frame, sample): append the sample to each list it touches
+//   k_sort     per list (one warp): sort by sample index, so every cell later
+//              accumulates in sample order -- the reference's order -- and the
+//              result is deterministic whatever order the scatter produced
+//   k_samples_coil_last  [frame][coil][sample] -> [frame][sample][coil], so a
+//              warp reads one sample's coils as one coalesced segment
+//   k_rows     per (frame, grid row, coil group): each warp owns one
+//              32-column chunk of the row and its sorted list and accumulates
+//              lane-per-coil into shared memory with no atomics (a cell is
+//              only ever touched by its owning warp, in list order); the block
+//              then runs the row inverse FFT in shared memory and writes only
+//              the columns the image keeps
+//   k_cols     per (frame, column block): column inverse FFT per coil in
+//              shared memory, crop, deapodise, then write coil images or
+//              accumulate the RSS over coils in channel order
+//   k_coil_last  coil-major -> coil-last transpose for the reference layout
+//
+// Binning lists are (frame, grid row, 32-column chunk); a sample is listed
+// once per row its stencil covers and per chunk its W columns fall into
+// (one or two).  The "reference permutation" a list must equal is the
+// increasing sequence of sample indices whose stencil touches that row and
+// chunk, with the lower tap index floor(k N / 2 pi) of the exact coordinate
+// (the value the reference's double-precision grid_coordinate computes,
+// eigen_radial_gridding.cpp:262-277).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <mutex>
+#include <map>
+#include <tuple>
+#include <vector>
+
+#include "ksj_gpu.h"
+#include "ksj_gpu_internal.cuh"
+
+namespace ksj_gpu {
+namespace {
+
+constexpr int kChunk = 32;        // grid columns per binning list
+constexpr int kMaxWidth = 8;      // largest Kaiser-Bessel width
+constexpr int kMaxGrid = 512;
+constexpr int kEmax = 8;          // complex values per thread per FFT stage
+constexpr int kMaxThreads = 512;
+constexpr uint32_t kFlagBytes = 256;
+
+// Per (frame, sample) record written by k_prepare, read by k_rows.
+template <int W>
+struct alignas(16) SampleRecord {
+  int r0;        // first tap row (wrapped)
+  int c0;        // first tap column (wrapped)
+  float2 scale;  // dcf * exp(i * origin phase)
+  float wr[W];
+  float wc[W];
+};
+
+struct Shape {
+  int frames, channels, samples;
+  int rows, cols;          // image
+  int grid_rows, grid_cols;
+  int width;
+  int nchunks;             // ceil(grid_cols / 32)
+  int lists_per_frame;     // grid_rows * nchunks
+  size_t entries_per_frame;
+  int out_rows, out_cols;  // kept image region
+  bool kb;
+  float beta, inv_i0_beta;
+  float row_origin, col_origin;
+  float phase_row, phase_col, phase_sign;  // origin-phase coefficients
+  int coil_group, column_block, list_capacity;
+  FftPlan plan_rows, plan_cols;
+};
+
+struct Layout {
+  size_t flags, records, counts, cursor, offsets, entries, samples_t, inter, coil_major, tables, total;
+};
+
+size_t record_bytes(int width) {
+  switch (width) {
+    case 2: return sizeof(SampleRecord<2>);
+    case 4: return sizeof(SampleRecord<4>);
+    case 6: return sizeof(SampleRecord<6>);
+    default: return sizeof(SampleRecord<8>);
+  }
+}
+
+bool is_fft_size(uint32_t n) {
+  FftPlan p;
+  return n >= 2 && n <= kMaxGrid && make_fft_plan(static_cast<int>(n), &p);
+}
+
+ksj_gpu_status make_shape(const ksj_gpu_gridding_desc* d, const ksj_gpu_gridding_tuning* t, Shape* s) {
+  if (d == nullptr || d->struct_size < sizeof(ksj_gpu_gridding_desc)) return KSJ_GPU_ERROR_INVALID_ARGUMENT;
+  if (d->channels == 0 || d->samples == 0 || d->frames == 0 || d->image_rows < 2 || d->image_cols < 2)
+    return KSJ_GPU_ERROR_INVALID_ARGUMENT;
+  if (d->dcf_mode > KSJ_GPU_DCF_EXTERNAL || d->output > KSJ_GPU_OUTPUT_COIL_MAJOR ||
+      d->sample_format > KSJ_GPU_SAMPLES_BF16)
+    return KSJ_GPU_ERROR_INVALID_ARGUMENT;
+  if (!std::isfinite(d->row_origin) || !std::isfinite(d->col_origin)) return KSJ_GPU_ERROR_INVALID_ARGUMENT;
+  if (d->samples > (1u << 26) || d->channels > 4096 || d->frames > 65535) return KSJ_GPU_ERROR_UNSUPPORTED;
+  s->kb = d->kernel == KSJ_GPU_KERNEL_KAISER_BESSEL;
+  if (d->kernel == KSJ_GPU_KERNEL_LINEAR) {
+    if (d->kernel_width != 2 || d->grid_rows != d->image_rows || d->grid_cols != d->image_cols)
+      return KSJ_GPU_ERROR_INVALID_ARGUMENT;
+  } else if (s->kb) {
+    if (d->kernel_width < 2 || d->kernel_width > kMaxWidth || (d->kernel_width & 1u) != 0)
+      return KSJ_GPU_ERROR_INVALID_ARGUMENT;
+    if (d->grid_rows < d->image_rows || d->grid_cols < d->image_cols || d->grid_rows < d->kernel_width ||
+        d->grid_cols < d->kernel_width)
+      return KSJ_GPU_ERROR_INVALID_ARGUMENT;
+  } else {
+    return KSJ_GPU_ERROR_INVALID_ARGUMENT;
+  }
+  if (!is_fft_size(d->grid_rows) || !is_fft_size(d->grid_cols)) return KSJ_GPU_ERROR_UNSUPPORTED;
+  s->frames = static_cast<int>(d->frames);
+  s->channels = static_cast<int>(d->channels);
+  s->samples = static_cast<int>(d->samples);
+  s->rows = static_cast<int>(d->image_rows);
+  s->cols = static_cast<int>(d->image_cols);
+  s->grid_rows = static_cast<int>(d->grid_rows);
+  s->grid_cols = static_cast<int>(d->grid_cols);
+  s->width = static_cast<int>(d->kernel_width);
+  s->nchunks = (s->grid_cols + kChunk - 1) / kChunk;
+  s->lists_per_frame = s->grid_rows * s->nchunks;
+  s->entries_per_frame = static_cast<size_t>(s->samples) * s->width * 2;
+  s->out_rows = s->rows;
+  s->out_cols = s->cols;
+  s->row_origin = static_cast<float>(d->row_origin);
+  s->col_origin = static_cast<float>(d->col_origin);
+  if (s->kb) {
+    const double sigma = static_cast<double>(d->grid_rows) / static_cast<double>(d->image_rows);
+    double beta = d->kb_beta;
+    if (!(beta > 0.0)) {
+      const double a = (static_cast<double>(d->kernel_width) / sigma) * (sigma - 0.5);
+      const double arg = a * a - 0.8;
+      if (arg <= 0.0) return KSJ_GPU_ERROR_INVALID_ARGUMENT;
+      beta = 3.14159265358979323846 * std::sqrt(arg);
+    }
+    s->beta = static_cast<float>(beta);
+    s->inv_i0_beta = static_cast<float>(1.0 / std::cyl_bessel_i(0.0, beta));
+    // exp(i k (q + delta)), delta = n/2 - origin: the image is centred on
+    // offsets q = p - n/2 so the deapodisation sees |q| <= n/2.
+    s->phase_row = static_cast<float>(static_cast<double>(s->rows / 2) - d->row_origin);
+    s->phase_col = static_cast<float>(static_cast<double>(s->cols / 2) - d->col_origin);
+    s->phase_sign = 1.0f;
+    if (static_cast<double>(s->phase_row) != static_cast<double>(s->rows / 2) - d->row_origin ||
+        static_cast<double>(s->phase_col) != static_cast<double>(s->cols / 2) - d->col_origin)
+      return KSJ_GPU_ERROR_UNSUPPORTED;
+  } else {
+    s->beta = 0.0f;
+    s->inv_i0_beta = 0.0f;
+    // exp(-i (k_r r0 + k_c c0)) (eigen_radial_gridding.cpp:330-334)
+    s->phase_row = s->row_origin;
+    s->phase_col = s->col_origin;
+    s->phase_sign = -1.0f;
+    if (static_cast<double>(s->row_origin) != d->row_origin || static_cast<double>(s->col_origin) != d->col_origin)
+      return KSJ_GPU_ERROR_UNSUPPORTED;  // origins must be exact floats (the reference casts them, :320-321)
+  }
+  make_fft_plan(s->grid_rows, &s->plan_rows);
+  make_fft_plan(s->grid_cols, &s->plan_cols);
+
+  // tuning
+  int cg = t && t->coil_group ? static_cast<int>(t->coil_group) : 0;
+  int cb = t && t->column_block ? static_cast<int>(t->column_block) : 0;
+  int cap = t && t->list_capacity ? static_cast<int>(t->list_capacity) : 0;
+  if (cap == 0) cap = 512;
+  if (cap < 64 || cap > 2048 || (cap & (cap - 1)) != 0) return KSJ_GPU_ERROR_INVALID_ARGUMENT;
+  const size_t smem_limit = 200 * 1024;
+  auto rows_smem = [&](int g) {
+    return static_cast<size_t>(s->grid_cols) * g * sizeof(float2) + static_cast<size_t>(s->grid_cols) * sizeof(float2);
+  };
+  if (cg == 0) {
+    int want = 1;
+    while (want < s->channels && want < 32) want <<= 1;
+    cg = want;
+    while (cg > 1 && rows_smem(cg) > 110 * 1024) cg >>= 1;
+  }
+  if (cg < 1 || cg > 32 || (cg & (cg - 1)) != 0 || rows_smem(cg) > smem_limit) return KSJ_GPU_ERROR_INVALID_ARGUMENT;
+  if (cb == 0) {
+    cb = 16;
+    while (cb > 4 && static_cast<long>(s->grid_rows) * cb > static_cast<long>(kEmax) * kMaxThreads) cb >>= 1;
+  }
+  if (cb < 4 || cb > 32 || (cb & (cb - 1)) != 0) return KSJ_GPU_ERROR_INVALID_ARGUMENT;
+  if (static_cast<long>(s->grid_rows) * cb > static_cast<long>(kEmax) * kMaxThreads) return KSJ_GPU_ERROR_INVALID_ARGUMENT;
+  s->coil_group = cg;
+  s->column_block = cb;
+  s->list_capacity = cap;
+  return KSJ_GPU_OK;
+}
+
+size_t sample_bytes(uint32_t format) { return format == KSJ_GPU_SAMPLES_BF16 ? 4 : 8; }
+
+Layout make_layout(const Shape& s, const ksj_gpu_gridding_desc* d) {
+  Layout l{};
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    const size_t at = off;
+    off = align_up(off + bytes, 256);
+    return at;
+  };
+  const size_t fm = static_cast<size_t>(s.frames) * s.samples;
+  const size_t nl = static_cast<size_t>(s.frames) * s.lists_per_frame;
+  l.flags = take(kFlagBytes);
+  l.records = take(fm * record_bytes(s.width));
+  l.counts = take(nl * 4);
+  l.cursor = take(nl * 4);
+  l.offsets = take((nl + s.frames) * 4);
+  l.entries = take(static_cast<size_t>(s.frames) * s.entries_per_frame * 4);
+  l.samples_t = take(fm * s.channels * sample_bytes(d->sample_format));
+  l.inter = take(static_cast<size_t>(s.frames) * s.channels * s.grid_rows * s.out_cols * sizeof(float2));
+  l.coil_major = d->output == KSJ_GPU_OUTPUT_COIL_LAST
+                     ? take(static_cast<size_t>(s.frames) * s.channels * s.out_rows * s.out_cols * sizeof(float2))
+                     : off;
+  // tables: twiddles for rows and cols, inverse deapodisation for rows and cols
+  l.tables = take((static_cast<size_t>(s.grid_rows) + s.grid_cols) * sizeof(float2) +
+                  (static_cast<size_t>(s.out_rows) + s.out_cols) * sizeof(float));
+  l.total = off;
+  return l;
+}
+
+// ------------------------------------------------------------------ kernels
+
+// Twiddles exp(2 pi i t / n) for both axes and the inverse deapodisation
+// factors 1 / psi(q), q = p - n/2, psi the continuous Fourier transform of the
+// normalised Kaiser-Bessel kernel: W sinh(z)/z / I0(beta),
+// z = sqrt(beta^2 - (pi W q / g)^2) (Jackson et al. 1991).  FP64 here only.
+__global__ void k_tables(float2* tw_rows, int grid_rows, float2* tw_cols, int grid_cols, float* inv_dr, int out_rows,
+                         float* inv_dc, int out_cols, int kb, int width, double beta, double i0_beta) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < grid_rows) tw_rows[i] = twiddle(i, grid_rows);
+  if (i < grid_cols) tw_cols[i] = twiddle(i, grid_cols);
+  auto inv_psi = [&](int p, int n, int g) -> float {
+    if (!kb) return 1.0f;
+    const double q = static_cast<double>(p - n / 2);
+    const double a = 3.14159265358979323846 * width * q / g;
+    const double z2 = beta * beta - a * a;
+    double shape;
+    if (z2 > 1e-12) {
+      const double z = sqrt(z2);
+      shape = sinh(z) / z;
+    } else if (z2 < -1e-12) {
+      const double z = sqrt(-z2);
+      shape = sin(z) / z;
+    } else {
+      shape = 1.0;
+    }
+    return static_cast<float>(i0_beta / (width * shape));
+  };
+  if (i < out_rows) inv_dr[i] = inv_psi(i, out_rows, grid_rows);
+  if (i < out_cols) inv_dc[i] = inv_psi(i, out_cols, grid_cols);
+}
+
+struct PrepareArgs {
+  const float* traj;
+  const float* dcf;
+  uint32_t dcf_mode;
+  uint32_t require_nyquist;
+  unsigned char* records;
+  uint32_t* counts;
+  uint32_t* flags;
+  int frames, samples, grid_rows, grid_cols, nchunks, lists_per_frame;
+  int kb;
+  float beta, two_over_w, inv_i0_beta;
+  float phase_row, phase_col, phase_sign;
+};
+
+template <int W>
+__device__ __forceinline__ void list_chunks(int c0, int grid_cols, int* k0, int* k1) {
+  const int last = c0 + W - 1 >= grid_cols ? c0 + W - 1 - grid_cols : c0 + W - 1;
+  *k0 = c0 / kChunk;
+  *k1 = last / kChunk;
+}
+
+template <int W>
+__global__ void __launch_bounds__(256) k_prepare(PrepareArgs a) {
+  const size_t idx = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  const size_t total = static_cast<size_t>(a.frames) * a.samples;
+  if (idx >= total) return;
+  const int f = static_cast<int>(idx / a.samples);
+  const float2 k = __ldg(reinterpret_cast<const float2*>(a.traj) + idx);
+  bool ok = isfinite(k.x) && isfinite(k.y);
+  if (ok && a.require_nyquist) ok = k.x >= -kPiF && k.x <= kPiF && k.y >= -kPiF && k.y <= kPiF;
+  // a coordinate far outside the grid would overflow the int tap arithmetic
+  if (ok && !a.require_nyquist) ok = fabsf(k.x) < 1.0e4f && fabsf(k.y) < 1.0e4f;
+  float w = 1.0f;
+  if (a.dcf_mode == KSJ_GPU_DCF_ANALYTIC_RAMP) {
+    w = hypotf(k.x, k.y);
+  } else if (a.dcf_mode == KSJ_GPU_DCF_EXTERNAL) {
+    w = __ldg(a.dcf + idx);
+    if (!(isfinite(w) && w >= 0.0f)) {
+      atomicOr(a.flags, KSJ_GPU_FLAG_BAD_DCF);
+      w = 0.0f;
+    }
+  }
+  SampleRecord<W> rec;
+  if (!ok) {
+    atomicOr(a.flags, KSJ_GPU_FLAG_BAD_TRAJECTORY);
+    rec.r0 = 0;
+    rec.c0 = 0;
+    rec.scale = make_float2(0.0f, 0.0f);
+#pragma unroll
+    for (int j = 0; j < W; ++j) {
+      rec.wr[j] = 0.0f;
+      rec.wc[j] = 0.0f;
+    }
+  } else {
+    const dfloat ur = grid_coordinate(k.x, static_cast<float>(a.grid_rows));
+    const dfloat uc = grid_coordinate(k.y, static_cast<float>(a.grid_cols));
+    float fr, fc;
+    const int lr = dfloor(ur, &fr);
+    const int lc = dfloor(uc, &fc);
+    if (!a.kb) {
+      // periodic 2x2 linear stencil (eigen_radial_gridding.cpp:325-342)
+      rec.r0 = wrap_index(lr, a.grid_rows);
+      rec.c0 = wrap_index(lc, a.grid_cols);
+      rec.wr[0] = 1.0f - fr;
+      rec.wr[1] = fr;
+      rec.wc[0] = 1.0f - fc;
+      rec.wc[1] = fc;
+#pragma unroll
+      for (int j = 2; j < W; ++j) {
+        rec.wr[j] = 0.0f;
+        rec.wc[j] = 0.0f;
+      }
+    } else {
+      const int sr = lr - W / 2 + 1;
+      const int sc = lc - W / 2 + 1;
+      rec.r0 = wrap_index(sr, a.grid_rows);
+      rec.c0 = wrap_index(sc, a.grid_cols);
+#pragma unroll
+      for (int j = 0; j < W; ++j) {
+        // offset (tap - u), exact in its high part
+        const float dr = __fsub_rn(__fsub_rn(static_cast<float>(sr + j), ur.hi), ur.lo);
+        const float dc = __fsub_rn(__fsub_rn(static_cast<float>(sc + j), uc.hi), uc.lo);
+        rec.wr[j] = kb_weight(dr, a.two_over_w, a.beta, a.inv_i0_beta);
+        rec.wc[j] = kb_weight(dc, a.two_over_w, a.beta, a.inv_i0_beta);
+      }
+    }
+    const float2 e = exp_i_dot(k.x, a.phase_row, k.y, a.phase_col, a.phase_sign);
+    rec.scale = cscale(e, w);
+  }
+  reinterpret_cast<SampleRecord<W>*>(a.records)[idx] = rec;
+  int k0, k1;
+  list_chunks<W>(rec.c0, a.grid_cols, &k0, &k1);
+  uint32_t* counts = a.counts + static_cast<size_t>(f) * a.lists_per_frame;
+#pragma unroll
+  for (int j = 0; j < W; ++j) {
+    int row = rec.r0 + j;
+    if (row >= a.grid_rows) row -= a.grid_rows;
+    atomicAdd(counts + row * a.nchunks + k0, 1u);
+    if (k1 != k0) atomicAdd(counts + row * a.nchunks + k1, 1u);
+  }
+}
+
+// Exclusive scan of one frame's list counts (one block per frame).
+__global__ void __launch_bounds__(1024) k_scan(const uint32_t* counts, uint32_t* offsets, int lists) {
+  __shared__ uint32_t warp_sums[32];
+  const int f = blockIdx.x;
+  const uint32_t* c = counts + static_cast<size_t>(f) * lists;
+  uint32_t* o = offsets + static_cast<size_t>(f) * (lists + 1);
+  const int per = (lists + blockDim.x - 1) / blockDim.x;
+  const int begin = threadIdx.x * per;
+  const int end = min(begin + per, lists);
+  uint32_t local = 0;
+  for (int i = begin; i < end; ++i) local += c[i];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t incl = local;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const uint32_t v = __shfl_up_sync(0xffffffffu, incl, d);
+    if (lane >= d) incl += v;
+  }
+  if (lane == 31) warp_sums[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    const int nw = blockDim.x >> 5;
+    uint32_t ws = lane < nw ? warp_sums[lane] : 0u;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint32_t v = __shfl_up_sync(0xffffffffu, ws, d);
+      if (lane >= d) ws += v;
+    }
+    if (lane < nw) warp_sums[lane] = ws;
+  }
+  __syncthreads();
+  uint32_t run = incl - local + (warp > 0 ? warp_sums[warp - 1] : 0u);
+  for (int i = begin; i < end; ++i) {
+    o[i] = run;
+    run += c[i];
+  }
+  if (threadIdx.x == blockDim.x - 1) o[lists] = run;
+}
+
+template <int W>
+__global__ void __launch_bounds__(256) k_scatter(const unsigned char* records, const uint32_t* offsets,
+                                                 uint32_t* cursor, uint32_t* entries, int frames, int samples,
+                                                 int grid_rows, int grid_cols, int nchunks, size_t entries_per_frame) {
+  const size_t idx = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (idx >= static_cast<size_t>(frames) * samples) return;
+  const int f = static_cast<int>(idx / samples);
+  const int s = static_cast<int>(idx - static_cast<size_t>(f) * samples);
+  const SampleRecord<W>* rec = reinterpret_cast<const SampleRecord<W>*>(records) + idx;
+  const int r0 = rec->r0, c0 = rec->c0;
+  int k0, k1;
+  list_chunks<W>(c0, grid_cols, &k0, &k1);
+  const int lists = grid_rows * nchunks;
+  const uint32_t* off = offsets + static_cast<size_t>(f) * (lists + 1);
+  uint32_t* cur = cursor + static_cast<size_t>(f) * lists;
+  uint32_t* ent = entries + static_cast<size_t>(f) * entries_per_frame;
+#pragma unroll
+  for (int j = 0; j < W; ++j) {
+    int row = r0 + j;
+    if (row >= grid_rows) row -= grid_rows;
+    const int l0 = row * nchunks + k0;
+    ent[off[l0] + atomicAdd(cur + l0, 1u)] = static_cast<uint32_t>(s);
+    if (k1 != k0) {
+      const int l1 = row * nchunks + k1;
+      ent[off[l1] + atomicAdd(cur + l1, 1u)] = static_cast<uint32_t>(s);
+    }
+  }
+}
+
+// Warp-cooperative ascending sort of buf[0, n) (shared or global memory):
+// the bitonic network in its all-ascending form (first comparator of each
+// merge flipped), so positions >= n behave as +infinity and are never
+// touched -- no padding is needed.
+__device__ __forceinline__ void warp_sort(uint32_t* buf, int n, int lane) {
+  int p = 1;
+  while (p < n) p <<= 1;
+  for (int k = 2; k <= p; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int i = lane; i < p; i += 32) {
+        const int partner = (j == (k >> 1)) ? (i ^ (k - 1)) : (i ^ j);
+        if (partner > i && partner < n) {
+          const uint32_t a = buf[i], b = buf[partner];
+          if (a > b) {
+            buf[i] = b;
+            buf[partner] = a;
+          }
+        }
+      }
+      __syncwarp();
+    }
+  }
+}
+
+// One warp per list: sort its sample indices ascending, in shared memory
+// when the list fits the per-warp buffer, in place in global memory otherwise.
+__global__ void __launch_bounds__(256) k_sort(const uint32_t* offsets, uint32_t* entries, int frames,
+                                              int lists_per_frame, size_t entries_per_frame, int capacity) {
+  extern __shared__ uint32_t sort_buf[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const size_t gl = static_cast<size_t>(blockIdx.x) * (blockDim.x >> 5) + warp;
+  if (gl >= static_cast<size_t>(frames) * lists_per_frame) return;
+  const int f = static_cast<int>(gl / lists_per_frame);
+  const int l = static_cast<int>(gl - static_cast<size_t>(f) * lists_per_frame);
+  const uint32_t* off = offsets + static_cast<size_t>(f) * (lists_per_frame + 1);
+  const uint32_t begin = off[l];
+  const int n = static_cast<int>(off[l + 1] - begin);
+  if (n < 2) return;
+  uint32_t* ent = entries + static_cast<size_t>(f) * entries_per_frame + begin;
+  if (n <= capacity) {
+    uint32_t* buf = sort_buf + static_cast<size_t>(warp) * capacity;
+    for (int i = lane; i < n; i += 32) buf[i] = ent[i];
+    __syncwarp();
+    warp_sort(buf, n, lane);
+    for (int i = lane; i < n; i += 32) ent[i] = buf[i];
+  } else {
+    warp_sort(ent, n, lane);
+  }
+}
+
+struct RowsArgs {
+  const void* samples_t;  // [frame][sample][channel]
+  const unsigned char* records;
+  const uint32_t* offsets;
+  const uint32_t* entries;
+  const float2* tw_cols;
+  float2* inter;
+  uint32_t* flags;
+  int frames, channels, samples, grid_rows, grid_cols, nchunks, lists_per_frame;
+  size_t entries_per_frame;
+  int coil_group;
+  int out_cols, kb, image_cols;
+  FftPlan plan;
+};
+
+// Accumulator layout [column][coil] with the coil index XOR-swizzled by the
+// column so that both a warp of consecutive coils at one column (gridding,
+// FFT) and a warp of consecutive columns for one coil (write-out) hit
+// distinct banks.
+struct AccAddr {
+  int cg;
+  __device__ __forceinline__ int operator()(int coil, int col) const { return col * cg + (coil ^ (col & (cg - 1))); }
+};
+
+template <int W, uint32_t kFormat>
+__global__ void __launch_bounds__(kMaxThreads) k_rows(RowsArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int row = blockIdx.x;
+  const int cgi = blockIdx.y;
+  const int f = blockIdx.z;
+  const int cg = a.coil_group;
+  const int tid = threadIdx.x;
+  const int nthreads = blockDim.x;
+  const int lane = tid & 31;
+  const int warp = tid >> 5;
+  float2* acc = reinterpret_cast<float2*>(smem_raw);
+  float2* tw = acc + static_cast<size_t>(a.grid_cols) * cg;
+  const AccAddr addr{cg};
+
+  for (int i = tid; i < a.grid_cols * cg; i += nthreads) acc[i] = make_float2(0.0f, 0.0f);
+  for (int i = tid; i < a.grid_cols; i += nthreads) tw[i] = a.tw_cols[i];
+  __syncthreads();
+
+  // ---- gridding: warp `warp` owns columns [32*warp, 32*warp + 32)
+  if (warp < a.nchunks) {
+    const int list = row * a.nchunks + warp;
+    const uint32_t* off = a.offsets + static_cast<size_t>(f) * (a.lists_per_frame + 1);
+    const uint32_t begin = off[list];
+    const int n = static_cast<int>(off[list + 1] - begin);
+    const uint32_t* ent = a.entries + static_cast<size_t>(f) * a.entries_per_frame + begin;
+    const int col_lo = warp * kChunk;
+    const int col_hi = min(col_lo + kChunk, a.grid_cols);
+    const SampleRecord<W>* recs =
+        reinterpret_cast<const SampleRecord<W>*>(a.records) + static_cast<size_t>(f) * a.samples;
+    // lanes: coil = lane % cgp, tap group = lane / cgp
+    int cgp = 1;
+    while (cgp < cg) cgp <<= 1;
+    const int ngroups = 32 / cgp;
+    const int my_coil = lane % cgp;
+    const int my_group = lane / cgp;
+    const int coil_global = cgi * cg + my_coil;
+    const bool coil_ok = my_coil < cg && coil_global < a.channels;
+    const size_t sample_base = static_cast<size_t>(f) * a.samples * a.channels + (coil_ok ? coil_global : 0);
+    bool bad = false;
+    for (int base = 0; base < n; base += 32) {
+      const uint32_t mine = base + lane < n ? __ldg(ent + base + lane) : 0u;
+      const int cnt = min(32, n - base);
+      for (int i = 0; i < cnt; ++i) {
+        const uint32_t s = __shfl_sync(0xffffffffu, mine, i);
+        const SampleRecord<W>& r = recs[s];
+        int ta = row - r.r0;
+        if (ta < 0) ta += a.grid_rows;
+        const float wr = r.wr[ta];
+        if (coil_ok) {
+          const float2 y = load_sample<kFormat>(a.samples_t, sample_base + static_cast<size_t>(s) * a.channels);
+          bad |= !(isfinite(y.x) && isfinite(y.y));
+          const float2 v = cmul(y, r.scale);
+#pragma unroll
+          for (int j = 0; j < W; ++j) {
+            if (j % ngroups != my_group) continue;
+            int col = r.c0 + j;
+            if (col >= a.grid_cols) col -= a.grid_cols;
+            if (col >= col_lo && col < col_hi) {
+              const float wt = wr * r.wc[j];
+              float2* cell = acc + addr(my_coil, col);
+              float2 c = *cell;
+              c.x = fmaf(v.x, wt, c.x);
+              c.y = fmaf(v.y, wt, c.y);
+              *cell = c;
+            }
+          }
+        }
+        __syncwarp();
+      }
+    }
+    if (bad) atomicOr(a.flags, KSJ_GPU_FLAG_NONFINITE_SAMPLE);
+  }
+  __syncthreads();
+
+  // ---- row inverse FFT of every coil line, in place, in batches of lines
+  {
+    int lg_batch = ilog2(max(1, min(cg, kEmax * nthreads / a.grid_cols)));
+    const int batch = 1 << lg_batch;
+    for (int l0 = 0; l0 < cg; l0 += batch) {
+      struct Shifted {
+        AccAddr base;
+        int l0;
+        __device__ __forceinline__ int operator()(int l, int i) const { return base(l + l0, i); }
+      } shifted{addr, l0};
+      fft_lines<kEmax>(acc, shifted, a.plan, lg_batch, tw, tid, nthreads);
+    }
+  }
+
+  // ---- write the kept columns: [frame][coil][grid_row][out_col]
+  const int coils_here = min(cg, a.channels - cgi * cg);
+  for (int i = tid; i < coils_here * a.out_cols; i += nthreads) {
+    const int c = i / a.out_cols;
+    const int pc = i - c * a.out_cols;
+    int src = pc;
+    if (a.kb) {
+      src = pc - a.image_cols / 2;
+      if (src < 0) src += a.grid_cols;
+    }
+    const size_t o = ((static_cast<size_t>(f) * a.channels + cgi * cg + c) * a.grid_rows + row) * a.out_cols + pc;
+    a.inter[o] = acc[addr(c, src)];
+  }
+}
+
+struct ColsArgs {
+  const float2* inter;
+  const float2* tw_rows;
+  const float* inv_dr;
+  const float* inv_dc;
+  void* out;
+  int frames, channels, grid_rows, out_rows, out_cols, column_block, kb, image_rows;
+  uint32_t output;  // RSS or COIL_MAJOR (COIL_LAST goes through COIL_MAJOR + transpose)
+  FftPlan plan;
+};
+
+struct TileAddr {
+  int pitch;
+  __device__ __forceinline__ int operator()(int line, int index) const { return index * pitch + line; }
+};
+
+template <int kOutPerThread>
+__global__ void __launch_bounds__(kMaxThreads) k_cols(ColsArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int cb = a.column_block;
+  const int col0 = blockIdx.x * cb;
+  const int f = blockIdx.y;
+  const int tid = threadIdx.x;
+  const int nthreads = blockDim.x;
+  float2* tile = reinterpret_cast<float2*>(smem_raw);
+  float2* tw = tile + static_cast<size_t>(a.grid_rows) * cb;
+  const TileAddr addr{cb};
+  for (int i = tid; i < a.grid_rows; i += nthreads) tw[i] = a.tw_rows[i];
+  const int ncols = min(cb, a.out_cols - col0);
+  const int nout = a.out_rows * cb;
+  float rss[kOutPerThread];
+#pragma unroll
+  for (int k = 0; k < kOutPerThread; ++k) rss[k] = 0.0f;
+
+  for (int c = 0; c < a.channels; ++c) {
+    const float2* src = a.inter + (static_cast<size_t>(f) * a.channels + c) * a.grid_rows * a.out_cols;
+    __syncthreads();
+    for (int i = tid; i < a.grid_rows * cb; i += nthreads) {
+      const int r = i / cb;
+      const int l = i - r * cb;
+      tile[i] = l < ncols ? src[static_cast<size_t>(r) * a.out_cols + col0 + l] : make_float2(0.0f, 0.0f);
+    }
+    __syncthreads();
+    fft_lines<kEmax>(tile, addr, a.plan, ilog2(cb), tw, tid, nthreads);
+#pragma unroll
+    for (int k = 0; k < kOutPerThread; ++k) {
+      const int i = tid + k * nthreads;
+      if (i < nout) {
+        const int pr = i / cb;
+        const int l = i - pr * cb;
+        if (l < ncols) {
+          int sr = pr;
+          if (a.kb) {
+            sr = pr - a.image_rows / 2;
+            if (sr < 0) sr += a.grid_rows;
+          }
+          float2 x = tile[sr * cb + l];
+          if (a.kb) {
+            const float sc = a.inv_dr[pr] * a.inv_dc[col0 + l];
+            x.x *= sc;
+            x.y *= sc;
+          }
+          if (a.output == KSJ_GPU_OUTPUT_RSS) {
+            // channel-order float sum of re^2 + im^2 (reductions.hpp:972-982)
+            rss[k] = __fadd_rn(rss[k], __fadd_rn(__fmul_rn(x.x, x.x), __fmul_rn(x.y, x.y)));
+          } else {
+            float2* o = static_cast<float2*>(a.out);
+            o[((static_cast<size_t>(f) * a.channels + c) * a.out_rows + pr) * a.out_cols + col0 + l] = x;
+          }
+        }
+      }
+    }
+  }
+  if (a.output == KSJ_GPU_OUTPUT_RSS) {
+    float* o = static_cast<float*>(a.out);
+#pragma unroll
+    for (int k = 0; k < kOutPerThread; ++k) {
+      const int i = tid + k * nthreads;
+      if (i < nout) {
+        const int pr = i / cb;
+        const int l = i - pr * cb;
+        if (l < ncols) o[(static_cast<size_t>(f) * a.out_rows + pr) * a.out_cols + col0 + l] = __fsqrt_rn(rss[k]);
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------------ driver
+
+size_t rows_smem_bytes(const Shape& s) {
+  return static_cast<size_t>(s.grid_cols) * s.coil_group * sizeof(float2) + s.grid_cols * sizeof(float2);
+}
+
+size_t cols_smem_bytes(const Shape& s) {
+  return static_cast<size_t>(s.grid_rows) * s.column_block * sizeof(float2) + s.grid_rows * sizeof(float2);
+}
+
+int cols_threads(const Shape& s) {
+  const int elems = s.grid_rows * s.column_block;
+  int t = (elems + kEmax - 1) / kEmax;
+  t = (t + 31) / 32 * 32;
+  return std::max(64, std::min(kMaxThreads, t));
+}
+
+template <int W, uint32_t kFormat>
+ksj_gpu_status launch_all(const Shape& s, const Layout& l, const ksj_gpu_gridding_desc* d, const void* d_kspace,
+                          const float* d_traj, const float* d_dcf, void* d_out, unsigned char* ws,
+                          cudaStream_t stream) {
+  uint32_t* flags = reinterpret_cast<uint32_t*>(ws + l.flags);
+  unsigned char* records = ws + l.records;
+  uint32_t* counts = reinterpret_cast<uint32_t*>(ws + l.counts);
+  uint32_t* cursor = reinterpret_cast<uint32_t*>(ws + l.cursor);
+  uint32_t* offsets = reinterpret_cast<uint32_t*>(ws + l.offsets);
+  uint32_t* entries = reinterpret_cast<uint32_t*>(ws + l.entries);
+  float2* inter = reinterpret_cast<float2*>(ws + l.inter);
+  float2* tw_rows = reinterpret_cast<float2*>(ws + l.tables);
+  float2* tw_cols = tw_rows + s.grid_rows;
+  float* inv_dr = reinterpret_cast<float*>(tw_cols + s.grid_cols);
+  float* inv_dc = inv_dr + s.out_rows;
+  const size_t nl = static_cast<size_t>(s.frames) * s.lists_per_frame;
+
+  if (cudaMemsetAsync(flags, 0, kFlagBytes, stream) != cudaSuccess) return KSJ_GPU_ERROR_CUDA;
+  if (cudaMemsetAsync(counts, 0, nl * 4, stream) != cudaSuccess) return KSJ_GPU_ERROR_CUDA;
+  if (cudaMemsetAsync(cursor, 0, nl * 4, stream) != cudaSuccess) return KSJ_GPU_ERROR_CUDA;
+
+  {
+    const int n = std::max(std::max(s.grid_rows, s.grid_cols), std::max(s.out_rows, s.out_cols));
+    const double beta = s.beta;
+    k_tables<<<(n + 255) / 256, 256, 0, stream>>>(tw_rows, s.grid_rows, tw_cols, s.grid_cols, inv_dr, s.out_rows,
+                                                  inv_dc, s.out_cols, s.kb ? 1 : 0, s.width, beta,
+                                                  s.kb ? std::cyl_bessel_i(0.0, beta) : 1.0);
+    count_launch();
+  }
+  const size_t fm = static_cast<size_t>(s.frames) * s.samples;
+  {
+    PrepareArgs p{};
+    p.traj = d_traj;
+    p.dcf = d_dcf;
+    p.dcf_mode = d->dcf_mode;
+    p.require_nyquist = d->require_nyquist;
+    p.records = records;
+    p.counts = counts;
+    p.flags = flags;
+    p.frames = s.frames;
+    p.samples = s.samples;
+    p.grid_rows = s.grid_rows;
+    p.grid_cols = s.grid_cols;
+    p.nchunks = s.nchunks;
+    p.lists_per_frame = s.lists_per_frame;
+    p.kb = s.kb ? 1 : 0;
+    p.beta = s.beta;
+    p.two_over_w = 2.0f / static_cast<float>(s.width);
+    p.inv_i0_beta = s.inv_i0_beta;
+    p.phase_row = s.phase_row;
+    p.phase_col = s.phase_col;
+    p.phase_sign = s.phase_sign;
+    k_prepare<W><<<static_cast<unsigned>((fm + 255) / 256), 256, 0, stream>>>(p);
+    count_launch();
+  }
+  k_scan<<<s.frames, 1024, 0, stream>>>(counts, offsets, s.lists_per_frame);
+  count_launch();
+  k_scatter<W><<<static_cast<unsigned>((fm + 255) / 256), 256, 0, stream>>>(
+      records, offsets, cursor, entries, s.frames, s.samples, s.grid_rows, s.grid_cols, s.nchunks,
+      s.entries_per_frame);
+  count_launch();
+  {
+    const size_t smem = static_cast<size_t>(8) * s.list_capacity * 4;
+    if (cudaFuncSetAttribute(k_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)) !=
+        cudaSuccess)
+      return KSJ_GPU_ERROR_CUDA;
+    k_sort<<<static_cast<unsigned>((nl + 7) / 8), 256, smem, stream>>>(offsets, entries, s.frames,
+                                                                        s.lists_per_frame, s.entries_per_frame,
+                                                                        s.list_capacity);
+    count_launch();
+  }
+  {
+    const dim3 tg((s.samples + 31) / 32, (s.channels + 31) / 32, s.frames);
+    if (kFormat == KSJ_GPU_SAMPLES_BF16)
+      k_transpose<uint32_t><<<tg, dim3(32, 8), 0, stream>>>(static_cast<const uint32_t*>(d_kspace),
+                                                            reinterpret_cast<uint32_t*>(ws + l.samples_t),
+                                                            s.channels, s.samples);
+    else
+      k_transpose<unsigned long long><<<tg, dim3(32, 8), 0, stream>>>(
+          static_cast<const unsigned long long*>(d_kspace), reinterpret_cast<unsigned long long*>(ws + l.samples_t),
+          s.channels, s.samples);
+    count_launch();
+  }
+  {
+    RowsArgs r{};
+    r.samples_t = ws + l.samples_t;
+    r.records = records;
+    r.offsets = offsets;
+    r.entries = entries;
+    r.tw_cols = tw_cols;
+    r.inter = inter;
+    r.flags = flags;
+    r.frames = s.frames;
+    r.channels = s.channels;
+    r.samples = s.samples;
+    r.grid_rows = s.grid_rows;
+    r.grid_cols = s.grid_cols;
+    r.nchunks = s.nchunks;
+    r.lists_per_frame = s.lists_per_frame;
+    r.entries_per_frame = s.entries_per_frame;
+    r.coil_group = s.coil_group;
+    r.out_cols = s.out_cols;
+    r.kb = s.kb ? 1 : 0;
+    r.image_cols = s.cols;
+    r.plan = s.plan_cols;
+    const size_t smem = rows_smem_bytes(s);
+    auto kern = k_rows<W, kFormat>;
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)) !=
+        cudaSuccess)
+      return KSJ_GPU_ERROR_CUDA;
+    const dim3 grid(s.grid_rows, (s.channels + s.coil_group - 1) / s.coil_group, s.frames);
+    const int threads = std::max(64, s.nchunks * 32);
+    kern<<<grid, threads, smem, stream>>>(r);
+    count_launch();
+  }
+  {
+    ColsArgs c{};
+    c.inter = inter;
+    c.tw_rows = tw_rows;
+    c.inv_dr = inv_dr;
+    c.inv_dc = inv_dc;
+    c.frames = s.frames;
+    c.channels = s.channels;
+    c.grid_rows = s.grid_rows;
+    c.out_rows = s.out_rows;
+    c.out_cols = s.out_cols;
+    c.column_block = s.column_block;
+    c.kb = s.kb ? 1 : 0;
+    c.image_rows = s.rows;
+    c.plan = s.plan_rows;
+    const bool coil_last = d->output == KSJ_GPU_OUTPUT_COIL_LAST;
+    c.output = d->output == KSJ_GPU_OUTPUT_RSS ? KSJ_GPU_OUTPUT_RSS : KSJ_GPU_OUTPUT_COIL_MAJOR;
+    c.out = coil_last ? static_cast<void*>(ws + l.coil_major) : d_out;
+    const int threads = cols_threads(s);
+    const int per = (s.out_rows * s.column_block + threads - 1) / threads;
+    const size_t smem = cols_smem_bytes(s);
+    const dim3 grid((s.out_cols + s.column_block - 1) / s.column_block, s.frames);
+    auto pick = [&](auto kern) -> ksj_gpu_status {
+      if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)) !=
+          cudaSuccess)
+        return KSJ_GPU_ERROR_CUDA;
+      kern<<<grid, threads, smem, stream>>>(c);
+      count_launch();
+      return KSJ_GPU_OK;
+    };
+    ksj_gpu_status st;
+    if (per <= 4) st = pick(k_cols<4>);
+    else if (per <= 8) st = pick(k_cols<8>);
+    else if (per <= 16) st = pick(k_cols<16>);
+    else return KSJ_GPU_ERROR_UNSUPPORTED;
+    if (st != KSJ_GPU_OK) return st;
+    if (coil_last) {
+      const int pixels = s.out_rows * s.out_cols;
+      const dim3 tg((pixels + 31) / 32, (s.channels + 31) / 32, s.frames);
+      k_transpose<unsigned long long><<<tg, dim3(32, 8), 0, stream>>>(
+          reinterpret_cast<const unsigned long long*>(ws + l.coil_major), static_cast<unsigned long long*>(d_out),
+          s.channels, pixels);
+      count_launch();
+    }
+  }
+  return check_launch();
+}
+
+template <int W>
+ksj_gpu_status dispatch_format(const Shape& s, const Layout& l, const ksj_gpu_gridding_desc* d, const void* k,
+                               const float* t, const float* w, void* o, unsigned char* ws, cudaStream_t st) {
+  if (d->sample_format == KSJ_GPU_SAMPLES_BF16) return launch_all<W, KSJ_GPU_SAMPLES_BF16>(s, l, d, k, t, w, o, ws, st);
+  return launch_all<W, KSJ_GPU_SAMPLES_CF32>(s, l, d, k, t, w, o, ws, st);
+}
+
+}  // namespace
+}  // namespace ksj_gpu
+
+using namespace ksj_gpu;
+
+extern "C" size_t ksj_gpu_gridding_workspace_bytes(const ksj_gpu_gridding_desc* desc) {
+  Shape s{};
+  if (make_shape(desc, nullptr, &s) != KSJ_GPU_OK) return 0;
+  return make_layout(s, desc).total;
+}
+
+extern "C" ksj_gpu_status ksj_gpu_gridding_adjoint(const ksj_gpu_gridding_desc* desc,
+                                                   const ksj_gpu_gridding_tuning* tuning, const void* d_kspace,
+                                                   const float* d_traj, const float* d_dcf, void* d_out,
+                                                   void* d_workspace, size_t workspace_bytes, void* stream) {
+  Shape s{};
+  const ksj_gpu_status st = make_shape(desc, tuning, &s);
+  if (st != KSJ_GPU_OK) return st;
+  if (d_kspace == nullptr || d_traj == nullptr || d_out == nullptr) return KSJ_GPU_ERROR_INVALID_ARGUMENT;
+  if (desc->dcf_mode == KSJ_GPU_DCF_EXTERNAL && d_dcf == nullptr) return KSJ_GPU_ERROR_INVALID_ARGUMENT;
+  const Layout l = make_layout(s, desc);
+  if (d_workspace == nullptr || (reinterpret_cast<uintptr_t>(d_workspace) & 255u) != 0 || workspace_bytes < l.total)
+    return KSJ_GPU_ERROR_WORKSPACE;
+  if ((reinterpret_cast<uintptr_t>(d_kspace) & (sample_bytes(desc->sample_format) - 1)) != 0 ||
+      (reinterpret_cast<uintptr_t>(d_traj) & 7u) != 0 || (reinterpret_cast<uintptr_t>(d_out) & 7u) != 0)
+    return KSJ_GPU_ERROR_INVALID_ARGUMENT;
+  unsigned char* ws = static_cast<unsigned char*>(d_workspace);
+  cudaStream_t cs = static_cast<cudaStream_t>(stream);
+  switch (s.width) {
+    case 2: return dispatch_format<2>(s, l, desc, d_kspace, d_traj, d_dcf, d_out, ws, cs);
+    case 4: return dispatch_format<4>(s, l, desc, d_kspace, d_traj, d_dcf, d_out, ws, cs);
+    case 6: return dispatch_format<6>(s, l, desc, d_kspace, d_traj, d_dcf, d_out, ws, cs);
+    case 8: return dispatch_format<8>(s, l, desc, d_kspace, d_traj, d_dcf, d_out, ws, cs);
+    default: return KSJ_GPU_ERROR_UNSUPPORTED;
+  }
+}
+
+extern "C" ksj_gpu_status ksj_gpu_gridding_binning(const ksj_gpu_gridding_desc* desc,
+                                                   const ksj_gpu_gridding_tuning* tuning, const void* d_workspace,
+                                                   uint32_t* out_chunk_width, uint64_t* out_list_count,
+                                                   uint64_t* out_entry_count, uint64_t* out_offsets,
+                                                   uint32_t* out_samples) {
+  Shape s{};
+  const ksj_gpu_status st = make_shape(desc, tuning, &s);
+  if (st != KSJ_GPU_OK) return st;
+  if (d_workspace == nullptr) return KSJ_GPU_ERROR_WORKSPACE;
+  const Layout l = make_layout(s, desc);
+  const unsigned char* ws = static_cast<const unsigned char*>(d_workspace);
+  const size_t lists = static_cast<size_t>(s.frames) * s.lists_per_frame;
+  if (out_chunk_width) *out_chunk_width = kChunk;
+  if (out_list_count) *out_list_count = lists;
+  std::vector<uint32_t> off(static_cast<size_t>(s.frames) * (s.lists_per_frame + 1));
+  if (cudaDeviceSynchronize() != cudaSuccess) return KSJ_GPU_ERROR_CUDA;
+  if (cudaMemcpy(off.data(), ws + l.offsets, off.size() * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
+    return KSJ_GPU_ERROR_CUDA;
+  uint64_t total = 0;
+  for (int f = 0; f < s.frames; ++f) total += off[static_cast<size_t>(f) * (s.lists_per_frame + 1) + s.lists_per_frame];
+  if (out_entry_count) *out_entry_count = total;
+  if (out_offsets == nullptr || out_samples == nullptr) return KSJ_GPU_OK;
+  uint64_t base = 0;
+  for (int f = 0; f < s.frames; ++f) {
+    const uint32_t* fo = off.data() + static_cast<size_t>(f) * (s.lists_per_frame + 1);
+    for (int i = 0; i < s.lists_per_frame; ++i)
+      out_offsets[static_cast<size_t>(f) * s.lists_per_frame + i] = base + fo[i];
+    const uint32_t n = fo[s.lists_per_frame];
+    if (n && cudaMemcpy(out_samples + base, ws + l.entries + static_cast<size_t>(f) * s.entries_per_frame * 4,
+                        static_cast<size_t>(n) * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
+      return KSJ_GPU_ERROR_CUDA;
+    base += n;
+  }
+  out_offsets[lists] = base;
+  return KSJ_GPU_OK;
+}
+
+extern "C" ksj_gpu_status ksj_gpu_read_flags(const void* d_workspace, void* stream, uint32_t* out_flags) {
+  if (d_workspace == nullptr || out_flags == nullptr) return KSJ_GPU_ERROR_INVALID_ARGUMENT;
+  cudaStream_t cs = static_cast<cudaStream_t>(stream);
+  if (cudaStreamSynchronize(cs) != cudaSuccess) return KSJ_GPU_ERROR_CUDA;
+  if (cudaMemcpy(out_flags, d_workspace, sizeof(uint32_t), cudaMemcpyDeviceToHost) != cudaSuccess)
+    return KSJ_GPU_ERROR_CUDA;
+  return KSJ_GPU_OK;
+}
+
+namespace {
+std::mutex g_tune_mutex;
+std::map<std::tuple<uint32_t, uint32_t, uint32_t, uint32_t, uint32_t, uint32_t, uint32_t, uint32_t, uint32_t,
+                    uint32_t, uint32_t>,
+         ksj_gpu_gridding_tuning>
+    g_tune_cache;
+}  // namespace
+
+extern "C" ksj_gpu_status ksj_gpu_gridding_tune(const ksj_gpu_gridding_desc* desc, const void* d_kspace,
+                                                const float* d_traj, const float* d_dcf, void* d_out,
+                                                void* d_workspace, size_t workspace_bytes, void* stream,
+                                                ksj_gpu_gridding_tuning* tuning) {
+  if (desc == nullptr || tuning == nullptr) return KSJ_GPU_ERROR_INVALID_ARGUMENT;
+  const auto key = std::make_tuple(desc->kernel, desc->image_rows, desc->image_cols, desc->grid_rows,
+                                   desc->grid_cols, desc->kernel_width, desc->channels, desc->samples, desc->frames,
+                                   desc->output, desc->sample_format);
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    const auto it = g_tune_cache.find(key);
+    if (it != g_tune_cache.end()) {
+      *tuning = it->second;
+      return KSJ_GPU_OK;
+    }
+  }
+  cudaStream_t cs = static_cast<cudaStream_t>(stream);
+  cudaEvent_t e0, e1;
+  if (cudaEventCreate(&e0) != cudaSuccess) return KSJ_GPU_ERROR_CUDA;
+  if (cudaEventCreate(&e1) != cudaSuccess) {
+    cudaEventDestroy(e0);
+    return KSJ_GPU_ERROR_CUDA;
+  }
+  ksj_gpu_gridding_tuning best{};
+  float best_ms = 1e30f;
+  for (uint32_t cg : {32u, 16u, 8u, 4u, 2u, 1u}) {
+    if (cg > 1 && cg / 2 >= desc->channels) continue;
+    for (uint32_t cb : {8u, 16u, 32u}) {
+      ksj_gpu_gridding_tuning t{};
+      t.struct_size = sizeof(t);
+      t.coil_group = cg;
+      t.column_block = cb;
+      Shape s{};
+      if (make_shape(desc, &t, &s) != KSJ_GPU_OK) continue;
+      if (workspace_bytes < make_layout(s, desc).total) continue;
+      if (ksj_gpu_gridding_adjoint(desc, &t, d_kspace, d_traj, d_dcf, d_out, d_workspace, workspace_bytes, stream) !=
+          KSJ_GPU_OK)
+        continue;
+      cudaEventRecord(e0, cs);
+      for (int rep = 0; rep < 2; ++rep)
+        ksj_gpu_gridding_adjoint(desc, &t, d_kspace, d_traj, d_dcf, d_out, d_workspace, workspace_bytes, stream);
+      cudaEventRecord(e1, cs);
+      if (cudaEventSynchronize(e1) != cudaSuccess) break;
+      float ms = 0.0f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (ms < best_ms) {
+        best_ms = ms;
+        best = t;
+      }
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (best.struct_size == 0) return KSJ_GPU_ERROR_UNSUPPORTED;
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    g_tune_cache[key] = best;
+  }
+  *tuning = best;
+  return KSJ_GPU_OK;
+}

@@ -1,0 +1,349 @@
+// ksj_gpu_internal.cuh -- device building blocks shared by the sm_103a kernels
+// of the non-Cartesian path: float2 complex arithmetic, error-free-transform
+// grid coordinates and origin phases, the Kaiser-Bessel tap weight, and an
+// in-place mixed-radix (2/3/4/8) Stockham FFT over lines held in shared
+// memory.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "ksj_gpu.h"
+
+namespace ksj_gpu {
+
+// ------------------------------------------------------------------ launches
+
+void count_launch();                 // increments the library launch counter
+ksj_gpu_status check_launch();       // cudaGetLastError -> status
+
+inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+// ------------------------------------------------------------------- complex
+
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+__device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+__device__ __forceinline__ float2 cmul_i(float2 a) { return make_float2(-a.y, a.x); }  // a * i
+
+// ------------------------------------------------- error-free transformations
+
+// A float pair hi + lo carrying about 46 significant bits.
+struct dfloat {
+  float hi, lo;
+};
+
+__device__ __forceinline__ dfloat two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return {s, e};
+}
+
+__device__ __forceinline__ dfloat fast_two_sum(float a, float b) {  // |a| >= |b|
+  const float s = __fadd_rn(a, b);
+  return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+
+// fl32(2 pi) and the remainder 2 pi - fl32(2 pi).
+constexpr float kTwoPiHi = 6.2831854820251465f;
+constexpr float kTwoPiLo = -1.7484555314695172e-07f;
+// Three-part Cody-Waite split of 2 pi: C1 has 8 significant bits, so n * C1
+// is exact for |n| < 2^16; C1 + C2 + C3 = 2 pi to about 2^-60.
+constexpr float kCw1 = 6.28125f;
+constexpr float kCw2 = 0.0019353071693331003f;
+constexpr float kCw3 = 1.0253376273028358e-11f;
+constexpr float kInvTwoPi = 0.15915493667125702f;
+constexpr float kPiF = 3.14159265358979323846f;
+
+// The real number f * n / (2 pi) (f, n float; n an exact integer) to about
+// 2^-46 relative error.  The reference evaluates fl(fl(f*n) / fl(2 pi)) in
+// float (eigen_radial_gridding.cpp:264), whose ~1e-7 relative error moves the
+// linear weights by up to 3e-5 on a 512 grid; here the product error is kept
+// with an FMA, the quotient remainder is exact (p - q*C for q = fl(p/C)), and
+// the low part of 2 pi enters the correction term.
+__device__ __forceinline__ dfloat grid_coordinate(float f, float n) {
+  const float p = __fmul_rn(f, n);
+  const float pe = __fmaf_rn(f, n, -p);
+  const float q = __fdiv_rn(p, kTwoPiHi);
+  const float r = __fmaf_rn(-q, kTwoPiHi, p);
+  const float num = __fmaf_rn(-q, kTwoPiLo, __fadd_rn(r, pe));
+  return fast_two_sum(q, __fdiv_rn(num, kTwoPiHi));
+}
+
+// floor of hi + lo, and the fractional part in [0, 1).
+__device__ __forceinline__ int dfloor(dfloat x, float* frac) {
+  float l = floorf(x.hi);
+  float f;
+  if (l == x.hi) {
+    if (x.lo < 0.0f) {
+      l -= 1.0f;
+      f = __fadd_rn(1.0f, x.lo);
+    } else {
+      f = x.lo;
+    }
+  } else {
+    f = __fadd_rn(__fsub_rn(x.hi, l), x.lo);
+  }
+  if (f >= 1.0f) {
+    l += 1.0f;
+    f = 0.0f;
+  }
+  *frac = f;
+  return static_cast<int>(l);
+}
+
+__device__ __forceinline__ int wrap_index(int i, int n) {
+  int r = i % n;
+  return r < 0 ? r + n : r;
+}
+
+// exp(i * sign * (a1*b1 + a2*b2)) for float a, b with |a1 b1 + a2 b2| < 2^14:
+// exact products and sum (FMA error terms, two-sum), Cody-Waite reduction by
+// 2 pi (Cody & Waite 1980) with the low parts added after the exact first
+// step, then sincosf of an argument in [-pi - 0.5, pi + 0.5].  The reference
+// rounds the whole phase to float before cos/sin (eigen_radial_gridding.cpp:
+// 330-334), an absolute error up to 6e-5 rad on a 512 grid.
+__device__ __forceinline__ float2 exp_i_dot(float a1, float b1, float a2, float b2, float sign) {
+  const float p1 = __fmul_rn(a1, b1);
+  const float e1 = __fmaf_rn(a1, b1, -p1);
+  const float p2 = __fmul_rn(a2, b2);
+  const float e2 = __fmaf_rn(a2, b2, -p2);
+  const dfloat s = two_sum(p1, p2);
+  const float lo = __fadd_rn(s.lo, __fadd_rn(e1, e2));
+  const float n = rintf(__fmul_rn(s.hi, kInvTwoPi));
+  float r = __fmaf_rn(-n, kCw1, s.hi);
+  r = __fmaf_rn(-n, kCw2, r);
+  r = __fmaf_rn(-n, kCw3, r);
+  r = __fadd_rn(r, lo);
+  float sn, cs;
+  sincosf(sign * r, &sn, &cs);
+  return make_float2(cs, sn);
+}
+
+// Kaiser-Bessel tap weight at offset d (grid cells), normalised to 1 at d = 0:
+// I0(beta sqrt(1 - (2d/W)^2)) / I0(beta).
+__device__ __forceinline__ float kb_weight(float d, float two_over_w, float beta, float inv_i0_beta) {
+  const float t = d * two_over_w;
+  const float a = fmaxf(fmaf(-t, t, 1.0f), 0.0f);
+  return cyl_bessel_i0f(beta * sqrtf(a)) * inv_i0_beta;
+}
+
+// ----------------------------------------------------------------- bfloat16
+
+__device__ __forceinline__ float bf16_to_float(uint16_t h) { return __uint_as_float(static_cast<uint32_t>(h) << 16); }
+
+template <uint32_t kFormat>
+__device__ __forceinline__ float2 load_sample(const void* base, size_t index);
+
+template <>
+__device__ __forceinline__ float2 load_sample<KSJ_GPU_SAMPLES_CF32>(const void* base, size_t index) {
+  return __ldg(static_cast<const float2*>(base) + index);
+}
+
+template <>
+__device__ __forceinline__ float2 load_sample<KSJ_GPU_SAMPLES_BF16>(const void* base, size_t index) {
+  const uint32_t packed = __ldg(static_cast<const uint32_t*>(base) + index);
+  return make_float2(bf16_to_float(static_cast<uint16_t>(packed & 0xffffu)),
+                     bf16_to_float(static_cast<uint16_t>(packed >> 16)));
+}
+
+// -------------------------------------------------------------------- FFT
+
+// In-place R-point inverse DFT (exp(+2 pi i j k / R)) on registers.
+template <int R>
+__device__ __forceinline__ void dft_inverse(float2* v);
+
+template <>
+__device__ __forceinline__ void dft_inverse<2>(float2* v) {
+  const float2 a = v[0], b = v[1];
+  v[0] = cadd(a, b);
+  v[1] = csub(a, b);
+}
+
+template <>
+__device__ __forceinline__ void dft_inverse<3>(float2* v) {
+  constexpr float kS3 = 0.8660254037844386f;  // sin(2 pi / 3)
+  const float2 t1 = cadd(v[1], v[2]);
+  const float2 t2 = make_float2(fmaf(-0.5f, t1.x, v[0].x), fmaf(-0.5f, t1.y, v[0].y));
+  const float2 t3 = cscale(csub(v[1], v[2]), kS3);
+  v[0] = cadd(v[0], t1);
+  v[1] = make_float2(t2.x - t3.y, t2.y + t3.x);
+  v[2] = make_float2(t2.x + t3.y, t2.y - t3.x);
+}
+
+template <>
+__device__ __forceinline__ void dft_inverse<4>(float2* v) {
+  const float2 a = cadd(v[0], v[2]), b = csub(v[0], v[2]);
+  const float2 c = cadd(v[1], v[3]), d = cmul_i(csub(v[1], v[3]));
+  v[0] = cadd(a, c);
+  v[2] = csub(a, c);
+  v[1] = cadd(b, d);
+  v[3] = csub(b, d);
+}
+
+template <>
+__device__ __forceinline__ void dft_inverse<8>(float2* v) {
+  constexpr float kC = 0.70710678118654752f;
+  float2 e[4] = {v[0], v[2], v[4], v[6]};
+  float2 o[4] = {v[1], v[3], v[5], v[7]};
+  dft_inverse<4>(e);
+  dft_inverse<4>(o);
+  // o[k] *= exp(2 pi i k / 8)
+  o[1] = make_float2((o[1].x - o[1].y) * kC, (o[1].x + o[1].y) * kC);
+  o[2] = cmul_i(o[2]);
+  o[3] = make_float2(-(o[3].x + o[3].y) * kC, (o[3].x - o[3].y) * kC);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    v[k] = cadd(e[k], o[k]);
+    v[k + 4] = csub(e[k], o[k]);
+  }
+}
+
+// A radix plan for n = 2^a 3^b (b <= 1): radices in execution order.
+struct FftPlan {
+  int n;
+  int stages;
+  int radix[12];
+};
+
+inline bool make_fft_plan(int n, FftPlan* plan) {
+  if (n < 2 || n > 4096) return false;
+  int m = n, threes = 0;
+  while (m % 3 == 0) {
+    m /= 3;
+    ++threes;
+  }
+  if (threes > 1 || (m & (m - 1)) != 0) return false;
+  plan->n = n;
+  plan->stages = 0;
+  while (m >= 8) {
+    plan->radix[plan->stages++] = 8;
+    m /= 8;
+  }
+  if (m == 4) plan->radix[plan->stages++] = 4;
+  if (m == 2) plan->radix[plan->stages++] = 2;
+  if (threes) plan->radix[plan->stages++] = 3;
+  return true;
+}
+
+// One Stockham stage over `nlines` = 2^lg_lines lines of length n held in
+// shared memory; element (line, index) lives at smem[addr(line, index)].
+// Threads map line-fastest so that a warp touches consecutive lines of one
+// index (the layouts below put those in distinct banks).  Every thread first
+// loads all of its butterflies' inputs, the block synchronises, then all
+// outputs are stored: the stage is in place with one buffer.  The plan puts
+// the radix-3 stage last, so the span ns = 2^lg_ns is always a power of two.
+// Requires n * nlines <= kEmax * nthreads.
+template <int R, int kEmax, class Addr>
+__device__ __forceinline__ void fft_stage(float2* smem, const Addr& addr, int n, int lg_lines, int lg_ns,
+                                          const float2* __restrict__ tw, int tid, int nthreads) {
+  constexpr int K = (kEmax + R - 1) / R;
+  const int nbf = n / R;
+  const int total = nbf << lg_lines;
+  const int lmask = (1 << lg_lines) - 1;
+  float2 v[K][R];
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    const int t = tid + k * nthreads;
+    if (t < total) {
+      const int l = t & lmask;
+      const int j = t >> lg_lines;
+#pragma unroll
+      for (int r = 0; r < R; ++r) v[k][r] = smem[addr(l, j + r * nbf)];
+    }
+  }
+  __syncthreads();
+  const int ns = 1 << lg_ns;
+  const int step = nbf >> lg_ns;  // n / (ns * R)
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    const int t = tid + k * nthreads;
+    if (t < total) {
+      const int l = t & lmask;
+      const int j = t >> lg_lines;
+      const int kk = j & (ns - 1);
+      if (lg_ns > 0) {
+#pragma unroll
+        for (int r = 1; r < R; ++r) v[k][r] = cmul(v[k][r], tw[r * kk * step]);
+      }
+      dft_inverse<R>(v[k]);
+      const int dst = ((j >> lg_ns) << lg_ns) * R + kk;
+#pragma unroll
+      for (int r = 0; r < R; ++r) smem[addr(l, dst + r * ns)] = v[k][r];
+    }
+  }
+  __syncthreads();
+}
+
+// Unnormalised inverse FFT of 2^lg_lines lines (tw[t] = exp(2 pi i t / n)).
+template <int kEmax, class Addr>
+__device__ __forceinline__ void fft_lines(float2* smem, const Addr& addr, const FftPlan& plan, int lg_lines,
+                                          const float2* __restrict__ tw, int tid, int nthreads) {
+  int lg_ns = 0;
+  for (int s = 0; s < plan.stages; ++s) {
+    const int r = plan.radix[s];
+    if (r == 8) {
+      fft_stage<8, kEmax>(smem, addr, plan.n, lg_lines, lg_ns, tw, tid, nthreads);
+      lg_ns += 3;
+    } else if (r == 4) {
+      fft_stage<4, kEmax>(smem, addr, plan.n, lg_lines, lg_ns, tw, tid, nthreads);
+      lg_ns += 2;
+    } else if (r == 2) {
+      fft_stage<2, kEmax>(smem, addr, plan.n, lg_lines, lg_ns, tw, tid, nthreads);
+      lg_ns += 1;
+    } else {
+      fft_stage<3, kEmax>(smem, addr, plan.n, lg_lines, lg_ns, tw, tid, nthreads);
+    }
+  }
+}
+
+__host__ __device__ __forceinline__ int ilog2(int v) {
+  int r = 0;
+  while ((1 << (r + 1)) <= v) ++r;
+  return r;
+}
+
+// exp(2 pi i t / n) in float.  The angle is split into the nearest quarter
+// turn (an exact rotation) and a remainder pi * x with |x| <= 1/4, so the one
+// rounding of x = rem / (2n) moves the angle by at most ~5e-8 rad.
+__device__ __forceinline__ float2 twiddle(int t, int n) {
+  const int t4 = 4 * t;
+  const int q = (2 * t4 + n) / (2 * n);  // nearest quarter turn, t >= 0
+  const int rem = t4 - q * n;            // in [-n/2, n/2]
+  float s, c;
+  sincospif(static_cast<float>(rem) / static_cast<float>(2 * n), &s, &c);
+  switch (q & 3) {
+    case 0: return make_float2(c, s);
+    case 1: return make_float2(-s, c);
+    case 2: return make_float2(-c, -s);
+    default: return make_float2(s, -c);
+  }
+}
+
+// [frame][a][b] -> [frame][b][a] for 4- or 8-byte elements, 32x32 tiles
+// through shared memory (launch with blockDim (32, 8), grid (ceil(nb/32),
+// ceil(na/32), frames)).
+template <typename T>
+__global__ void __launch_bounds__(256) k_transpose(const T* in, T* out, int na, int nb) {
+  __shared__ T t[32][33];
+  const int f = blockIdx.z;
+  const int b0 = blockIdx.x * 32;
+  const int a0 = blockIdx.y * 32;
+  const T* src = in + static_cast<size_t>(f) * na * nb;
+  T* dst = out + static_cast<size_t>(f) * na * nb;
+  for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+    const int a = a0 + y, b = b0 + threadIdx.x;
+    if (a < na && b < nb) t[y][threadIdx.x] = src[static_cast<size_t>(a) * nb + b];
+  }
+  __syncthreads();
+  for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+    const int b = b0 + y, a = a0 + threadIdx.x;
+    if (a < na && b < nb) dst[static_cast<size_t>(b) * na + a] = t[threadIdx.x][y];
+  }
+}
+
+}  // namespace ksj_gpu

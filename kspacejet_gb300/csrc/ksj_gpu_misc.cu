@@ -1,0 +1,273 @@
+// ksj_gpu_misc.cu -- direct NUDFT adjoint, root-sum-of-squares combine, the
+// device context used by the Provider plug-ins, and library bookkeeping.
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdint>
+#include <cstring>
+#include <new>
+
+#include "ksj_gpu.h"
+#include "ksj_gpu_internal.cuh"
+
+namespace ksj_gpu {
+
+namespace {
+std::atomic<uint64_t> g_launches{0};
+}
+
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+ksj_gpu_status check_launch() {
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? KSJ_GPU_OK : KSJ_GPU_ERROR_CUDA;
+}
+
+namespace {
+
+// ------------------------------------------------------------- direct NUDFT
+
+constexpr int kDirectPixels = 128;  // threads (pixels) per block
+constexpr int kDirectTile = 256;    // samples staged per iteration
+constexpr int kDirectCoils = 8;     // accumulators per thread
+
+// img[c][r][col] = sum_s y[c][s] exp(i (k_r,s (r - r0) + k_c,s (col - c0))),
+// summed in sample order in float; the phase of every (pixel, sample) pair
+// is formed exactly and reduced by 2 pi before sincosf (the reference rounds
+// it to float first, eigen_nufft_direct_nudft.cpp:88-90).
+__global__ void __launch_bounds__(kDirectPixels) k_direct_adjoint(const float2* __restrict__ kspace,
+                                                                  const float2* __restrict__ traj, float2* out,
+                                                                  int rows, int cols, float row_origin,
+                                                                  float col_origin, int channels, int samples) {
+  __shared__ float2 s_traj[kDirectTile];
+  __shared__ float2 s_y[kDirectCoils][kDirectTile];
+  const int p = blockIdx.x * kDirectPixels + threadIdx.x;
+  const int c0 = blockIdx.y * kDirectCoils;
+  const int nc = min(kDirectCoils, channels - c0);
+  const bool live = p < rows * cols;
+  const int r = live ? p / cols : 0;
+  const int col = live ? p - r * cols : 0;
+  const float xr = __fsub_rn(static_cast<float>(r), row_origin);
+  const float xc = __fsub_rn(static_cast<float>(col), col_origin);
+  float2 acc[kDirectCoils];
+#pragma unroll
+  for (int c = 0; c < kDirectCoils; ++c) acc[c] = make_float2(0.0f, 0.0f);
+  for (int s0 = 0; s0 < samples; s0 += kDirectTile) {
+    const int ns = min(kDirectTile, samples - s0);
+    __syncthreads();
+    for (int i = threadIdx.x; i < ns; i += kDirectPixels) s_traj[i] = traj[s0 + i];
+    for (int i = threadIdx.x; i < ns * nc; i += kDirectPixels) {
+      const int c = i / ns, s = i - c * ns;
+      s_y[c][s] = kspace[static_cast<size_t>(c0 + c) * samples + s0 + s];
+    }
+    __syncthreads();
+    for (int s = 0; s < ns; ++s) {
+      const float2 k = s_traj[s];
+      const float2 e = exp_i_dot(k.x, xr, k.y, xc, 1.0f);
+#pragma unroll
+      for (int c = 0; c < kDirectCoils; ++c) {
+        if (c < nc) acc[c] = cadd(acc[c], cmul(s_y[c][s], e));
+      }
+    }
+  }
+  if (live) {
+#pragma unroll
+    for (int c = 0; c < kDirectCoils; ++c)
+      if (c < nc) out[static_cast<size_t>(c0 + c) * rows * cols + p] = acc[c];
+  }
+}
+
+// --------------------------------------------------------------------- RSS
+
+// out[p] = sqrt(sum_c re^2 + im^2), a float sum in channel order with every
+// product and sum rounded separately: the order and rounding points of
+// squared_norm_across + sqrt (reductions.hpp:972-982), so equal inputs give
+// bit-identical outputs.
+__global__ void __launch_bounds__(256) k_rss(const float2* __restrict__ in, float* out, uint64_t pixels,
+                                             int channels) {
+  const uint64_t p = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (p >= pixels) return;
+  const float2* v = in + p * channels;
+  float total = 0.0f;
+  for (int c = 0; c < channels; ++c) {
+    const float2 x = __ldg(v + c);
+    total = __fadd_rn(total, __fadd_rn(__fmul_rn(x.x, x.x), __fmul_rn(x.y, x.y)));
+  }
+  out[p] = __fsqrt_rn(total);
+}
+
+}  // namespace
+}  // namespace ksj_gpu
+
+using namespace ksj_gpu;
+
+extern "C" size_t ksj_gpu_direct_workspace_bytes(uint32_t rows, uint32_t cols, uint32_t channels) {
+  return align_up(static_cast<size_t>(rows) * cols * channels * sizeof(float2), 256);
+}
+
+extern "C" ksj_gpu_status ksj_gpu_direct_adjoint(uint32_t rows, uint32_t cols, double row_origin, double col_origin,
+                                                 uint32_t channels, uint32_t samples, const void* d_kspace,
+                                                 const float* d_traj, void* d_out, void* d_workspace,
+                                                 size_t workspace_bytes, void* stream) {
+  if (rows == 0 || cols == 0 || channels == 0 || samples == 0 || d_kspace == nullptr || d_traj == nullptr ||
+      d_out == nullptr)
+    return KSJ_GPU_ERROR_INVALID_ARGUMENT;
+  if (rows > 8192 || cols > 8192 || static_cast<uint64_t>(rows) * cols > (1u << 26))
+    return KSJ_GPU_ERROR_UNSUPPORTED;
+  const float ro = static_cast<float>(row_origin), co = static_cast<float>(col_origin);
+  if (static_cast<double>(ro) != row_origin || static_cast<double>(co) != col_origin)
+    return KSJ_GPU_ERROR_UNSUPPORTED;
+  if (d_workspace == nullptr || workspace_bytes < ksj_gpu_direct_workspace_bytes(rows, cols, channels) ||
+      (reinterpret_cast<uintptr_t>(d_workspace) & 255u) != 0)
+    return KSJ_GPU_ERROR_WORKSPACE;
+  cudaStream_t cs = static_cast<cudaStream_t>(stream);
+  float2* tmp = static_cast<float2*>(d_workspace);
+  const int pixels = static_cast<int>(rows * cols);
+  const dim3 grid((pixels + kDirectPixels - 1) / kDirectPixels, (channels + kDirectCoils - 1) / kDirectCoils);
+  k_direct_adjoint<<<grid, kDirectPixels, 0, cs>>>(static_cast<const float2*>(d_kspace),
+                                                   reinterpret_cast<const float2*>(d_traj), tmp,
+                                                   static_cast<int>(rows), static_cast<int>(cols), ro, co,
+                                                   static_cast<int>(channels), static_cast<int>(samples));
+  count_launch();
+  const dim3 tg((pixels + 31) / 32, (channels + 31) / 32, 1);
+  k_transpose<unsigned long long><<<tg, dim3(32, 8), 0, cs>>>(reinterpret_cast<const unsigned long long*>(tmp),
+                                                              static_cast<unsigned long long*>(d_out),
+                                                              static_cast<int>(channels), pixels);
+  count_launch();
+  return check_launch();
+}
+
+extern "C" ksj_gpu_status ksj_gpu_rss_coil_last(uint64_t pixels, uint32_t channels, const void* d_coil_last,
+                                                float* d_out, void* stream) {
+  if (pixels == 0 || channels == 0 || d_coil_last == nullptr || d_out == nullptr)
+    return KSJ_GPU_ERROR_INVALID_ARGUMENT;
+  cudaStream_t cs = static_cast<cudaStream_t>(stream);
+  k_rss<<<static_cast<unsigned>((pixels + 255) / 256), 256, 0, cs>>>(static_cast<const float2*>(d_coil_last), d_out,
+                                                                     pixels, static_cast<int>(channels));
+  count_launch();
+  return check_launch();
+}
+
+// ------------------------------------------------------------------ context
+
+struct ksj_gpu_context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  void* buffers[8] = {};
+  size_t buffer_bytes[8] = {};
+  void* pinned[4] = {};
+  size_t pinned_bytes[4] = {};
+};
+
+extern "C" ksj_gpu_status ksj_gpu_context_create(int device, ksj_gpu_context** out_context) {
+  if (out_context == nullptr) return KSJ_GPU_ERROR_INVALID_ARGUMENT;
+  *out_context = nullptr;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || device < 0 || device >= count) return KSJ_GPU_ERROR_CUDA;
+  if (cudaSetDevice(device) != cudaSuccess) return KSJ_GPU_ERROR_CUDA;
+  auto* ctx = new (std::nothrow) ksj_gpu_context{};
+  if (ctx == nullptr) return KSJ_GPU_ERROR_OUT_OF_MEMORY;
+  ctx->device = device;
+  if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete ctx;
+    return KSJ_GPU_ERROR_CUDA;
+  }
+  *out_context = ctx;
+  return KSJ_GPU_OK;
+}
+
+extern "C" void ksj_gpu_context_destroy(ksj_gpu_context* ctx) {
+  if (ctx == nullptr) return;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  for (void* b : ctx->buffers)
+    if (b) cudaFree(b);
+  for (void* b : ctx->pinned)
+    if (b) cudaFreeHost(b);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+}
+
+extern "C" void* ksj_gpu_context_stream(ksj_gpu_context* ctx) { return ctx ? ctx->stream : nullptr; }
+
+extern "C" ksj_gpu_status ksj_gpu_context_buffer(ksj_gpu_context* ctx, uint32_t slot, size_t bytes,
+                                                 void** out_pointer) {
+  if (ctx == nullptr || slot >= 8 || out_pointer == nullptr) return KSJ_GPU_ERROR_INVALID_ARGUMENT;
+  if (bytes == 0) bytes = 256;
+  if (ctx->buffer_bytes[slot] < bytes) {
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return KSJ_GPU_ERROR_CUDA;
+    if (ctx->buffers[slot]) {
+      cudaStreamSynchronize(ctx->stream);
+      cudaFree(ctx->buffers[slot]);
+      ctx->buffers[slot] = nullptr;
+      ctx->buffer_bytes[slot] = 0;
+    }
+    void* p = nullptr;
+    if (cudaMalloc(&p, bytes) != cudaSuccess) {
+      cudaGetLastError();
+      return KSJ_GPU_ERROR_OUT_OF_MEMORY;
+    }
+    ctx->buffers[slot] = p;
+    ctx->buffer_bytes[slot] = bytes;
+  }
+  *out_pointer = ctx->buffers[slot];
+  return KSJ_GPU_OK;
+}
+
+extern "C" ksj_gpu_status ksj_gpu_context_pinned(ksj_gpu_context* ctx, uint32_t slot, size_t bytes,
+                                                 void** out_pointer) {
+  if (ctx == nullptr || slot >= 4 || out_pointer == nullptr) return KSJ_GPU_ERROR_INVALID_ARGUMENT;
+  if (bytes == 0) bytes = 256;
+  if (ctx->pinned_bytes[slot] < bytes) {
+    if (ctx->pinned[slot]) {
+      cudaStreamSynchronize(ctx->stream);
+      cudaFreeHost(ctx->pinned[slot]);
+      ctx->pinned[slot] = nullptr;
+      ctx->pinned_bytes[slot] = 0;
+    }
+    void* p = nullptr;
+    if (cudaMallocHost(&p, bytes) != cudaSuccess) {
+      cudaGetLastError();
+      return KSJ_GPU_ERROR_OUT_OF_MEMORY;
+    }
+    ctx->pinned[slot] = p;
+    ctx->pinned_bytes[slot] = bytes;
+  }
+  *out_pointer = ctx->pinned[slot];
+  return KSJ_GPU_OK;
+}
+
+extern "C" ksj_gpu_status ksj_gpu_context_copy(ksj_gpu_context* ctx, void* dst, const void* src, size_t bytes,
+                                               int kind) {
+  if (ctx == nullptr || (bytes && (dst == nullptr || src == nullptr))) return KSJ_GPU_ERROR_INVALID_ARGUMENT;
+  if (bytes == 0) return KSJ_GPU_OK;
+  const cudaMemcpyKind k = kind == 0 ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost;
+  return cudaMemcpyAsync(dst, src, bytes, k, ctx->stream) == cudaSuccess ? KSJ_GPU_OK : KSJ_GPU_ERROR_CUDA;
+}
+
+extern "C" ksj_gpu_status ksj_gpu_context_sync(ksj_gpu_context* ctx) {
+  if (ctx == nullptr) return KSJ_GPU_ERROR_INVALID_ARGUMENT;
+  return cudaStreamSynchronize(ctx->stream) == cudaSuccess ? KSJ_GPU_OK : KSJ_GPU_ERROR_CUDA;
+}
+
+extern "C" uint64_t ksj_gpu_context_device_bytes(const ksj_gpu_context* ctx) {
+  if (ctx == nullptr) return 0;
+  uint64_t total = 0;
+  for (size_t b : ctx->buffer_bytes) total += b;
+  return total;
+}
+
+extern "C" const char* ksj_gpu_status_string(ksj_gpu_status status) {
+  switch (status) {
+    case KSJ_GPU_OK: return "ok";
+    case KSJ_GPU_ERROR_INVALID_ARGUMENT: return "invalid argument";
+    case KSJ_GPU_ERROR_UNSUPPORTED: return "unsupported configuration";
+    case KSJ_GPU_ERROR_CUDA: return "CUDA runtime error";
+    case KSJ_GPU_ERROR_WORKSPACE: return "workspace null, misaligned or too small";
+    case KSJ_GPU_ERROR_OUT_OF_MEMORY: return "out of memory";
+    case KSJ_GPU_ERROR_NONFINITE_INPUT: return "non-finite or out-of-range input rejected on the device";
+    default: return "unknown status";
+  }
+}
+
+extern "C" uint64_t ksj_gpu_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }

@@ -1,0 +1,225 @@
+"""ctypes bindings for ``include/ksj_gpu.h`` over torch CUDA tensors.
+
+torch provides device memory and streams only; all arithmetic happens in
+``libksj_gpu.so``.  Loading fails loudly if the library is missing.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+from dataclasses import dataclass
+
+import torch
+
+from . import GPU_LIB, NativeLibraryMissing
+
+KERNEL_LINEAR, KERNEL_KAISER_BESSEL = 0, 1
+DCF_NONE, DCF_ANALYTIC_RAMP, DCF_EXTERNAL = 0, 1, 2
+OUTPUT_COIL_LAST, OUTPUT_RSS, OUTPUT_COIL_MAJOR = 0, 1, 2
+SAMPLES_CF32, SAMPLES_BF16 = 0, 1
+FLAG_NONFINITE_SAMPLE, FLAG_BAD_TRAJECTORY, FLAG_BAD_DCF = 1, 2, 4
+
+STATUS_TEXT = {0: "ok", 1: "invalid argument", 2: "unsupported", 3: "CUDA error", 4: "workspace",
+               5: "out of memory", 6: "non-finite input"}
+
+
+class GpuError(RuntimeError):
+    def __init__(self, status: int, what: str):
+        super().__init__(f"{what}: ksj_gpu status {status} ({STATUS_TEXT.get(status, '?')})")
+        self.status = status
+
+
+class GriddingDesc(ctypes.Structure):
+    _fields_ = [("struct_size", ctypes.c_uint32), ("kernel", ctypes.c_uint32), ("image_rows", ctypes.c_uint32),
+                ("image_cols", ctypes.c_uint32), ("grid_rows", ctypes.c_uint32), ("grid_cols", ctypes.c_uint32),
+                ("kernel_width", ctypes.c_uint32), ("kb_beta", ctypes.c_float), ("row_origin", ctypes.c_double),
+                ("col_origin", ctypes.c_double), ("channels", ctypes.c_uint32), ("samples", ctypes.c_uint32),
+                ("frames", ctypes.c_uint32), ("dcf_mode", ctypes.c_uint32), ("output", ctypes.c_uint32),
+                ("sample_format", ctypes.c_uint32), ("require_nyquist", ctypes.c_uint32),
+                ("reserved0", ctypes.c_uint32)]
+
+
+class GriddingTuning(ctypes.Structure):
+    _fields_ = [("struct_size", ctypes.c_uint32), ("coil_group", ctypes.c_uint32),
+                ("column_block", ctypes.c_uint32), ("list_capacity", ctypes.c_uint32)]
+
+
+_lib = None
+
+
+def lib() -> ctypes.CDLL:
+    global _lib
+    if _lib is None:
+        if not GPU_LIB.exists():
+            raise NativeLibraryMissing(f"{GPU_LIB} is not built; run kspacejet_gb300.build()")
+        L = ctypes.CDLL(str(GPU_LIB))
+        vp, u32, u64, sz = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_size_t
+        L.ksj_gpu_gridding_workspace_bytes.restype = sz
+        L.ksj_gpu_gridding_workspace_bytes.argtypes = [ctypes.POINTER(GriddingDesc)]
+        L.ksj_gpu_gridding_adjoint.restype = ctypes.c_int32
+        L.ksj_gpu_gridding_adjoint.argtypes = [ctypes.POINTER(GriddingDesc), ctypes.POINTER(GriddingTuning), vp, vp,
+                                               vp, vp, vp, sz, vp]
+        L.ksj_gpu_gridding_binning.restype = ctypes.c_int32
+        L.ksj_gpu_gridding_binning.argtypes = [ctypes.POINTER(GriddingDesc), ctypes.POINTER(GriddingTuning), vp,
+                                               ctypes.POINTER(u32), ctypes.POINTER(u64), ctypes.POINTER(u64), vp, vp]
+        L.ksj_gpu_read_flags.restype = ctypes.c_int32
+        L.ksj_gpu_read_flags.argtypes = [vp, vp, ctypes.POINTER(u32)]
+        L.ksj_gpu_gridding_tune.restype = ctypes.c_int32
+        L.ksj_gpu_gridding_tune.argtypes = [ctypes.POINTER(GriddingDesc), vp, vp, vp, vp, vp, sz, vp,
+                                            ctypes.POINTER(GriddingTuning)]
+        L.ksj_gpu_direct_workspace_bytes.restype = sz
+        L.ksj_gpu_direct_workspace_bytes.argtypes = [u32, u32, u32]
+        L.ksj_gpu_direct_adjoint.restype = ctypes.c_int32
+        L.ksj_gpu_direct_adjoint.argtypes = [u32, u32, ctypes.c_double, ctypes.c_double, u32, u32, vp, vp, vp, vp,
+                                             sz, vp]
+        L.ksj_gpu_rss_coil_last.restype = ctypes.c_int32
+        L.ksj_gpu_rss_coil_last.argtypes = [u64, u32, vp, vp, vp]
+        L.ksj_gpu_launch_count.restype = u64
+        L.ksj_gpu_launch_count.argtypes = []
+        L.ksj_gpu_status_string.restype = ctypes.c_char_p
+        L.ksj_gpu_status_string.argtypes = [ctypes.c_int32]
+        _lib = L
+    return _lib
+
+
+def _check(status: int, what: str) -> None:
+    if status != 0:
+        raise GpuError(status, what)
+
+
+def _stream(stream: torch.cuda.Stream | None) -> int:
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return s.cuda_stream
+
+
+def launch_count() -> int:
+    return int(lib().ksj_gpu_launch_count())
+
+
+@dataclass
+class Gridding:
+    """One adjoint-gridding shape (see ``ksj_gpu_gridding_desc``)."""
+
+    image: tuple[int, int]
+    channels: int
+    samples: int
+    frames: int = 1
+    kernel: int = KERNEL_LINEAR
+    grid: tuple[int, int] | None = None
+    width: int = 2
+    beta: float = 0.0
+    origin: tuple[float, float] | None = None
+    dcf: int = DCF_ANALYTIC_RAMP
+    output: int = OUTPUT_COIL_LAST
+    sample_format: int = SAMPLES_CF32
+    require_nyquist: bool = True
+
+    def desc(self) -> GriddingDesc:
+        rows, cols = self.image
+        grid = self.grid if self.grid is not None else self.image
+        ro, co = self.origin if self.origin is not None else ((rows - 1) / 2.0, (cols - 1) / 2.0)
+        return GriddingDesc(ctypes.sizeof(GriddingDesc), self.kernel, rows, cols, grid[0], grid[1], self.width,
+                            self.beta, ro, co, self.channels, self.samples, self.frames, self.dcf, self.output,
+                            self.sample_format, int(self.require_nyquist), 0)
+
+    def workspace_bytes(self) -> int:
+        d = self.desc()
+        n = lib().ksj_gpu_gridding_workspace_bytes(ctypes.byref(d))
+        if n == 0:
+            raise GpuError(1, "gridding_workspace_bytes")
+        return int(n)
+
+    def output_shape(self) -> tuple[int, ...]:
+        rows, cols = self.image
+        if self.output == OUTPUT_RSS:
+            return (self.frames, rows, cols)
+        if self.output == OUTPUT_COIL_MAJOR:
+            return (self.frames, self.channels, rows, cols)
+        return (self.frames, rows, cols, self.channels)
+
+    def output_dtype(self) -> torch.dtype:
+        return torch.float32 if self.output == OUTPUT_RSS else torch.complex64
+
+    def new_workspace(self, device="cuda") -> torch.Tensor:
+        return torch.empty(self.workspace_bytes(), dtype=torch.uint8, device=device)
+
+    def new_output(self, device="cuda") -> torch.Tensor:
+        return torch.empty(self.output_shape(), dtype=self.output_dtype(), device=device)
+
+    def run(self, kspace: torch.Tensor, traj: torch.Tensor, out: torch.Tensor, workspace: torch.Tensor,
+            dcf: torch.Tensor | None = None, tuning: GriddingTuning | None = None,
+            stream: torch.cuda.Stream | None = None) -> None:
+        d = self.desc()
+        for t in (kspace, traj, out, workspace):
+            if not t.is_cuda or not t.is_contiguous():
+                raise ValueError("tensors must be contiguous CUDA tensors")
+        st = lib().ksj_gpu_gridding_adjoint(ctypes.byref(d), ctypes.byref(tuning) if tuning else None,
+                                            kspace.data_ptr(), traj.data_ptr(),
+                                            dcf.data_ptr() if dcf is not None else None, out.data_ptr(),
+                                            workspace.data_ptr(), workspace.numel(), _stream(stream))
+        _check(st, "gridding_adjoint")
+
+    def flags(self, workspace: torch.Tensor, stream: torch.cuda.Stream | None = None) -> int:
+        v = ctypes.c_uint32()
+        _check(lib().ksj_gpu_read_flags(workspace.data_ptr(), _stream(stream), ctypes.byref(v)), "read_flags")
+        return int(v.value)
+
+    def binning(self, workspace: torch.Tensor, tuning: GriddingTuning | None = None):
+        """(chunk_width, offsets[frames*lists+1] int64, samples uint32) of the last call."""
+        import numpy as np
+
+        d = self.desc()
+        cw, nl, ne = ctypes.c_uint32(), ctypes.c_uint64(), ctypes.c_uint64()
+        L = lib()
+        tp = ctypes.byref(tuning) if tuning else None
+        _check(L.ksj_gpu_gridding_binning(ctypes.byref(d), tp, workspace.data_ptr(), ctypes.byref(cw),
+                                          ctypes.byref(nl), ctypes.byref(ne), None, None), "binning sizes")
+        off = np.zeros(nl.value + 1, dtype=np.uint64)
+        smp = np.zeros(max(1, ne.value), dtype=np.uint32)
+        _check(L.ksj_gpu_gridding_binning(ctypes.byref(d), tp, workspace.data_ptr(), None, None, None,
+                                          off.ctypes.data, smp.ctypes.data), "binning")
+        return int(cw.value), off.astype(np.int64), smp[: ne.value]
+
+    def tune(self, kspace, traj, out, workspace, dcf=None, stream=None) -> GriddingTuning:
+        d = self.desc()
+        t = GriddingTuning()
+        _check(lib().ksj_gpu_gridding_tune(ctypes.byref(d), kspace.data_ptr(), traj.data_ptr(),
+                                           dcf.data_ptr() if dcf is not None else None, out.data_ptr(),
+                                           workspace.data_ptr(), workspace.numel(), _stream(stream),
+                                           ctypes.byref(t)), "gridding_tune")
+        return t
+
+
+def kb_gridding(image: int, grid: int, channels: int, samples: int, frames: int = 1, width: int = 4,
+                output: int = OUTPUT_RSS, dcf: int = DCF_ANALYTIC_RAMP, sample_format: int = SAMPLES_CF32) -> Gridding:
+    """Kaiser-Bessel shape: square image and grid, beta from Beatty et al. 2005."""
+    return Gridding(image=(image, image), channels=channels, samples=samples, frames=frames,
+                    kernel=KERNEL_KAISER_BESSEL, grid=(grid, grid), width=width, dcf=dcf, output=output,
+                    sample_format=sample_format, require_nyquist=False)
+
+
+def direct_adjoint(kspace: torch.Tensor, traj: torch.Tensor, rows: int, cols: int,
+                   origin: tuple[float, float] | None = None, stream=None) -> torch.Tensor:
+    """Exact direct NUDFT adjoint: kspace [C, M] complex64, traj [M, 2] -> [rows, cols, C]."""
+    c, m = kspace.shape
+    ro, co = origin if origin is not None else ((rows - 1) / 2.0, (cols - 1) / 2.0)
+    L = lib()
+    ws = torch.empty(L.ksj_gpu_direct_workspace_bytes(rows, cols, c), dtype=torch.uint8, device=kspace.device)
+    out = torch.empty((rows, cols, c), dtype=torch.complex64, device=kspace.device)
+    _check(L.ksj_gpu_direct_adjoint(rows, cols, ro, co, c, m, kspace.data_ptr(), traj.data_ptr(), out.data_ptr(),
+                                    ws.data_ptr(), ws.numel(), _stream(stream)), "direct_adjoint")
+    return out
+
+
+def rss_coil_last(coil_last: torch.Tensor, stream=None) -> torch.Tensor:
+    """[..., C] complex64 -> [...] float32 root sum of squares."""
+    c = coil_last.shape[-1]
+    p = coil_last.numel() // c
+    out = torch.empty(coil_last.shape[:-1], dtype=torch.float32, device=coil_last.device)
+    _check(lib().ksj_gpu_rss_coil_last(p, c, coil_last.data_ptr(), out.data_ptr(), _stream(stream)), "rss")
+    return out
+
+
+def kb_beta(width: int, sigma: float) -> float:
+    a = (width / sigma) * (sigma - 0.5)
+    return math.pi * math.sqrt(a * a - 0.8)
