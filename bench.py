@@ -1,0 +1,379 @@
+#!/usr/bin/env python
+"""Benchmark: gridded samples/s of batched 2-D radial adjoint reconstruction.
+
+Workload (the batched dynamic 2-D radial configuration): 96 frames x 34
+golden-angle spokes x 384 readout samples, 32 coils, complex64, moving-ellipse
+phantom (analytic k-space, linear-phase coil maps, 30 dB noise); Kaiser-Bessel
+width 4 on a sigma = 2 grid (384^2) for a 192^2 image, analytic ramp (Ram-Lak)
+DCF, deapodised, cropped and combined by root sum of squares.  One step = one
+call reconstructing all 96 frames x 32 coils (40 108 032 gridded samples).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+`value`: device-resident inputs (321 MB of samples, larger than the 129 MB L2,
+so no flush is needed between steps).  `e2e`: the same call with the samples
+and trajectory copied from pinned host memory and the images copied back
+inside every step.  `--impl reference` times the reference's CPU path
+(radial_linear_gridding2_adjoint + ramp DCF, the C restatement that is
+bit-identical to it) on a bounded sample of the same workload over all host
+cores.  Under torchrun every rank reconstructs its own batch (replicas, weak
+scaling, no collective on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import re
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+FRAMES, SPOKES, READOUT, COILS = 96, 34, 384, 32
+IMAGE, GRID, WIDTH = 192, 384, 4
+METRIC = "gridded samples/s"
+WORKLOAD = "batched dynamic 2D radial adjoint (KB W=4, sigma=2) + RSS"
+
+
+def workload_config(extra: dict | None = None) -> dict:
+    cfg = {"workload": WORKLOAD, "frames": FRAMES, "spokes_per_frame": SPOKES, "readout": READOUT, "coils": COILS,
+           "image": IMAGE, "grid": GRID, "kernel": "kaiser_bessel", "kernel_width": WIDTH, "oversampling": 2.0,
+           "dcf": "analytic ramp (Ram-Lak)", "output": "rss float32 [96,192,192]",
+           "l2": "inputs larger than L2 (321 MB samples)"}
+    if extra:
+        cfg.update(extra)
+    return cfg
+
+
+def make_inputs(seed: int = 7):
+    from kspacejet_gb300 import synth
+
+    traj, ksp = synth.dynamic_radial(FRAMES, SPOKES, READOUT, COILS, seed=seed, image=IMAGE, snr_db=30.0)
+    return np.ascontiguousarray(traj, dtype=np.float32), np.ascontiguousarray(ksp, dtype=np.complex64)
+
+
+# --------------------------------------------------------------- clocks
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.device_index = device_index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device_index}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        loaded = [s for s in sm if s > 0.5 * max(sm)] or sm
+        return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# --------------------------------------------------------- CPU baseline
+
+def cpu_reference_rate(traj: np.ndarray, ksp: np.ndarray, budget_s: float = 2.5, min_pairs: int = 0):
+    """Gridded samples/s of the reference's CPU path (ramp DCF + linear
+    gridding + separable inverse DFT, one (frame, coil) image per task) on all
+    host cores.  Uses the compiled reference where it was built on this
+    machine, else the C restatement that is bit-identical to it."""
+    import oracle
+
+    try:
+        impl, kind = oracle.Reference(), "reference"
+    except FileNotFoundError:
+        impl, kind = oracle.Oracle(), "port"
+    cores = os.cpu_count() or 1
+    rng = np.random.default_rng(0)
+    pairs = [(int(f), int(c)) for f, c in zip(rng.integers(0, FRAMES, 4096), rng.integers(0, COILS, 4096))]
+    dcfs = {}
+
+    def task(fc):
+        f, c = fc
+        d = dcfs.get(f)
+        if d is None:
+            d = impl.ramp_dcf(traj[f])
+            dcfs[f] = d
+        impl.linear_gridding(IMAGE, IMAGE, ksp[f, c], traj[f], d)
+        return traj.shape[1]
+
+    done = 0
+    samples = 0
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=cores) as pool:
+        while True:
+            batch = pairs[done:done + cores]
+            samples += sum(pool.map(task, batch))
+            done += len(batch)
+            el = time.perf_counter() - t0
+            if (el >= budget_s and done >= min_pairs) or done >= len(pairs):
+                break
+    el = time.perf_counter() - t0
+    return {"value": samples / el, "unit": METRIC, "cores": cores, "kind": kind,
+            "sample": f"{done} (frame, coil) images of the workload ({traj.shape[1]} samples each) through "
+                      f"radial_linear_gridding2_adjoint with ramp DCF on a {IMAGE}x{IMAGE} grid (the reference's "
+                      f"direct-DFT fallback for a non-power-of-two axis), {cores} threads, {el:.2f} s wall"}
+
+
+# ------------------------------------------------------------ GPU arm
+
+def dist_setup(n_gpus: int):
+    if int(os.environ.get("WORLD_SIZE", "1")) > 1:
+        import torch.distributed as dist
+
+        backend = "gloo"
+        dist.init_process_group(backend=backend)
+        return dist, dist.get_rank(), dist.get_world_size(), int(os.environ.get("LOCAL_RANK", "0"))
+    return None, 0, 1, 0
+
+
+def read_traffic() -> float | None:
+    """dram__bytes_read.sum + dram__bytes_write.sum per launch of the dominant
+    kernel from the committed ncu summary (profiles/)."""
+    p = ROOT / "profiles" / "k_rows_dynamic2d.md"
+    if not p.exists():
+        return None
+    m = re.search(r"traffic_bytes_per_full_launch:\s*([0-9.eE+]+)", p.read_text())
+    return float(m.group(1)) if m else None
+
+
+def kernel_bytes(g, entries: int) -> dict:
+    """Algorithmic HBM bytes per launch of each kernel of one call."""
+    F, C, M = g.frames, g.channels, g.samples
+    N, G = IMAGE, GRID
+    rec = 16 + 8 * WIDTH
+    inter = F * C * G * N * 8
+    return {
+        "k_rows": F * M * C * 8 + F * M * rec + entries * 4 + inter,
+        "k_cols": inter + F * N * N * 4,
+        "k_samples_coil_last": 2 * F * C * M * 8,
+        "k_prepare": F * M * 8 + F * M * rec,
+    }
+
+
+def run_ours(args) -> dict | None:
+    import torch
+
+    from kspacejet_gb300 import gpu
+
+    dist, rank, world, local_rank = dist_setup(args.gpus)
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    traj_h, ksp_h = make_inputs(seed=7 + rank)
+    cpu = cpu_reference_rate(traj_h, ksp_h) if rank == 0 else None
+
+    g = gpu.kb_gridding(image=IMAGE, grid=GRID, channels=COILS, samples=traj_h.shape[1], frames=FRAMES, width=WIDTH,
+                        output=gpu.OUTPUT_RSS)
+    k = torch.from_numpy(ksp_h).to(dev)
+    t = torch.from_numpy(traj_h).to(dev)
+    out = g.new_output(dev)
+    ws = g.new_workspace(dev)
+    stream = torch.cuda.current_stream()
+    tuning = g.tune(k, t, out, ws)
+    for _ in range(args.warmup):
+        g.run(k, t, out, ws, tuning=tuning)
+    torch.cuda.synchronize()
+    _, _, entries = None, None, None
+    cw, off, smp = g.binning(ws, tuning)
+    entries = int(off[-1])
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    # ---- value: device-resident inputs
+    gpu.timing_reset()
+    gpu.timing_enable(True)
+    launches0 = gpu.launch_count()
+    barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local_rank) as clocks:
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            g.run(k, t, out, ws, tuning=tuning)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    launches = gpu.launch_count() - launches0
+    gpu.timing_enable(False)
+    kernels = gpu.timing_read()
+    ms = e0.elapsed_time(e1) / args.steps
+
+    # ---- e2e: pinned host buffers, copies inside every step
+    kh = torch.from_numpy(ksp_h).pin_memory()
+    th = torch.from_numpy(traj_h).pin_memory()
+    oh = torch.empty(out.shape, dtype=out.dtype).pin_memory()
+    for _ in range(2):
+        k.copy_(kh, non_blocking=True)
+        t.copy_(th, non_blocking=True)
+        g.run(k, t, out, ws, tuning=tuning)
+        oh.copy_(out, non_blocking=True)
+    barrier()
+    torch.cuda.synchronize()
+    x0 = torch.cuda.Event(enable_timing=True)
+    x1 = torch.cuda.Event(enable_timing=True)
+    x0.record(stream)
+    for _ in range(args.steps):
+        k.copy_(kh, non_blocking=True)
+        t.copy_(th, non_blocking=True)
+        g.run(k, t, out, ws, tuning=tuning)
+        oh.copy_(out, non_blocking=True)
+    x1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    e2e_ms = x0.elapsed_time(x1) / args.steps
+    if not np.isfinite(oh.numpy()).all():
+        raise RuntimeError("non-finite reconstruction")
+
+    if dist is not None:
+        tt = torch.tensor([ms, e2e_ms], dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms, e2e_ms = float(tt[0]), float(tt[1])
+    if rank != 0:
+        return None
+
+    per_step = FRAMES * COILS * traj_h.shape[1]
+    value = world * per_step / (ms / 1000.0)
+    e2e = world * per_step / (e2e_ms / 1000.0)
+
+    # roofline of the dominant kernel
+    peaks = {}
+    pp = ROOT / "MEASURED_PEAKS.json"
+    if pp.exists():
+        peaks = json.loads(pp.read_text())
+    peak = peaks.get("hbm_gbs")
+    peak_src = "measured" if peak else "fallback"
+    peak = peak or 6800.0
+    bytes_per = kernel_bytes(g, entries)
+    dom = max(kernels, key=lambda kv: kv[2]) if kernels else None
+    roofline = None
+    per_kernel = {}
+    for name, n, tot in kernels:
+        avg = tot / max(n, 1)
+        entry = {"launches": n, "avg_ms": round(avg, 4), "share": round(tot / max(sum(x[2] for x in kernels), 1e-9), 4)}
+        if name in bytes_per:
+            entry["algorithmic_GBps"] = round(bytes_per[name] / (avg / 1000.0) / 1e9, 1)
+        per_kernel[name] = entry
+    if dom is not None:
+        name, n, tot = dom
+        avg_s = tot / max(n, 1) / 1000.0
+        ach = bytes_per.get(name, 0) / avg_s / 1e9
+        traffic = read_traffic() if name == "k_rows" else None
+        roofline = {"bound": "hbm", "kernel": name, "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
+                    "frac": round(ach / peak, 4), "peak_source": f"{peak_src} hbm_gbs",
+                    "algorithmic_bytes_per_launch": bytes_per.get(name), "traffic": traffic}
+    return {
+        "metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 (complex64 samples, float32 gridding/FFT)", "data": "synthetic",
+        "config": workload_config({"parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                                   "tuning": {"coil_group": tuning.coil_group, "column_block": tuning.column_block},
+                                   "gridded_samples_per_step_per_gpu": per_step}),
+        "e2e": {"value": e2e, "unit": "samples/s", "ms_per_step": e2e_ms,
+                "h2d_bytes_per_step": int(ksp_h.nbytes + traj_h.nbytes), "d2h_bytes_per_step": int(out.numel() * 4)},
+        "gpu_launches": int(launches),
+        "roofline": roofline, "kernels": per_kernel,
+        "clocks": clocks.summary(),
+        "cpu_baseline": cpu,
+    }
+
+
+def run_reference(args) -> dict | None:
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return None
+    traj_h, ksp_h = make_inputs()
+    per = []
+    cpu = None
+    for i in range(args.warmup + args.steps):
+        r = cpu_reference_rate(traj_h, ksp_h, budget_s=1.0, min_pairs=os.cpu_count() or 1)
+        if i >= args.warmup:
+            per.append(r)
+            cpu = r
+    value = statistics.median(p["value"] for p in per)
+    cpu = dict(cpu)
+    cpu["value"] = value
+    ms = FRAMES * COILS * traj_h.shape[1] / value * 1000.0
+    return {"metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
+            "config": workload_config({"note": "reference CPU path on a bounded sample of each step's images; "
+                                               "ms_per_step extrapolated to the full 96x32-image step"}),
+            "e2e": {"value": value, "unit": "samples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "cpu_baseline": cpu}
+
+
+def main() -> int:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    if args.impl == "reference":
+        res = run_reference(args)
+    else:
+        import kspacejet_gb300
+
+        kspacejet_gb300.build()
+        res = run_ours(args)
+    if res is not None:
+        print(json.dumps(res))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -187,6 +187,16 @@ KSJ_GPU_API ksj_gpu_status ksj_gpu_context_sync(ksj_gpu_context* context);
 /* Total device bytes and streams the context holds (the Provider declares them). */
 KSJ_GPU_API uint64_t ksj_gpu_context_device_bytes(const ksj_gpu_context* context);
 
+/* Per-kernel timing for measurement.  While enabled, every kernel the
+ * library launches is bracketed by CUDA events on the stream it is launched
+ * on; ksj_gpu_timing_read waits for those events and returns, per kernel
+ * name, the launch count and the summed event-to-event milliseconds since the
+ * last reset.  names receives max_entries rows of 48 bytes.  Returns the
+ * number of distinct kernels (which may exceed max_entries). */
+KSJ_GPU_API void ksj_gpu_timing_enable(int enable);
+KSJ_GPU_API void ksj_gpu_timing_reset(void);
+KSJ_GPU_API uint32_t ksj_gpu_timing_read(uint32_t max_entries, char* names, uint64_t* launches, double* total_ms);
+
 /* Human-readable status text (static storage). */
 KSJ_GPU_API const char* ksj_gpu_status_string(ksj_gpu_status status);
 /* Number of kernel launches this process issued through the library. */

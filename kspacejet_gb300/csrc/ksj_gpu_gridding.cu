@@ -546,35 +546,67 @@ __global__ void __launch_bounds__(kMaxThreads) k_rows(RowsArgs a) {
     const bool coil_ok = my_coil < cg && coil_global < a.channels;
     const size_t sample_base = static_cast<size_t>(f) * a.samples * a.channels + (coil_ok ? coil_global : 0);
     bool bad = false;
+    const void* ks = a.samples_t;
     for (int base = 0; base < n; base += 32) {
-      const uint32_t mine = base + lane < n ? __ldg(ent + base + lane) : 0u;
       const int cnt = min(32, n - base);
-      for (int i = 0; i < cnt; ++i) {
-        const uint32_t s = __shfl_sync(0xffffffffu, mine, i);
-        const SampleRecord<W>& r = recs[s];
+      // lane i owns list entry base + i: its sample index, first tap column,
+      // the W tap weights of this row (row weight folded in) and dcf * phase
+      uint32_t my_s = 0;
+      int my_c0 = 0;
+      float2 my_scale = make_float2(0.0f, 0.0f);
+      float my_w[W];
+#pragma unroll
+      for (int j = 0; j < W; ++j) my_w[j] = 0.0f;
+      if (lane < cnt) {
+        my_s = __ldg(ent + base + lane);
+        const SampleRecord<W>& r = recs[my_s];
         int ta = row - r.r0;
         if (ta < 0) ta += a.grid_rows;
         const float wr = r.wr[ta];
-        if (coil_ok) {
-          const float2 y = load_sample<kFormat>(a.samples_t, sample_base + static_cast<size_t>(s) * a.channels);
-          bad |= !(isfinite(y.x) && isfinite(y.y));
-          const float2 v = cmul(y, r.scale);
+        my_c0 = r.c0;
+        my_scale = r.scale;
 #pragma unroll
-          for (int j = 0; j < W; ++j) {
-            if (j % ngroups != my_group) continue;
-            int col = r.c0 + j;
-            if (col >= a.grid_cols) col -= a.grid_cols;
-            if (col >= col_lo && col < col_hi) {
-              const float wt = wr * r.wc[j];
-              float2* cell = acc + addr(my_coil, col);
-              float2 c = *cell;
-              c.x = fmaf(v.x, wt, c.x);
-              c.y = fmaf(v.y, wt, c.y);
-              *cell = c;
+        for (int j = 0; j < W; ++j) my_w[j] = wr * r.wc[j];
+      }
+      // groups of 8 samples: all 8 coil loads in flight before the first use
+      for (int i0 = 0; i0 < cnt; i0 += 8) {
+        float2 yv[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+          const uint32_t sk = __shfl_sync(0xffffffffu, my_s, (i0 + k) & 31);
+          yv[k] = (coil_ok && i0 + k < cnt) ? load_sample<kFormat>(ks, sample_base + static_cast<size_t>(sk) * a.channels)
+                                             : make_float2(0.0f, 0.0f);
+        }
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+          const int i = i0 + k;
+          if (i >= cnt) break;
+          const int c0 = __shfl_sync(0xffffffffu, my_c0, i);
+          float2 sc;
+          sc.x = __shfl_sync(0xffffffffu, my_scale.x, i);
+          sc.y = __shfl_sync(0xffffffffu, my_scale.y, i);
+          float wt[W];
+#pragma unroll
+          for (int j = 0; j < W; ++j) wt[j] = __shfl_sync(0xffffffffu, my_w[j], i);
+          if (coil_ok) {
+            bad |= !(isfinite(yv[k].x) && isfinite(yv[k].y));
+            const float2 v = cmul(yv[k], sc);
+#pragma unroll
+            for (int j = 0; j < W; ++j) {
+              if (j % ngroups != my_group) continue;
+              int col = c0 + j;
+              if (col >= a.grid_cols) col -= a.grid_cols;
+              if (col >= col_lo && col < col_hi) {
+                float2* cell = acc + addr(my_coil, col);
+                float2 c = *cell;
+                c.x = fmaf(v.x, wt[j], c.x);
+                c.y = fmaf(v.y, wt[j], c.y);
+                *cell = c;
+              }
             }
           }
+          __syncwarp();
         }
-        __syncwarp();
       }
     }
     if (bad) atomicOr(a.flags, KSJ_GPU_FLAG_NONFINITE_SAMPLE);
@@ -738,10 +770,10 @@ ksj_gpu_status launch_all(const Shape& s, const Layout& l, const ksj_gpu_griddin
   {
     const int n = std::max(std::max(s.grid_rows, s.grid_cols), std::max(s.out_rows, s.out_cols));
     const double beta = s.beta;
+    LaunchScope scope("k_tables", stream);
     k_tables<<<(n + 255) / 256, 256, 0, stream>>>(tw_rows, s.grid_rows, tw_cols, s.grid_cols, inv_dr, s.out_rows,
                                                   inv_dc, s.out_cols, s.kb ? 1 : 0, s.width, beta,
                                                   s.kb ? std::cyl_bessel_i(0.0, beta) : 1.0);
-    count_launch();
   }
   const size_t fm = static_cast<size_t>(s.frames) * s.samples;
   {
@@ -766,27 +798,32 @@ ksj_gpu_status launch_all(const Shape& s, const Layout& l, const ksj_gpu_griddin
     p.phase_row = s.phase_row;
     p.phase_col = s.phase_col;
     p.phase_sign = s.phase_sign;
+    LaunchScope scope("k_prepare", stream);
     k_prepare<W><<<static_cast<unsigned>((fm + 255) / 256), 256, 0, stream>>>(p);
-    count_launch();
   }
-  k_scan<<<s.frames, 1024, 0, stream>>>(counts, offsets, s.lists_per_frame);
-  count_launch();
-  k_scatter<W><<<static_cast<unsigned>((fm + 255) / 256), 256, 0, stream>>>(
-      records, offsets, cursor, entries, s.frames, s.samples, s.grid_rows, s.grid_cols, s.nchunks,
-      s.entries_per_frame);
-  count_launch();
+  {
+    LaunchScope scope("k_scan", stream);
+    k_scan<<<s.frames, 1024, 0, stream>>>(counts, offsets, s.lists_per_frame);
+  }
+  {
+    LaunchScope scope("k_scatter", stream);
+    k_scatter<W><<<static_cast<unsigned>((fm + 255) / 256), 256, 0, stream>>>(
+        records, offsets, cursor, entries, s.frames, s.samples, s.grid_rows, s.grid_cols, s.nchunks,
+        s.entries_per_frame);
+  }
   {
     const size_t smem = static_cast<size_t>(8) * s.list_capacity * 4;
     if (cudaFuncSetAttribute(k_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)) !=
         cudaSuccess)
       return KSJ_GPU_ERROR_CUDA;
+    LaunchScope scope("k_sort", stream);
     k_sort<<<static_cast<unsigned>((nl + 7) / 8), 256, smem, stream>>>(offsets, entries, s.frames,
                                                                         s.lists_per_frame, s.entries_per_frame,
                                                                         s.list_capacity);
-    count_launch();
   }
   {
     const dim3 tg((s.samples + 31) / 32, (s.channels + 31) / 32, s.frames);
+    LaunchScope scope("k_samples_coil_last", stream);
     if (kFormat == KSJ_GPU_SAMPLES_BF16)
       k_transpose<uint32_t><<<tg, dim3(32, 8), 0, stream>>>(static_cast<const uint32_t*>(d_kspace),
                                                             reinterpret_cast<uint32_t*>(ws + l.samples_t),
@@ -795,7 +832,6 @@ ksj_gpu_status launch_all(const Shape& s, const Layout& l, const ksj_gpu_griddin
       k_transpose<unsigned long long><<<tg, dim3(32, 8), 0, stream>>>(
           static_cast<const unsigned long long*>(d_kspace), reinterpret_cast<unsigned long long*>(ws + l.samples_t),
           s.channels, s.samples);
-    count_launch();
   }
   {
     RowsArgs r{};
@@ -826,8 +862,8 @@ ksj_gpu_status launch_all(const Shape& s, const Layout& l, const ksj_gpu_griddin
       return KSJ_GPU_ERROR_CUDA;
     const dim3 grid(s.grid_rows, (s.channels + s.coil_group - 1) / s.coil_group, s.frames);
     const int threads = std::max(64, s.nchunks * 32);
+    LaunchScope scope("k_rows", stream);
     kern<<<grid, threads, smem, stream>>>(r);
-    count_launch();
   }
   {
     ColsArgs c{};
@@ -855,8 +891,8 @@ ksj_gpu_status launch_all(const Shape& s, const Layout& l, const ksj_gpu_griddin
       if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)) !=
           cudaSuccess)
         return KSJ_GPU_ERROR_CUDA;
+      LaunchScope scope("k_cols", stream);
       kern<<<grid, threads, smem, stream>>>(c);
-      count_launch();
       return KSJ_GPU_OK;
     };
     ksj_gpu_status st;
@@ -868,10 +904,10 @@ ksj_gpu_status launch_all(const Shape& s, const Layout& l, const ksj_gpu_griddin
     if (coil_last) {
       const int pixels = s.out_rows * s.out_cols;
       const dim3 tg((pixels + 31) / 32, (s.channels + 31) / 32, s.frames);
+      LaunchScope scope("k_images_coil_last", stream);
       k_transpose<unsigned long long><<<tg, dim3(32, 8), 0, stream>>>(
           reinterpret_cast<const unsigned long long*>(ws + l.coil_major), static_cast<unsigned long long*>(d_out),
           s.channels, pixels);
-      count_launch();
     }
   }
   return check_launch();

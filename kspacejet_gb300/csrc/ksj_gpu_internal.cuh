@@ -14,8 +14,23 @@ namespace ksj_gpu {
 
 // ------------------------------------------------------------------ launches
 
-void count_launch();                 // increments the library launch counter
 ksj_gpu_status check_launch();       // cudaGetLastError -> status
+
+// Brackets one kernel launch: counts it and, while timing is enabled, records
+// CUDA events before and after it on its stream.  Construct immediately
+// before the launch; the destructor runs after it.
+class LaunchScope {
+ public:
+  LaunchScope(const char* name, cudaStream_t stream);
+  ~LaunchScope();
+  LaunchScope(const LaunchScope&) = delete;
+  LaunchScope& operator=(const LaunchScope&) = delete;
+
+ private:
+  const char* name_;
+  cudaStream_t stream_;
+  cudaEvent_t start_ = nullptr;
+};
 
 inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
@@ -74,7 +89,10 @@ __device__ __forceinline__ dfloat grid_coordinate(float f, float n) {
   return fast_two_sum(q, __fdiv_rn(num, kTwoPiHi));
 }
 
-// floor of hi + lo, and the fractional part in [0, 1).
+// floor of hi + lo (|lo| <= ulp(hi)/2), and the fractional part in [0, 1).
+// The floor is exact; a fraction within 2^-25 of 1 is not representable and
+// rounds to 1.0f, so it is clamped to the largest float below 1 -- the floor
+// itself must not move, or the tap window would shift by one cell.
 __device__ __forceinline__ int dfloor(dfloat x, float* frac) {
   float l = floorf(x.hi);
   float f;
@@ -88,11 +106,7 @@ __device__ __forceinline__ int dfloor(dfloat x, float* frac) {
   } else {
     f = __fadd_rn(__fsub_rn(x.hi, l), x.lo);
   }
-  if (f >= 1.0f) {
-    l += 1.0f;
-    f = 0.0f;
-  }
-  *frac = f;
+  *frac = fminf(f, 0.99999994f);
   return static_cast<int>(l);
 }
 

@@ -3,6 +3,9 @@
 #include <cuda_runtime.h>
 
 #include <atomic>
+#include <mutex>
+#include <string>
+#include <vector>
 #include <cstdint>
 #include <cstring>
 #include <new>
@@ -14,9 +17,65 @@ namespace ksj_gpu {
 
 namespace {
 std::atomic<uint64_t> g_launches{0};
+std::atomic<int> g_timing{0};
+
+struct Pending {
+  const char* name;
+  cudaEvent_t start, stop;
+};
+struct Totals {
+  std::string name;
+  uint64_t launches = 0;
+  double ms = 0.0;
+};
+std::mutex g_timing_mutex;
+std::vector<Pending> g_pending;
+std::vector<Totals> g_totals;
+
+void settle_locked() {
+  for (const Pending& p : g_pending) {
+    float ms = 0.0f;
+    if (cudaEventSynchronize(p.stop) == cudaSuccess && cudaEventElapsedTime(&ms, p.start, p.stop) == cudaSuccess) {
+      Totals* t = nullptr;
+      for (Totals& x : g_totals)
+        if (x.name == p.name) t = &x;
+      if (t == nullptr) {
+        g_totals.push_back(Totals{p.name, 0, 0.0});
+        t = &g_totals.back();
+      }
+      t->launches += 1;
+      t->ms += ms;
+    }
+    cudaEventDestroy(p.start);
+    cudaEventDestroy(p.stop);
+  }
+  g_pending.clear();
+}
+}  // namespace
+
+LaunchScope::LaunchScope(const char* name, cudaStream_t stream) : name_(name), stream_(stream) {
+  g_launches.fetch_add(1, std::memory_order_relaxed);
+  if (g_timing.load(std::memory_order_relaxed) &&
+      cudaEventCreateWithFlags(&start_, cudaEventDefault) == cudaSuccess) {
+    if (cudaEventRecord(start_, stream_) != cudaSuccess) {
+      cudaEventDestroy(start_);
+      start_ = nullptr;
+    }
+  }
 }
 
-void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+LaunchScope::~LaunchScope() {
+  if (start_ == nullptr) return;
+  cudaEvent_t stop = nullptr;
+  if (cudaEventCreateWithFlags(&stop, cudaEventDefault) != cudaSuccess || cudaEventRecord(stop, stream_) != cudaSuccess) {
+    if (stop) cudaEventDestroy(stop);
+    cudaEventDestroy(start_);
+    return;
+  }
+  std::lock_guard<std::mutex> lock(g_timing_mutex);
+  g_pending.push_back(Pending{name_, start_, stop});
+  if (g_pending.size() > 4096) settle_locked();
+}
 
 ksj_gpu_status check_launch() {
   const cudaError_t e = cudaGetLastError();
@@ -124,16 +183,18 @@ extern "C" ksj_gpu_status ksj_gpu_direct_adjoint(uint32_t rows, uint32_t cols, d
   float2* tmp = static_cast<float2*>(d_workspace);
   const int pixels = static_cast<int>(rows * cols);
   const dim3 grid((pixels + kDirectPixels - 1) / kDirectPixels, (channels + kDirectCoils - 1) / kDirectCoils);
+  {
+  LaunchScope scope("k_direct_adjoint", cs);
   k_direct_adjoint<<<grid, kDirectPixels, 0, cs>>>(static_cast<const float2*>(d_kspace),
                                                    reinterpret_cast<const float2*>(d_traj), tmp,
                                                    static_cast<int>(rows), static_cast<int>(cols), ro, co,
                                                    static_cast<int>(channels), static_cast<int>(samples));
-  count_launch();
+  }
   const dim3 tg((pixels + 31) / 32, (channels + 31) / 32, 1);
+  LaunchScope scope("k_images_coil_last", cs);
   k_transpose<unsigned long long><<<tg, dim3(32, 8), 0, cs>>>(reinterpret_cast<const unsigned long long*>(tmp),
                                                               static_cast<unsigned long long*>(d_out),
                                                               static_cast<int>(channels), pixels);
-  count_launch();
   return check_launch();
 }
 
@@ -142,9 +203,9 @@ extern "C" ksj_gpu_status ksj_gpu_rss_coil_last(uint64_t pixels, uint32_t channe
   if (pixels == 0 || channels == 0 || d_coil_last == nullptr || d_out == nullptr)
     return KSJ_GPU_ERROR_INVALID_ARGUMENT;
   cudaStream_t cs = static_cast<cudaStream_t>(stream);
+  LaunchScope scope("k_rss", cs);
   k_rss<<<static_cast<unsigned>((pixels + 255) / 256), 256, 0, cs>>>(static_cast<const float2*>(d_coil_last), d_out,
                                                                      pixels, static_cast<int>(channels));
-  count_launch();
   return check_launch();
 }
 
@@ -271,3 +332,25 @@ extern "C" const char* ksj_gpu_status_string(ksj_gpu_status status) {
 }
 
 extern "C" uint64_t ksj_gpu_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
+
+extern "C" void ksj_gpu_timing_enable(int enable) { g_timing.store(enable ? 1 : 0); }
+
+extern "C" void ksj_gpu_timing_reset(void) {
+  std::lock_guard<std::mutex> lock(g_timing_mutex);
+  settle_locked();
+  g_totals.clear();
+}
+
+extern "C" uint32_t ksj_gpu_timing_read(uint32_t max_entries, char* names, uint64_t* launches, double* total_ms) {
+  std::lock_guard<std::mutex> lock(g_timing_mutex);
+  settle_locked();
+  for (uint32_t i = 0; i < max_entries && i < g_totals.size(); ++i) {
+    if (names) {
+      std::strncpy(names + 48 * i, g_totals[i].name.c_str(), 47);
+      names[48 * i + 47] = 0;
+    }
+    if (launches) launches[i] = g_totals[i].launches;
+    if (total_ms) total_ms[i] = g_totals[i].ms;
+  }
+  return static_cast<uint32_t>(g_totals.size());
+}

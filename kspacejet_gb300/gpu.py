@@ -76,6 +76,10 @@ def lib() -> ctypes.CDLL:
         L.ksj_gpu_rss_coil_last.argtypes = [u64, u32, vp, vp, vp]
         L.ksj_gpu_launch_count.restype = u64
         L.ksj_gpu_launch_count.argtypes = []
+        L.ksj_gpu_timing_enable.argtypes = [ctypes.c_int]
+        L.ksj_gpu_timing_reset.argtypes = []
+        L.ksj_gpu_timing_read.restype = u32
+        L.ksj_gpu_timing_read.argtypes = [u32, vp, vp, vp]
         L.ksj_gpu_status_string.restype = ctypes.c_char_p
         L.ksj_gpu_status_string.argtypes = [ctypes.c_int32]
         _lib = L
@@ -94,6 +98,26 @@ def _stream(stream: torch.cuda.Stream | None) -> int:
 
 def launch_count() -> int:
     return int(lib().ksj_gpu_launch_count())
+
+
+def timing_enable(on: bool = True) -> None:
+    lib().ksj_gpu_timing_enable(1 if on else 0)
+
+
+def timing_reset() -> None:
+    lib().ksj_gpu_timing_reset()
+
+
+def timing_read() -> list[tuple[str, int, float]]:
+    """[(kernel name, launches, total ms)] since the last reset (waits for the events)."""
+    L = lib()
+    n = int(L.ksj_gpu_timing_read(0, None, None, None))
+    names = ctypes.create_string_buffer(48 * max(n, 1))
+    launches = (ctypes.c_uint64 * max(n, 1))()
+    ms = (ctypes.c_double * max(n, 1))()
+    n = int(L.ksj_gpu_timing_read(n, names, launches, ms))
+    raw = names.raw
+    return [(raw[48 * i:48 * i + 48].split(b"\0")[0].decode(), int(launches[i]), float(ms[i])) for i in range(n)]
 
 
 @dataclass

@@ -75,14 +75,14 @@ SHEPP_LOGAN = [
 
 
 def ellipse_kspace(traj: np.ndarray, image: int, ellipses=SHEPP_LOGAN, shift=(0.0, 0.0)) -> np.ndarray:
-    """Continuous FT of an ellipse phantom sampled at `traj` (rad/px of an
-    `image`-pixel grid), with the FT sign convention of the direct forward
-    NUDFT (exp(-i k.x)), x measured in pixels from the image centre.  `shift`
-    moves the whole phantom (pixels)."""
-    kr = traj[:, 0].astype(np.float64)
-    kc = traj[:, 1].astype(np.float64)
+    """Continuous FT of an ellipse phantom sampled at `traj` ([..., 2], rad/px
+    of an `image`-pixel grid), with the FT sign convention of the direct
+    forward NUDFT (exp(-i k.x)), x measured in pixels from the image centre.
+    `shift` moves the whole phantom (pixels)."""
+    kr = traj[..., 0].astype(np.float64)
+    kc = traj[..., 1].astype(np.float64)
     half = image / 2.0
-    out = np.zeros(traj.shape[0], dtype=np.complex128)
+    out = np.zeros(kr.shape, dtype=np.complex128)
     for (cr, cc, ar, ac, ang, rho) in ellipses:
         th = math.radians(ang)
         a, b = ar * half, ac * half
@@ -109,11 +109,8 @@ def multicoil_kspace(traj: np.ndarray, image: int, channels: int, seed: int, snr
     g_c exp(i s_c . x) (an exact shift of the phantom's FT by s_c), plus
     complex Gaussian noise at `snr_db` relative to the mean signal power."""
     gains, slopes = coil_parameters(channels, seed, image)
-    m = traj.shape[0]
-    out = np.empty((channels, m), dtype=np.complex128)
-    for c in range(channels):
-        shifted = traj.astype(np.float64) - slopes[c][None, :]
-        out[c] = gains[c] * ellipse_kspace(shifted, image, ellipses, shift)
+    shifted = traj.astype(np.float64)[None, :, :] - slopes[:, None, :]
+    out = gains[:, None] * ellipse_kspace(shifted, image, ellipses, shift)
     if snr_db is not None:
         rng = np.random.default_rng(seed + 1)
         p = np.mean(np.abs(out) ** 2)

@@ -72,10 +72,12 @@ def test_large_linear_matches_fp64(native, cuda, orc):
         tr = synth.golden_angle_radial(512, 128)
         ks = synth.random_kspace(4, tr.shape[0], seed=n)
         _, out, _, _ = _run_linear(native, cuda, ks, tr, n, n)
-        d64 = orc.ramp_dcf(tr.astype(np.float64))
+        # float32(-pi) lies just outside double pi: weight with numpy, not the checked ramp
+        d64 = np.hypot(tr[:, 0].astype(np.float64), tr[:, 1].astype(np.float64))
         for c in range(2):
             exact = orc.linear_gridding(n, n, ks[c].astype(np.complex128), tr.astype(np.float64), d64, exact=True)
             err = oracle.rel_l2(out[0, ..., c], exact)
+            print(f"linear N={n} coil {c}: rel L2 vs FP64 {err:.3e}")
             assert err <= TOL_FP64, (n, c, err)
 
 
@@ -144,15 +146,18 @@ def _kb_case(orc, image, grid, width, channels, spokes, seed):
     return tr, ks
 
 
-@pytest.mark.parametrize("image,grid,width", [(64, 128, 4), (48, 96, 4), (32, 64, 6), (64, 96, 4)])
-def test_kaiser_bessel_matches_fp64_oracle(native, cuda, orc, image, grid, width):
+@pytest.mark.parametrize("image,grid,width,first", [(64, 128, 4, 1), (48, 96, 4, 2), (32, 64, 6, 3), (64, 96, 4, 4),
+                                                    (32, 64, 4, 0), (32, 64, 2, 0), (64, 128, 8, 0)])
+def test_kaiser_bessel_matches_fp64_oracle(native, cuda, orc, image, grid, width, first):
     """Same algorithm in FP64 (oracle) vs the FP32 GPU path: <= 1e-5; against
     the exact direct NUDFT of the DCF-weighted samples: the KB approximation
     bound (width 4: 3e-3, width 6: 2e-4)."""
     import torch
     from kspacejet_gb300 import gpu
 
-    tr, ks = _kb_case(orc, image, grid, width, channels=2, spokes=40, seed=image + width)
+    # first = 0 puts spoke 0 on the column axis: coordinates within 2^-25 of
+    # grid integers, where the tap window is decided by the last bit
+    tr, ks = _kb_case(orc, image, grid, width, channels=2, spokes=40, seed=first)
     g = gpu.kb_gridding(image=image, grid=grid, channels=2, samples=tr.shape[0], width=width,
                         output=gpu.OUTPUT_COIL_MAJOR)
     out = g.new_output(cuda)
@@ -161,9 +166,11 @@ def test_kaiser_bessel_matches_fp64_oracle(native, cuda, orc, image, grid, width
     d64 = np.hypot(tr[:, 0].astype(np.float64), tr[:, 1].astype(np.float64))
     for c in range(2):
         ref = orc.kb_gridding(grid, image, ks[c].astype(np.complex128), tr.astype(np.float64), d64, width=width)
-        assert oracle.rel_l2(got[c], ref) <= TOL_FP64
         exact = orc.direct_adjoint(image, image, ks[c].astype(np.complex128) * d64, tr.astype(np.float64))
-        assert oracle.rel_l2(got[c], exact) <= (3e-3 if width == 4 else 2e-4)
+        e_ref, e_exact = oracle.rel_l2(got[c], ref), oracle.rel_l2(got[c], exact)
+        print(f"KB {image}/{grid} W={width} coil {c}: vs FP64 KB {e_ref:.3e}, vs exact NUDFT {e_exact:.3e}")
+        assert e_ref <= TOL_FP64
+        assert e_exact <= {2: 5e-2, 4: 3e-3, 6: 2e-4, 8: 2e-5}[width]
 
 
 def test_rss_epilogue_equals_rss_of_coil_images(native, cuda, orc):
