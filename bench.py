@@ -230,10 +230,31 @@ def run_ours(args) -> dict | None:
         if dist is not None:
             dist.barrier()
 
+    # ---- the batched call captured once in a CUDA graph (all kernels, one replay per step)
+    graph = None
+    try:
+        graph = torch.cuda.CUDAGraph()
+        side = torch.cuda.Stream()
+        side.wait_stream(stream)
+        with torch.cuda.stream(side):
+            g.run(k, t, out, ws, tuning=tuning)
+        stream.wait_stream(side)
+        with torch.cuda.graph(graph):
+            g.run(k, t, out, ws, tuning=tuning)
+        for _ in range(args.warmup):
+            graph.replay()
+        torch.cuda.synchronize()
+    except Exception as exc:  # capture is an optimisation; the direct path stays measured
+        graph = None
+        graph_error = repr(exc)
+
+    def step():
+        if graph is not None:
+            graph.replay()
+        else:
+            g.run(k, t, out, ws, tuning=tuning)
+
     # ---- value: device-resident inputs
-    gpu.timing_reset()
-    gpu.timing_enable(True)
-    launches0 = gpu.launch_count()
     barrier()
     torch.cuda.synchronize()
     with ClockSampler(local_rank) as clocks:
@@ -241,14 +262,47 @@ def run_ours(args) -> dict | None:
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         for _ in range(args.steps):
-            g.run(k, t, out, ws, tuning=tuning)
+            step()
         e1.record(stream)
         torch.cuda.synchronize()
     barrier()
-    launches = gpu.launch_count() - launches0
+    ms = e0.elapsed_time(e1) / args.steps
+    # launches inside the timed region: a graph replays the captured call's launches
+    per_call_launches = None
+
+    # ---- the same call issued directly, with per-kernel event timing (roofline)
+    gpu.timing_reset()
+    gpu.timing_enable(True)
+    l0 = gpu.launch_count()
+    d0 = torch.cuda.Event(enable_timing=True)
+    d1 = torch.cuda.Event(enable_timing=True)
+    d0.record(stream)
+    for _ in range(args.steps):
+        g.run(k, t, out, ws, tuning=tuning)
+    d1.record(stream)
+    torch.cuda.synchronize()
+    per_call_launches = (gpu.launch_count() - l0) // args.steps
     gpu.timing_enable(False)
     kernels = gpu.timing_read()
-    ms = e0.elapsed_time(e1) / args.steps
+    direct_ms = d0.elapsed_time(d1) / args.steps
+    launches = per_call_launches * args.steps
+
+    # ---- per-frame loop: the same 96 frames as 96 one-frame calls
+    g1 = gpu.kb_gridding(image=IMAGE, grid=GRID, channels=COILS, samples=traj_h.shape[1], frames=1, width=WIDTH,
+                         output=gpu.OUTPUT_RSS)
+    ws1 = g1.new_workspace(dev)
+    out1 = g1.new_output(dev)
+    for f in range(3):
+        g1.run(k[f:f + 1], t[f:f + 1], out1, ws1)
+    torch.cuda.synchronize()
+    p0 = torch.cuda.Event(enable_timing=True)
+    p1 = torch.cuda.Event(enable_timing=True)
+    p0.record(stream)
+    for f in range(FRAMES):
+        g1.run(k[f:f + 1], t[f:f + 1], out1, ws1)
+    p1.record(stream)
+    torch.cuda.synchronize()
+    per_frame_ms = p0.elapsed_time(p1)
 
     # ---- e2e: pinned host buffers, copies inside every step
     kh = torch.from_numpy(ksp_h).pin_memory()
@@ -299,8 +353,11 @@ def run_ours(args) -> dict | None:
     dom = max(kernels, key=lambda kv: kv[2]) if kernels else None
     roofline = None
     per_kernel = {}
+    calls = args.steps  # per-kernel totals come from the direct (event-timed) pass of args.steps calls
     for name, n, tot in kernels:
         avg = tot / max(n, 1)
+        if name in bytes_per:
+            bytes_per[name] = bytes_per[name] * calls / max(n, 1)  # per launch (a call may launch a kernel per pass)
         entry = {"launches": n, "avg_ms": round(avg, 4), "share": round(tot / max(sum(x[2] for x in kernels), 1e-9), 4)}
         if name in bytes_per:
             entry["algorithmic_GBps"] = round(bytes_per[name] / (avg / 1000.0) / 1e9, 1)
@@ -318,11 +375,16 @@ def run_ours(args) -> dict | None:
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 (complex64 samples, float32 gridding/FFT)", "data": "synthetic",
         "config": workload_config({"parallelism": f"replicas x{world}" if world > 1 else "single GPU",
-                                   "tuning": {"coil_group": tuning.coil_group, "column_block": tuning.column_block},
+                                   "tuning": {"coil_group": tuning.coil_group, "column_block": tuning.column_block,
+                                              "frames_per_pass": tuning.frames_per_pass or FRAMES,
+                                              "rows_blocks_per_sm": tuning.rows_blocks_per_sm},
                                    "gridded_samples_per_step_per_gpu": per_step}),
         "e2e": {"value": e2e, "unit": "samples/s", "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": int(ksp_h.nbytes + traj_h.nbytes), "d2h_bytes_per_step": int(out.numel() * 4)},
         "gpu_launches": int(launches),
+    "batched": {"graph_replay": graph is not None, "ms_per_step_graph_or_direct": ms,
+                "ms_per_step_direct": direct_ms, "per_frame_loop_ms_per_step": per_frame_ms,
+                "speedup_vs_per_frame_loop": per_frame_ms / ms, "launches_per_call": per_call_launches},
         "roofline": roofline, "kernels": per_kernel,
         "clocks": clocks.summary(),
         "cpu_baseline": cpu,

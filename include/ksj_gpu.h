@@ -56,6 +56,7 @@ typedef int32_t ksj_gpu_status;
 #define KSJ_GPU_FLAG_NONFINITE_SAMPLE (1u << 0)
 #define KSJ_GPU_FLAG_BAD_TRAJECTORY (1u << 1)   /* non-finite, or outside [-pi, pi] where required */
 #define KSJ_GPU_FLAG_BAD_DCF (1u << 2)          /* non-finite or negative external weight */
+#define KSJ_GPU_FLAG_WAIT_TIMEOUT (1u << 3)     /* a bounded device wait on a tile copy gave up; output invalid */
 
 /* ------------------------------------------------------------- gridding */
 
@@ -101,6 +102,8 @@ typedef struct ksj_gpu_gridding_tuning {
   uint32_t coil_group;      /* channels accumulated per row CTA: 1, 2, 4, 8, 16 or 32 */
   uint32_t column_block;    /* columns per column-pass CTA: 4, 8, 16 or 32 */
   uint32_t list_capacity;   /* per-warp sorted-list buffer, entries (power of two, 64..2048) */
+  uint32_t frames_per_pass; /* frames per row/column pass (the row-transformed grid of one pass stays in L2) */
+  uint32_t rows_blocks_per_sm; /* 1 or 2 resident row CTAs per SM (2 caps registers at 80 per thread) */
 } ksj_gpu_gridding_tuning;
 
 /* Workspace bytes ksj_gpu_gridding_adjoint needs for `desc` (0 on a bad desc). */

@@ -21,6 +21,7 @@ LIB_DIR = PACKAGE_DIR / "lib"
 GPU_LIB = LIB_DIR / "libksj_gpu.so"
 NONCARTESIAN_PLUGIN = LIB_DIR / "libksj_gb300_noncartesian_recon.so"
 COIL_COMBINE_PLUGIN = LIB_DIR / "libksj_gb300_coil_combine.so"
+KB_PLUGIN = LIB_DIR / "libksj_gb300_kb_recon.so"
 FIRING_HOST_LIB = LIB_DIR / "libksj_firing_host.so"
 
 

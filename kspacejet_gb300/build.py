@@ -4,6 +4,7 @@ compiled in parallel).
 * ``lib/libksj_gpu.so``      -- the sm_103a kernels behind ``include/ksj_gpu.h``
 * ``lib/libksj_gb300_noncartesian_recon.so`` -- drop-in ``org.kspacejet.noncartesian-recon`` plug-in
 * ``lib/libksj_gb300_coil_combine.so``       -- drop-in ``org.kspacejet.coil-combine`` plug-in
+* ``lib/libksj_gb300_kb_recon.so``           -- ``org.kspacejet.gb300-noncartesian-recon`` (Kaiser-Bessel operators)
 * ``lib/libksj_firing_host.so``              -- synchronous Provider host used by tests and the bench
 
 Every CUDA unit is compiled for ``-gencode arch=compute_103a,code=sm_103a``
@@ -27,6 +28,7 @@ LIB = PKG / "lib"
 GPU_LIB = LIB / "libksj_gpu.so"
 NONCARTESIAN_PLUGIN = LIB / "libksj_gb300_noncartesian_recon.so"
 COIL_COMBINE_PLUGIN = LIB / "libksj_gb300_coil_combine.so"
+KB_PLUGIN = LIB / "libksj_gb300_kb_recon.so"
 FIRING_HOST = LIB / "libksj_firing_host.so"
 
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc" if Path("/usr/local/cuda/bin/nvcc").exists() else "nvcc")
@@ -100,10 +102,11 @@ def build(verbose: bool = False) -> list[Path]:
         objs = list(pool.map(_compile_cu, CU_SOURCES))
         _link_gpu(objs)
         plugins = [pool.submit(_plugin, CSRC / "provider/noncartesian_recon_provider.cpp", NONCARTESIAN_PLUGIN),
-                   pool.submit(_plugin, CSRC / "provider/coil_combine_provider.cpp", COIL_COMBINE_PLUGIN)]
+                   pool.submit(_plugin, CSRC / "provider/coil_combine_provider.cpp", COIL_COMBINE_PLUGIN),
+                   pool.submit(_plugin, CSRC / "provider/kb_recon_provider.cpp", KB_PLUGIN)]
         for f in plugins + [host]:
             f.result()
-    out = [GPU_LIB, NONCARTESIAN_PLUGIN, COIL_COMBINE_PLUGIN, FIRING_HOST]
+    out = [GPU_LIB, NONCARTESIAN_PLUGIN, COIL_COMBINE_PLUGIN, KB_PLUGIN, FIRING_HOST]
     if verbose:
         for p in out:
             print(p)

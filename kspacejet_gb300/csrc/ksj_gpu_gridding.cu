@@ -32,6 +32,7 @@
 // chunk, with the lower tap index floor(k N / 2 pi) of the exact coordinate
 // (the value the reference's double-precision grid_coordinate computes,
 // eigen_radial_gridding.cpp:262-277).
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -54,6 +55,7 @@ constexpr int kMaxWidth = 8;      // largest Kaiser-Bessel width
 constexpr int kMaxGrid = 512;
 constexpr int kEmax = 8;          // complex values per thread per FFT stage
 constexpr int kMaxThreads = 512;
+constexpr int kAhead = 4;        // coil loads in flight per warp in k_rows
 constexpr uint32_t kFlagBytes = 256;
 
 // Per (frame, sample) record written by k_prepare, read by k_rows.
@@ -75,11 +77,12 @@ struct Shape {
   int lists_per_frame;     // grid_rows * nchunks
   size_t entries_per_frame;
   int out_rows, out_cols;  // kept image region
+  int inter_pitch;         // row pitch (elements) of the row-transformed grid: out_cols rounded to 2 (16 B)
   bool kb;
   float beta, inv_i0_beta;
   float row_origin, col_origin;
   float phase_row, phase_col, phase_sign;  // origin-phase coefficients
-  int coil_group, column_block, list_capacity;
+  int coil_group, column_block, list_capacity, frames_per_pass, rows_blocks;
   FftPlan plan_rows, plan_cols;
 };
 
@@ -137,6 +140,7 @@ ksj_gpu_status make_shape(const ksj_gpu_gridding_desc* d, const ksj_gpu_gridding
   s->entries_per_frame = static_cast<size_t>(s->samples) * s->width * 2;
   s->out_rows = s->rows;
   s->out_cols = s->cols;
+  s->inter_pitch = (s->cols + 1) & ~1;
   s->row_origin = static_cast<float>(d->row_origin);
   s->col_origin = static_cast<float>(d->col_origin);
   if (s->kb) {
@@ -197,6 +201,15 @@ ksj_gpu_status make_shape(const ksj_gpu_gridding_desc* d, const ksj_gpu_gridding
   s->coil_group = cg;
   s->column_block = cb;
   s->list_capacity = cap;
+  // frames per k_rows/k_cols pass: keep one pass's row-transformed grid
+  // (channels x grid_rows x out_cols complex) within ~64 MB of L2
+  int fpp = t && t->struct_size >= sizeof(ksj_gpu_gridding_tuning) ? static_cast<int>(t->frames_per_pass) : 0;
+  if (fpp <= 0) fpp = s->frames;
+  s->frames_per_pass = std::min(fpp, s->frames);
+  int rb = t && t->struct_size >= sizeof(ksj_gpu_gridding_tuning) ? static_cast<int>(t->rows_blocks_per_sm) : 0;
+  if (rb == 0) rb = 1;
+  if (rb != 1 && rb != 2) return KSJ_GPU_ERROR_INVALID_ARGUMENT;
+  s->rows_blocks = rb;
   return KSJ_GPU_OK;
 }
 
@@ -219,7 +232,7 @@ Layout make_layout(const Shape& s, const ksj_gpu_gridding_desc* d) {
   l.offsets = take((nl + s.frames) * 4);
   l.entries = take(static_cast<size_t>(s.frames) * s.entries_per_frame * 4);
   l.samples_t = take(fm * s.channels * sample_bytes(d->sample_format));
-  l.inter = take(static_cast<size_t>(s.frames) * s.channels * s.grid_rows * s.out_cols * sizeof(float2));
+  l.inter = take(static_cast<size_t>(s.frames) * s.channels * s.grid_rows * s.inter_pitch * sizeof(float2));
   l.coil_major = d->output == KSJ_GPU_OUTPUT_COIL_LAST
                      ? take(static_cast<size_t>(s.frames) * s.channels * s.out_rows * s.out_cols * sizeof(float2))
                      : off;
@@ -483,6 +496,7 @@ __global__ void __launch_bounds__(256) k_sort(const uint32_t* offsets, uint32_t*
 }
 
 struct RowsArgs {
+  int frame0;             // first frame of this pass
   const void* samples_t;  // [frame][sample][channel]
   const unsigned char* records;
   const uint32_t* offsets;
@@ -493,7 +507,7 @@ struct RowsArgs {
   int frames, channels, samples, grid_rows, grid_cols, nchunks, lists_per_frame;
   size_t entries_per_frame;
   int coil_group;
-  int out_cols, kb, image_cols;
+  int out_cols, inter_pitch, kb, image_cols;
   FftPlan plan;
 };
 
@@ -506,17 +520,18 @@ struct AccAddr {
   __device__ __forceinline__ int operator()(int coil, int col) const { return col * cg + (coil ^ (col & (cg - 1))); }
 };
 
-template <int W, uint32_t kFormat>
-__global__ void __launch_bounds__(kMaxThreads) k_rows(RowsArgs a) {
+// kBlocks CTAs per SM: 2 for rows of up to 384 columns (384 threads), 1
+// above; two resident CTAs let one block's FFT overlap another's gridding.
+template <int W, uint32_t kFormat, int kThreads, int kBlocks>
+__global__ void __launch_bounds__(kThreads, kBlocks) k_rows(RowsArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int row = blockIdx.x;
   const int cgi = blockIdx.y;
-  const int f = blockIdx.z;
+  const int f = a.frame0 + blockIdx.z;
   const int cg = a.coil_group;
   const int tid = threadIdx.x;
   const int nthreads = blockDim.x;
   const int lane = tid & 31;
-  const int warp = tid >> 5;
   float2* acc = reinterpret_cast<float2*>(smem_raw);
   float2* tw = acc + static_cast<size_t>(a.grid_cols) * cg;
   const AccAddr addr{cg};
@@ -525,87 +540,123 @@ __global__ void __launch_bounds__(kMaxThreads) k_rows(RowsArgs a) {
   for (int i = tid; i < a.grid_cols; i += nthreads) tw[i] = a.tw_cols[i];
   __syncthreads();
 
-  // ---- gridding: warp `warp` owns columns [32*warp, 32*warp + 32)
-  if (warp < a.nchunks) {
-    const int list = row * a.nchunks + warp;
-    const uint32_t* off = a.offsets + static_cast<size_t>(f) * (a.lists_per_frame + 1);
-    const uint32_t begin = off[list];
-    const int n = static_cast<int>(off[list + 1] - begin);
-    const uint32_t* ent = a.entries + static_cast<size_t>(f) * a.entries_per_frame + begin;
-    const int col_lo = warp * kChunk;
-    const int col_hi = min(col_lo + kChunk, a.grid_cols);
+  // ---- gridding.  A task is (column chunk, coil part): the chunk's sorted
+  // list applied to a subset of the coil group.  Cells of different coils are
+  // independent, so parts of one list run on different warps with every cell
+  // still summed in sample order; tasks are taken longest list first from a
+  // shared counter, so one long list does not leave the other warps idle.
+  const int parts = cg >= 32 ? 2 : 1;
+  const int cpart = cg / parts;
+  const int ntasks = a.nchunks * parts;
+  __shared__ int task_order[2 * (kMaxGrid / kChunk)];
+  __shared__ int task_next;
+  const uint32_t* off = a.offsets + static_cast<size_t>(f) * (a.lists_per_frame + 1);
+  if (tid == 0) {
+    int order[kMaxGrid / kChunk];
+    int len[kMaxGrid / kChunk];
+    for (int k = 0; k < a.nchunks; ++k) {
+      const int list = row * a.nchunks + k;
+      len[k] = static_cast<int>(off[list + 1] - off[list]);
+      int i = k;
+      while (i > 0 && len[order[i - 1]] < len[k]) {
+        order[i] = order[i - 1];
+        --i;
+      }
+      order[i] = k;
+    }
+    for (int i = 0; i < a.nchunks; ++i)
+      for (int p = 0; p < parts; ++p) task_order[i * parts + p] = order[i] * parts + p;
+    task_next = 0;
+  }
+  __syncthreads();
+  {
     const SampleRecord<W>* recs =
         reinterpret_cast<const SampleRecord<W>*>(a.records) + static_cast<size_t>(f) * a.samples;
-    // lanes: coil = lane % cgp, tap group = lane / cgp
-    int cgp = 1;
-    while (cgp < cg) cgp <<= 1;
-    const int ngroups = 32 / cgp;
-    const int my_coil = lane % cgp;
-    const int my_group = lane / cgp;
-    const int coil_global = cgi * cg + my_coil;
-    const bool coil_ok = my_coil < cg && coil_global < a.channels;
-    const size_t sample_base = static_cast<size_t>(f) * a.samples * a.channels + (coil_ok ? coil_global : 0);
+    // lanes: coil = lane % cpp, tap group = lane / cpp
+    int cpp = 1;
+    while (cpp < cpart) cpp <<= 1;
+    const int ngroups = 32 / cpp;
+    const int my_group = lane / cpp;
     bool bad = false;
     const void* ks = a.samples_t;
-    for (int base = 0; base < n; base += 32) {
-      const int cnt = min(32, n - base);
-      // lane i owns list entry base + i: its sample index, first tap column,
-      // the W tap weights of this row (row weight folded in) and dcf * phase
-      uint32_t my_s = 0;
-      int my_c0 = 0;
-      float2 my_scale = make_float2(0.0f, 0.0f);
-      float my_w[W];
+    for (;;) {
+      int task = 0;
+      if (lane == 0) task = atomicAdd(&task_next, 1);
+      task = __shfl_sync(0xffffffffu, task, 0);
+      if (task >= ntasks) break;
+      const int chunk = task_order[task] / parts;
+      const int part = task_order[task] - chunk * parts;
+      const int list = row * a.nchunks + chunk;
+      const uint32_t begin = off[list];
+      const int n = static_cast<int>(off[list + 1] - begin);
+      const uint32_t* ent = a.entries + static_cast<size_t>(f) * a.entries_per_frame + begin;
+      const int col_lo = chunk * kChunk;
+      const int col_hi = min(col_lo + kChunk, a.grid_cols);
+      const int my_coil = part * cpart + lane % cpp;  // coil index within the group
+      const int coil_global = cgi * cg + my_coil;
+      const bool coil_ok = (lane % cpp) < cpart && coil_global < a.channels;
+      const size_t sample_base = static_cast<size_t>(f) * a.samples * a.channels + (coil_ok ? coil_global : 0);
+      for (int base = 0; base < n; base += 32) {
+        const int cnt = min(32, n - base);
+        // lane i owns list entry base + i: its sample index, first tap column,
+        // the W tap weights of this row (row weight folded in) and dcf * phase
+        uint32_t my_s = 0;
+        int my_c0 = 0;
+        float2 my_scale = make_float2(0.0f, 0.0f);
+        float my_w[W];
 #pragma unroll
-      for (int j = 0; j < W; ++j) my_w[j] = 0.0f;
-      if (lane < cnt) {
-        my_s = __ldg(ent + base + lane);
-        const SampleRecord<W>& r = recs[my_s];
-        int ta = row - r.r0;
-        if (ta < 0) ta += a.grid_rows;
-        const float wr = r.wr[ta];
-        my_c0 = r.c0;
-        my_scale = r.scale;
+        for (int j = 0; j < W; ++j) my_w[j] = 0.0f;
+        if (lane < cnt) {
+          my_s = __ldg(ent + base + lane);
+          const SampleRecord<W>& r = recs[my_s];
+          int ta = row - r.r0;
+          if (ta < 0) ta += a.grid_rows;
+          const float wr = r.wr[ta];
+          my_c0 = r.c0;
+          my_scale = r.scale;
 #pragma unroll
-        for (int j = 0; j < W; ++j) my_w[j] = wr * r.wc[j];
-      }
-      // groups of 8 samples: all 8 coil loads in flight before the first use
-      for (int i0 = 0; i0 < cnt; i0 += 8) {
-        float2 yv[8];
-#pragma unroll
-        for (int k = 0; k < 8; ++k) {
-          const uint32_t sk = __shfl_sync(0xffffffffu, my_s, (i0 + k) & 31);
-          yv[k] = (coil_ok && i0 + k < cnt) ? load_sample<kFormat>(ks, sample_base + static_cast<size_t>(sk) * a.channels)
-                                             : make_float2(0.0f, 0.0f);
+          for (int j = 0; j < W; ++j) my_w[j] = wr * r.wc[j];
         }
+        // groups of kAhead samples: all their coil loads in flight before the first use
+        for (int i0 = 0; i0 < cnt; i0 += kAhead) {
+          float2 yv[kAhead];
 #pragma unroll
-        for (int k = 0; k < 8; ++k) {
-          const int i = i0 + k;
-          if (i >= cnt) break;
-          const int c0 = __shfl_sync(0xffffffffu, my_c0, i);
-          float2 sc;
-          sc.x = __shfl_sync(0xffffffffu, my_scale.x, i);
-          sc.y = __shfl_sync(0xffffffffu, my_scale.y, i);
-          float wt[W];
+          for (int k = 0; k < kAhead; ++k) {
+            const uint32_t sk = __shfl_sync(0xffffffffu, my_s, (i0 + k) & 31);
+            yv[k] = (coil_ok && i0 + k < cnt)
+                        ? load_sample<kFormat>(ks, sample_base + static_cast<size_t>(sk) * a.channels)
+                        : make_float2(0.0f, 0.0f);
+          }
 #pragma unroll
-          for (int j = 0; j < W; ++j) wt[j] = __shfl_sync(0xffffffffu, my_w[j], i);
-          if (coil_ok) {
-            bad |= !(isfinite(yv[k].x) && isfinite(yv[k].y));
-            const float2 v = cmul(yv[k], sc);
+          for (int k = 0; k < kAhead; ++k) {
+            const int i = i0 + k;
+            if (i >= cnt) break;
+            const int c0 = __shfl_sync(0xffffffffu, my_c0, i);
+            float2 sc;
+            sc.x = __shfl_sync(0xffffffffu, my_scale.x, i);
+            sc.y = __shfl_sync(0xffffffffu, my_scale.y, i);
+            float wt[W];
 #pragma unroll
-            for (int j = 0; j < W; ++j) {
-              if (j % ngroups != my_group) continue;
-              int col = c0 + j;
-              if (col >= a.grid_cols) col -= a.grid_cols;
-              if (col >= col_lo && col < col_hi) {
-                float2* cell = acc + addr(my_coil, col);
-                float2 c = *cell;
-                c.x = fmaf(v.x, wt[j], c.x);
-                c.y = fmaf(v.y, wt[j], c.y);
-                *cell = c;
+            for (int j = 0; j < W; ++j) wt[j] = __shfl_sync(0xffffffffu, my_w[j], i);
+            if (coil_ok) {
+              bad |= !(isfinite(yv[k].x) && isfinite(yv[k].y));
+              const float2 v = cmul(yv[k], sc);
+#pragma unroll
+              for (int j = 0; j < W; ++j) {
+                if (j % ngroups != my_group) continue;
+                int col = c0 + j;
+                if (col >= a.grid_cols) col -= a.grid_cols;
+                if (col >= col_lo && col < col_hi) {
+                  float2* cell = acc + addr(my_coil, col);
+                  float2 c = *cell;
+                  c.x = fmaf(v.x, wt[j], c.x);
+                  c.y = fmaf(v.y, wt[j], c.y);
+                  *cell = c;
+                }
               }
             }
+            __syncwarp();
           }
-          __syncwarp();
         }
       }
     }
@@ -637,19 +688,21 @@ __global__ void __launch_bounds__(kMaxThreads) k_rows(RowsArgs a) {
       src = pc - a.image_cols / 2;
       if (src < 0) src += a.grid_cols;
     }
-    const size_t o = ((static_cast<size_t>(f) * a.channels + cgi * cg + c) * a.grid_rows + row) * a.out_cols + pc;
+    const size_t o = ((static_cast<size_t>(f) * a.channels + cgi * cg + c) * a.grid_rows + row) * a.inter_pitch + pc;
     a.inter[o] = acc[addr(c, src)];
   }
 }
 
 struct ColsArgs {
-  const float2* inter;
   const float2* tw_rows;
   const float* inv_dr;
   const float* inv_dc;
   void* out;
+  uint32_t* flags;
+  int frame0;  // first frame of this pass
   int frames, channels, grid_rows, out_rows, out_cols, column_block, kb, image_rows;
-  uint32_t output;  // RSS or COIL_MAJOR (COIL_LAST goes through COIL_MAJOR + transpose)
+  int box_rows, boxes;  // TMA boxes of box_rows x column_block cover one column tile
+  uint32_t output;      // RSS or COIL_MAJOR (COIL_LAST goes through COIL_MAJOR + transpose)
   FftPlan plan;
 };
 
@@ -658,33 +711,66 @@ struct TileAddr {
   __device__ __forceinline__ int operator()(int line, int index) const { return index * pitch + line; }
 };
 
+constexpr uint32_t kWaitLimit = 1u << 22;  // mbarrier polls before a tile wait gives up
+
+// One CTA per (frame, column block).  The row-transformed grid
+// [frame][coil][grid_row][out_col] is read one coil tile (grid_rows x
+// column_block) at a time by TMA into a double buffer: while the block
+// transforms coil c, the copy of coil c+1 is in flight.  Each tile is
+// inverse-transformed along rows in place, cropped, deapodised, and either
+// written (coil-major) or squared into the channel-order RSS accumulators.
 template <int kOutPerThread>
-__global__ void __launch_bounds__(kMaxThreads) k_cols(ColsArgs a) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+__global__ void __launch_bounds__(kMaxThreads) k_cols(const __grid_constant__ CUtensorMap inter_map, ColsArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_cols[];
+  unsigned char* smem_raw = smem_cols;
   const int cb = a.column_block;
   const int col0 = blockIdx.x * cb;
   const int f = blockIdx.y;
+  const int fg = a.frame0 + f;
   const int tid = threadIdx.x;
   const int nthreads = blockDim.x;
-  float2* tile = reinterpret_cast<float2*>(smem_raw);
-  float2* tw = tile + static_cast<size_t>(a.grid_rows) * cb;
+  // each tile buffer starts on a 128-byte boundary (TMA destination)
+  const size_t tile_elems = (static_cast<size_t>(a.grid_rows) * cb + 15) & ~static_cast<size_t>(15);
+  float2* tiles = reinterpret_cast<float2*>(smem_raw + ((128u - (smem_addr(smem_raw) & 127u)) & 127u));
+  float2* tw = tiles + 2 * tile_elems;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(tw + a.grid_rows);
   const TileAddr addr{cb};
+  const uint32_t tile_bytes = static_cast<uint32_t>(static_cast<size_t>(a.grid_rows) * cb * sizeof(float2));
+  if (tid == 0) {
+    mbar_init(&bars[0], 1);
+    mbar_init(&bars[1], 1);
+    mbar_init_fence();
+  }
   for (int i = tid; i < a.grid_rows; i += nthreads) tw[i] = a.tw_rows[i];
+  __syncthreads();
+  auto issue = [&](int c, int b) {
+    float2* dst = tiles + b * tile_elems;
+    mbar_arrive_expect_tx(&bars[b], tile_bytes);
+    for (int k = 0; k < a.boxes; ++k)
+      tma_load_3d(dst + static_cast<size_t>(k) * a.box_rows * cb, &inter_map, col0, k * a.box_rows,
+                  fg * a.channels + c, &bars[b]);
+  };
+  if (tid == 0) issue(0, 0);
   const int ncols = min(cb, a.out_cols - col0);
   const int nout = a.out_rows * cb;
   float rss[kOutPerThread];
 #pragma unroll
   for (int k = 0; k < kOutPerThread; ++k) rss[k] = 0.0f;
-
+  bool ok = true;
+  int issued = 1;
   for (int c = 0; c < a.channels; ++c) {
-    const float2* src = a.inter + (static_cast<size_t>(f) * a.channels + c) * a.grid_rows * a.out_cols;
-    __syncthreads();
-    for (int i = tid; i < a.grid_rows * cb; i += nthreads) {
-      const int r = i / cb;
-      const int l = i - r * cb;
-      tile[i] = l < ncols ? src[static_cast<size_t>(r) * a.out_cols + col0 + l] : make_float2(0.0f, 0.0f);
+    const int b = c & 1;
+    if (tid == 0 && c + 1 < a.channels) {
+      fence_proxy_async_shared();  // this buffer was last written by the FFT (generic proxy)
+      issue(c + 1, b ^ 1);
+      ++issued;
     }
-    __syncthreads();
+    const bool mine = mbar_wait_bounded(&bars[b], static_cast<uint32_t>((c >> 1) & 1), kWaitLimit);
+    if (!__syncthreads_and(mine)) {
+      ok = false;
+      break;
+    }
+    float2* tile = tiles + b * tile_elems;
     fft_lines<kEmax>(tile, addr, a.plan, ilog2(cb), tw, tid, nthreads);
 #pragma unroll
     for (int k = 0; k < kOutPerThread; ++k) {
@@ -709,11 +795,21 @@ __global__ void __launch_bounds__(kMaxThreads) k_cols(ColsArgs a) {
             rss[k] = __fadd_rn(rss[k], __fadd_rn(__fmul_rn(x.x, x.x), __fmul_rn(x.y, x.y)));
           } else {
             float2* o = static_cast<float2*>(a.out);
-            o[((static_cast<size_t>(f) * a.channels + c) * a.out_rows + pr) * a.out_cols + col0 + l] = x;
+            o[((static_cast<size_t>(fg) * a.channels + c) * a.out_rows + pr) * a.out_cols + col0 + l] = x;
           }
         }
       }
     }
+    __syncthreads();
+  }
+  if (!ok) {
+    // a copy never completed: report, then give every copy this block issued
+    // a bounded chance to land before the block's shared memory is released
+    if (tid == 0) {
+      atomicOr(a.flags, KSJ_GPU_FLAG_WAIT_TIMEOUT);
+      for (int u = 0; u < issued; ++u) mbar_wait_bounded(&bars[u & 1], static_cast<uint32_t>((u >> 1) & 1), kWaitLimit);
+    }
+    return;
   }
   if (a.output == KSJ_GPU_OUTPUT_RSS) {
     float* o = static_cast<float*>(a.out);
@@ -723,7 +819,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_cols(ColsArgs a) {
       if (i < nout) {
         const int pr = i / cb;
         const int l = i - pr * cb;
-        if (l < ncols) o[(static_cast<size_t>(f) * a.out_rows + pr) * a.out_cols + col0 + l] = __fsqrt_rn(rss[k]);
+        if (l < ncols) o[(static_cast<size_t>(fg) * a.out_rows + pr) * a.out_cols + col0 + l] = __fsqrt_rn(rss[k]);
       }
     }
   }
@@ -736,7 +832,44 @@ size_t rows_smem_bytes(const Shape& s) {
 }
 
 size_t cols_smem_bytes(const Shape& s) {
-  return static_cast<size_t>(s.grid_rows) * s.column_block * sizeof(float2) + s.grid_rows * sizeof(float2);
+  const size_t tile = (static_cast<size_t>(s.grid_rows) * s.column_block + 15) & ~static_cast<size_t>(15);
+  return 128 + 2 * tile * sizeof(float2) + s.grid_rows * sizeof(float2) + 2 * sizeof(uint64_t);
+}
+
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_tiled() {
+  static EncodeTiledFn fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    return reinterpret_cast<EncodeTiledFn>(p);
+  }();
+  return fn;
+}
+
+// Tensor map over the row-transformed grid [frame*coil][grid_row][out_col]
+// of 8-byte elements, box (column_block, box_rows, 1).
+bool make_inter_map(const Shape& s, void* inter, CUtensorMap* map, int* box_rows, int* boxes) {
+  EncodeTiledFn enc = encode_tiled();
+  if (enc == nullptr) return false;
+  int nb = 1;
+  while (s.grid_rows / nb > 256 || s.grid_rows % nb != 0) ++nb;
+  *boxes = nb;
+  *box_rows = s.grid_rows / nb;
+  const cuuint64_t dims[3] = {static_cast<cuuint64_t>(s.out_cols), static_cast<cuuint64_t>(s.grid_rows),
+                              static_cast<cuuint64_t>(s.frames) * s.channels};
+  const cuuint64_t strides[2] = {static_cast<cuuint64_t>(s.inter_pitch) * 8,
+                                 static_cast<cuuint64_t>(s.inter_pitch) * s.grid_rows * 8};
+  const cuuint32_t box[3] = {static_cast<cuuint32_t>(s.column_block), static_cast<cuuint32_t>(*box_rows), 1};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  return enc(map, CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, inter, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+             CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 int cols_threads(const Shape& s) {
@@ -833,82 +966,92 @@ ksj_gpu_status launch_all(const Shape& s, const Layout& l, const ksj_gpu_griddin
           static_cast<const unsigned long long*>(d_kspace), reinterpret_cast<unsigned long long*>(ws + l.samples_t),
           s.channels, s.samples);
   }
-  {
-    RowsArgs r{};
-    r.samples_t = ws + l.samples_t;
-    r.records = records;
-    r.offsets = offsets;
-    r.entries = entries;
-    r.tw_cols = tw_cols;
-    r.inter = inter;
-    r.flags = flags;
-    r.frames = s.frames;
-    r.channels = s.channels;
-    r.samples = s.samples;
-    r.grid_rows = s.grid_rows;
-    r.grid_cols = s.grid_cols;
-    r.nchunks = s.nchunks;
-    r.lists_per_frame = s.lists_per_frame;
-    r.entries_per_frame = s.entries_per_frame;
-    r.coil_group = s.coil_group;
-    r.out_cols = s.out_cols;
-    r.kb = s.kb ? 1 : 0;
-    r.image_cols = s.cols;
-    r.plan = s.plan_cols;
-    const size_t smem = rows_smem_bytes(s);
-    auto kern = k_rows<W, kFormat>;
-    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)) !=
-        cudaSuccess)
-      return KSJ_GPU_ERROR_CUDA;
-    const dim3 grid(s.grid_rows, (s.channels + s.coil_group - 1) / s.coil_group, s.frames);
-    const int threads = std::max(64, s.nchunks * 32);
-    LaunchScope scope("k_rows", stream);
-    kern<<<grid, threads, smem, stream>>>(r);
-  }
-  {
-    ColsArgs c{};
-    c.inter = inter;
-    c.tw_rows = tw_rows;
-    c.inv_dr = inv_dr;
-    c.inv_dc = inv_dc;
-    c.frames = s.frames;
-    c.channels = s.channels;
-    c.grid_rows = s.grid_rows;
-    c.out_rows = s.out_rows;
-    c.out_cols = s.out_cols;
-    c.column_block = s.column_block;
-    c.kb = s.kb ? 1 : 0;
-    c.image_rows = s.rows;
-    c.plan = s.plan_rows;
-    const bool coil_last = d->output == KSJ_GPU_OUTPUT_COIL_LAST;
-    c.output = d->output == KSJ_GPU_OUTPUT_RSS ? KSJ_GPU_OUTPUT_RSS : KSJ_GPU_OUTPUT_COIL_MAJOR;
-    c.out = coil_last ? static_cast<void*>(ws + l.coil_major) : d_out;
-    const int threads = cols_threads(s);
-    const int per = (s.out_rows * s.column_block + threads - 1) / threads;
-    const size_t smem = cols_smem_bytes(s);
-    const dim3 grid((s.out_cols + s.column_block - 1) / s.column_block, s.frames);
-    auto pick = [&](auto kern) -> ksj_gpu_status {
-      if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)) !=
-          cudaSuccess)
-        return KSJ_GPU_ERROR_CUDA;
-      LaunchScope scope("k_cols", stream);
-      kern<<<grid, threads, smem, stream>>>(c);
-      return KSJ_GPU_OK;
-    };
-    ksj_gpu_status st;
-    if (per <= 4) st = pick(k_cols<4>);
-    else if (per <= 8) st = pick(k_cols<8>);
-    else if (per <= 16) st = pick(k_cols<16>);
-    else return KSJ_GPU_ERROR_UNSUPPORTED;
-    if (st != KSJ_GPU_OK) return st;
-    if (coil_last) {
-      const int pixels = s.out_rows * s.out_cols;
-      const dim3 tg((pixels + 31) / 32, (s.channels + 31) / 32, s.frames);
-      LaunchScope scope("k_images_coil_last", stream);
-      k_transpose<unsigned long long><<<tg, dim3(32, 8), 0, stream>>>(
-          reinterpret_cast<const unsigned long long*>(ws + l.coil_major), static_cast<unsigned long long*>(d_out),
-          s.channels, pixels);
+  RowsArgs r{};
+  r.samples_t = ws + l.samples_t;
+  r.records = records;
+  r.offsets = offsets;
+  r.entries = entries;
+  r.tw_cols = tw_cols;
+  r.inter = inter;
+  r.flags = flags;
+  r.frames = s.frames;
+  r.channels = s.channels;
+  r.samples = s.samples;
+  r.grid_rows = s.grid_rows;
+  r.grid_cols = s.grid_cols;
+  r.nchunks = s.nchunks;
+  r.lists_per_frame = s.lists_per_frame;
+  r.entries_per_frame = s.entries_per_frame;
+  r.coil_group = s.coil_group;
+  r.out_cols = s.out_cols;
+  r.inter_pitch = s.inter_pitch;
+  r.kb = s.kb ? 1 : 0;
+  r.image_cols = s.cols;
+  r.plan = s.plan_cols;
+  const size_t rows_smem = rows_smem_bytes(s);
+  const int rows_threads = std::max(64, s.nchunks * 32);
+  auto rows_kernel = (rows_threads <= 384 && s.rows_blocks == 2) ? k_rows<W, kFormat, 384, 2>
+                                                                 : k_rows<W, kFormat, kMaxThreads, 1>;
+  if (cudaFuncSetAttribute(rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(rows_smem)) !=
+          cudaSuccess ||
+      cudaFuncSetAttribute(rows_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100) != cudaSuccess)
+    return KSJ_GPU_ERROR_CUDA;
+
+  ColsArgs c{};
+  c.tw_rows = tw_rows;
+  c.inv_dr = inv_dr;
+  c.inv_dc = inv_dc;
+  c.flags = flags;
+  c.frames = s.frames;
+  c.channels = s.channels;
+  c.grid_rows = s.grid_rows;
+  c.out_rows = s.out_rows;
+  c.out_cols = s.out_cols;
+  c.column_block = s.column_block;
+  c.kb = s.kb ? 1 : 0;
+  c.image_rows = s.rows;
+  c.plan = s.plan_rows;
+  const bool coil_last = d->output == KSJ_GPU_OUTPUT_COIL_LAST;
+  c.output = d->output == KSJ_GPU_OUTPUT_RSS ? KSJ_GPU_OUTPUT_RSS : KSJ_GPU_OUTPUT_COIL_MAJOR;
+  c.out = coil_last ? static_cast<void*>(ws + l.coil_major) : d_out;
+  CUtensorMap map;
+  if (!make_inter_map(s, inter, &map, &c.box_rows, &c.boxes)) return KSJ_GPU_ERROR_CUDA;
+  const int cols_thr = cols_threads(s);
+  const int per = (s.out_rows * s.column_block + cols_thr - 1) / cols_thr;
+  const size_t cols_smem = cols_smem_bytes(s);
+  void (*cols_kernel)(const __grid_constant__ CUtensorMap, ColsArgs) = nullptr;
+  if (per <= 4) cols_kernel = k_cols<4>;
+  else if (per <= 8) cols_kernel = k_cols<8>;
+  else if (per <= 16) cols_kernel = k_cols<16>;
+  else return KSJ_GPU_ERROR_UNSUPPORTED;
+  if (cudaFuncSetAttribute(cols_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(cols_smem)) !=
+          cudaSuccess ||
+      cudaFuncSetAttribute(cols_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100) != cudaSuccess)
+    return KSJ_GPU_ERROR_CUDA;
+
+  // frames in passes sized so one pass's row-transformed grid stays in L2
+  for (int f0 = 0; f0 < s.frames; f0 += s.frames_per_pass) {
+    const int nf = std::min(s.frames_per_pass, s.frames - f0);
+    r.frame0 = f0;
+    c.frame0 = f0;
+    {
+      LaunchScope scope("k_rows", stream);
+      const dim3 grid(s.grid_rows, (s.channels + s.coil_group - 1) / s.coil_group, nf);
+      rows_kernel<<<grid, rows_threads, rows_smem, stream>>>(r);
     }
+    {
+      LaunchScope scope("k_cols", stream);
+      const dim3 grid((s.out_cols + s.column_block - 1) / s.column_block, nf);
+      cols_kernel<<<grid, cols_thr, cols_smem, stream>>>(map, c);
+    }
+  }
+  if (coil_last) {
+    const int pixels = s.out_rows * s.out_cols;
+    const dim3 tg((pixels + 31) / 32, (s.channels + 31) / 32, s.frames);
+    LaunchScope scope("k_images_coil_last", stream);
+    k_transpose<unsigned long long><<<tg, dim3(32, 8), 0, stream>>>(
+        reinterpret_cast<const unsigned long long*>(ws + l.coil_major), static_cast<unsigned long long*>(d_out),
+        s.channels, pixels);
   }
   return check_launch();
 }
@@ -1038,11 +1181,17 @@ extern "C" ksj_gpu_status ksj_gpu_gridding_tune(const ksj_gpu_gridding_desc* des
   float best_ms = 1e30f;
   for (uint32_t cg : {32u, 16u, 8u, 4u, 2u, 1u}) {
     if (cg > 1 && cg / 2 >= desc->channels) continue;
-    for (uint32_t cb : {8u, 16u, 32u}) {
+    if (cg * 4 < desc->channels && cg < 8) continue;
+    for (uint32_t cb : {4u, 8u, 16u})
+    for (uint32_t fpp : {0u, 12u})
+    for (uint32_t rb : {1u, 2u}) {
+      if (fpp >= desc->frames) continue;
       ksj_gpu_gridding_tuning t{};
       t.struct_size = sizeof(t);
       t.coil_group = cg;
       t.column_block = cb;
+      t.frames_per_pass = fpp;
+      t.rows_blocks_per_sm = rb;
       Shape s{};
       if (make_shape(desc, &t, &s) != KSJ_GPU_OK) continue;
       if (workspace_bytes < make_layout(s, desc).total) continue;

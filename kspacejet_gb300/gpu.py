@@ -17,7 +17,7 @@ KERNEL_LINEAR, KERNEL_KAISER_BESSEL = 0, 1
 DCF_NONE, DCF_ANALYTIC_RAMP, DCF_EXTERNAL = 0, 1, 2
 OUTPUT_COIL_LAST, OUTPUT_RSS, OUTPUT_COIL_MAJOR = 0, 1, 2
 SAMPLES_CF32, SAMPLES_BF16 = 0, 1
-FLAG_NONFINITE_SAMPLE, FLAG_BAD_TRAJECTORY, FLAG_BAD_DCF = 1, 2, 4
+FLAG_NONFINITE_SAMPLE, FLAG_BAD_TRAJECTORY, FLAG_BAD_DCF, FLAG_WAIT_TIMEOUT = 1, 2, 4, 8
 
 STATUS_TEXT = {0: "ok", 1: "invalid argument", 2: "unsupported", 3: "CUDA error", 4: "workspace",
                5: "out of memory", 6: "non-finite input"}
@@ -41,7 +41,8 @@ class GriddingDesc(ctypes.Structure):
 
 class GriddingTuning(ctypes.Structure):
     _fields_ = [("struct_size", ctypes.c_uint32), ("coil_group", ctypes.c_uint32),
-                ("column_block", ctypes.c_uint32), ("list_capacity", ctypes.c_uint32)]
+                ("column_block", ctypes.c_uint32), ("list_capacity", ctypes.c_uint32),
+                ("frames_per_pass", ctypes.c_uint32), ("rows_blocks_per_sm", ctypes.c_uint32)]
 
 
 _lib = None

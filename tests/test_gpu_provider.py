@@ -113,3 +113,35 @@ def test_nonfinite_sample_is_an_internal_error_with_released_grant(recon, cuda):
     tr = np.array([0.0, 0.0, math.pi, -0.5 * math.pi], dtype=np.float32)
     r = _fire(recon, "radial_gridding_reconstruct", H.radial_config(1, 2, 2, 2), ks, tr, 1, 4, 104)
     assert r.status == H.INTERNAL_ERROR and r.seal_calls == 0 and r.release_calls == 1
+
+
+def test_kaiser_bessel_plugin_matches_the_c_abi(native, orc, cuda):
+    """radial_kb_gridding_reconstruct / _rss through the plug-in equal the C-ABI
+    call on the same inputs (the plug-in adds only copies and validation)."""
+    import torch
+    from kspacejet_gb300 import gpu, synth
+
+    tr = synth.golden_angle_radial(128, 40, first_spoke=5)
+    ks = synth.multicoil_kspace(tr, 64, 3, seed=5)
+    cfg = ('{"channels":3,"density_compensation":"radial_analytic_ramp","grid_cols":128,"grid_rows":128,'
+           '"image_cols":64,"image_rows":64,"kernel_width":4,"sample_count":%d,'
+           '"trajectory_units":"radians_per_pixel"}' % tr.shape[0])
+    m = H.ProviderModule(native.KB_PLUGIN)
+    try:
+        coils = H.aligned((64 * 64 * 3,), np.complex64)
+        with m.instance("radial_kb_gridding_reconstruct", cfg) as inst:
+            r = inst.fire([(H.aligned_copy(ks), H.TYPE_KSPACE, 0), (H.aligned_copy(tr.ravel()), H.TYPE_TRAJECTORY, 1)],
+                          coils, H.TYPE_COIL_IMAGE)
+        assert r.status == 0 and r.consumed == 2
+        rss = H.aligned((64, 64), np.float32)
+        with m.instance("radial_kb_gridding_rss", cfg) as inst:
+            r = inst.fire([(H.aligned_copy(ks), H.TYPE_KSPACE, 0), (H.aligned_copy(tr.ravel()), H.TYPE_TRAJECTORY, 1)],
+                          rss, H.TYPE_IMAGE)
+        assert r.status == 0
+    finally:
+        m.close()
+    g = gpu.kb_gridding(image=64, grid=128, channels=3, samples=tr.shape[0], output=gpu.OUTPUT_COIL_LAST)
+    out = g.new_output(cuda)
+    g.run(torch.from_numpy(ks[None]).to(cuda), torch.from_numpy(tr[None]).to(cuda), out, g.new_workspace(cuda))
+    assert out.cpu().numpy()[0].tobytes() == coils.reshape(64, 64, 3).tobytes()
+    assert orc.rss(coils.reshape(64, 64, 3)).tobytes() == rss.tobytes()

@@ -170,3 +170,32 @@ def test_coil_combine_contract(native):
             assert r.status == H.CONTRACT_VIOLATION and r.acquire_calls == 1 and r.seal_calls == 0
     finally:
         m.close()
+
+
+def kb_config(channels=2, image=32, grid=64, width=4, samples=64, dcf="radial_analytic_ramp"):
+    return (f'{{"channels":{channels},"density_compensation":"{dcf}","grid_cols":{grid},"grid_rows":{grid},'
+            f'"image_cols":{image},"image_rows":{image},"kernel_width":{width},"sample_count":{samples},'
+            f'"trajectory_units":"radians_per_pixel"}}')
+
+
+def test_kaiser_bessel_plugin_descriptor_and_configs(native):
+    import hashlib
+
+    m = H.ProviderModule(native.KB_PLUGIN)
+    try:
+        ids = ["radial_kb_gridding_reconstruct", "radial_kb_gridding_rss"]
+        assert m.provider_id == "org.kspacejet.gb300-noncartesian-recon"
+        fields = ["kspacejet.provider-bundle", m.provider_id] + ids
+        assert m.digest_hex == hashlib.sha256(b"".join(f.encode() + b"\0" for f in fields)).hexdigest()
+        assert [o.id for o in m.operators] == ids
+        assert all(o.max_scratch_bytes == 0 and o.max_in_flight == 1 for o in m.operators)
+        for op in ids:
+            assert m.try_create(op, kb_config())[:2] == (0, True)
+            assert m.try_create(op, kb_config(grid=384, image=192, channels=32, samples=13056))[:2] == (0, True)
+            assert m.try_create(op, kb_config(dcf="none"))[:2] == (0, True)
+            for bad in [kb_config(width=5), kb_config(width=10), kb_config(grid=20), kb_config(grid=32, image=64),
+                        kb_config(dcf="pipe_menon"), kb_config(channels=65), kb_config(grid=1024, image=512),
+                        kb_config().replace('"grid_cols"', '"grid_colz"')]:
+                assert m.try_create(op, bad)[0] == H.INVALID_ARGUMENT, bad
+    finally:
+        m.close()
