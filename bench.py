@@ -377,7 +377,8 @@ def run_ours(args) -> dict | None:
         "config": workload_config({"parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                                    "tuning": {"coil_group": tuning.coil_group, "column_block": tuning.column_block,
                                               "frames_per_pass": tuning.frames_per_pass or FRAMES,
-                                              "rows_blocks_per_sm": tuning.rows_blocks_per_sm},
+                                              "rows_blocks_per_sm": tuning.rows_blocks_per_sm,
+                                              "coil_parts": tuning.coil_parts or 1},
                                    "gridded_samples_per_step_per_gpu": per_step}),
         "e2e": {"value": e2e, "unit": "samples/s", "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": int(ksp_h.nbytes + traj_h.nbytes), "d2h_bytes_per_step": int(out.numel() * 4)},
@@ -416,16 +417,117 @@ def run_reference(args) -> dict | None:
             "cpu_baseline": cpu}
 
 
+# ------------------------------------------------------- served stream
+
+SERVE_READOUTS = (128, 256, 384, 512)
+
+
+def serve_workload(n: int, seed: int):
+    """n slice requests: readout uniform in {128,256,384,512}, spokes uniform in
+    64..805, coils uniform in 8..32, image = readout/2 on a readout^2 grid
+    (sigma = 2, KB W=4), ramp DCF, RSS output.  Inputs are pinned host memory;
+    the k-space of every request is a prefix of one seeded random buffer (the
+    inputs are read-only, so requests may share it)."""
+    import torch
+    from kspacejet_gb300 import serve, synth
+
+    rng = np.random.default_rng(seed)
+    shapes = [(int(rng.choice(SERVE_READOUTS)), int(rng.integers(64, 806)), int(rng.integers(8, 33)))
+              for _ in range(n)]
+    biggest = max(r * sp * c for r, sp, c in shapes)
+    base = torch.from_numpy((rng.standard_normal(biggest) + 1j * rng.standard_normal(biggest)).astype(np.complex64))
+    base = base.pin_memory()
+    trajs = {}
+    reqs = []
+    for ro, sp, co in shapes:
+        if (ro, sp) not in trajs:
+            trajs[(ro, sp)] = torch.from_numpy(synth.golden_angle_radial(ro, sp)).pin_memory()
+        tr = trajs[(ro, sp)]
+        m = ro * sp
+        out = torch.empty((ro // 2, ro // 2), dtype=torch.float32).pin_memory()
+        r = serve.Request(image=ro // 2, grid=ro, kspace=base[: co * m].numpy().reshape(co, m),
+                          trajectory=tr.numpy(), trajectory_id=ro * 10000 + sp, pinned=True, out=out.numpy())
+        r._keep = (tr, out)
+        reqs.append(r)
+    return reqs, base
+
+
+def serve_pass(server, reqs, arrivals=None) -> dict:
+    """Submit reqs (at the given arrival offsets in seconds, or all at once),
+    wait for all, return the loop's statistics."""
+    server.reset_stats()
+    t0 = time.perf_counter()
+    tickets = []
+    for i, r in enumerate(reqs):
+        if arrivals is not None:
+            delay = t0 + arrivals[i] - time.perf_counter()
+            if delay > 0:
+                time.sleep(delay)
+        tickets.append(server.submit(r))
+    for t in tickets:
+        server.wait(t, timeout_ms=120000)
+    st = server.stats()
+    st["samples_per_s"] = st["gridded_samples"] / st["wall_seconds"] if st["wall_seconds"] > 0 else None
+    return st
+
+
+def run_serve(args) -> dict:
+    import torch
+    from kspacejet_gb300 import serve
+
+    torch.cuda.init()
+    n = args.serve_requests
+    reqs, _base = serve_workload(n, seed=11)
+    warm, _ = serve_workload(8, seed=12)
+    samples = sum(r.kspace.size for r in reqs)
+    out = {"metric": "served gridded samples/s", "unit": "samples/s", "higher_is_better": True, "n_gpus": 1,
+           "data": "synthetic", "dtype": "f32 (complex64 samples, float32 gridding/FFT)",
+           "config": {"workload": "served stream of 2D radial slices (KB W=4, sigma=2, ramp DCF, RSS)",
+                      "requests": n, "readout": list(SERVE_READOUTS), "spokes": [64, 805], "coils": [8, 32],
+                      "gridded_samples": samples, "inputs": "pinned host memory, results to pinned host memory",
+                      "slots": args.serve_slots}}
+    results = {}
+    for name, slots in (("serial", 1), ("served", args.serve_slots)):
+        with serve.Server(slots=slots, device_memory_cap=args.serve_cap_gib << 30) as s:
+            serve_pass(s, warm)
+            serve_pass(s, reqs)  # first pass uploads and caches the trajectories
+            burst = serve_pass(s, reqs)
+            results[name] = {"burst": burst}
+    # Poisson arrivals at 90% of the serial path's burst throughput
+    rate = 0.9 * n / results["serial"]["burst"]["wall_seconds"]
+    rng = np.random.default_rng(13)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, size=n))
+    for name, slots in (("serial", 1), ("served", args.serve_slots)):
+        with serve.Server(slots=slots, device_memory_cap=args.serve_cap_gib << 30) as s:
+            serve_pass(s, warm)
+            serve_pass(s, reqs)
+            results[name]["poisson"] = serve_pass(s, reqs, arrivals)
+    out["value"] = results["served"]["burst"]["samples_per_s"]
+    out["serial_value"] = results["serial"]["burst"]["samples_per_s"]
+    out["poisson_rate_per_s"] = rate
+    out["results"] = results
+    return out
+
+
 def main() -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--serve", action="store_true", help="served-stream benchmark (separate JSON line)")
+    ap.add_argument("--serve-requests", type=int, default=160)
+    ap.add_argument("--serve-slots", type=int, default=4)
+    ap.add_argument("--serve-cap-gib", type=int, default=24)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
-    if args.impl == "reference":
+    if args.serve:
+        import kspacejet_gb300
+
+        kspacejet_gb300.build()
+        res = run_serve(args)
+    elif args.impl == "reference":
         res = run_reference(args)
     else:
         import kspacejet_gb300

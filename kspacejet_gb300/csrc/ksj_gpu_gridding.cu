@@ -82,7 +82,7 @@ struct Shape {
   float beta, inv_i0_beta;
   float row_origin, col_origin;
   float phase_row, phase_col, phase_sign;  // origin-phase coefficients
-  int coil_group, column_block, list_capacity, frames_per_pass, rows_blocks;
+  int coil_group, column_block, list_capacity, frames_per_pass, rows_blocks, coil_parts;
   FftPlan plan_rows, plan_cols;
 };
 
@@ -203,13 +203,20 @@ ksj_gpu_status make_shape(const ksj_gpu_gridding_desc* d, const ksj_gpu_gridding
   s->list_capacity = cap;
   // frames per k_rows/k_cols pass: keep one pass's row-transformed grid
   // (channels x grid_rows x out_cols complex) within ~64 MB of L2
-  int fpp = t && t->struct_size >= sizeof(ksj_gpu_gridding_tuning) ? static_cast<int>(t->frames_per_pass) : 0;
+  // fields appended to the tuning struct are read only when the caller's
+  // struct_size covers them
+  auto has = [&](size_t field_end) { return t != nullptr && t->struct_size >= field_end; };
+  int fpp = has(offsetof(ksj_gpu_gridding_tuning, frames_per_pass) + 4) ? static_cast<int>(t->frames_per_pass) : 0;
   if (fpp <= 0) fpp = s->frames;
   s->frames_per_pass = std::min(fpp, s->frames);
-  int rb = t && t->struct_size >= sizeof(ksj_gpu_gridding_tuning) ? static_cast<int>(t->rows_blocks_per_sm) : 0;
+  int rb = has(offsetof(ksj_gpu_gridding_tuning, rows_blocks_per_sm) + 4) ? static_cast<int>(t->rows_blocks_per_sm) : 0;
   if (rb == 0) rb = 1;
   if (rb != 1 && rb != 2) return KSJ_GPU_ERROR_INVALID_ARGUMENT;
   s->rows_blocks = rb;
+  int parts = has(offsetof(ksj_gpu_gridding_tuning, coil_parts) + 4) ? static_cast<int>(t->coil_parts) : 0;
+  if (parts == 0) parts = 1;
+  if ((parts != 1 && parts != 2) || parts > cg) return KSJ_GPU_ERROR_INVALID_ARGUMENT;
+  s->coil_parts = parts;
   return KSJ_GPU_OK;
 }
 
@@ -506,7 +513,7 @@ struct RowsArgs {
   uint32_t* flags;
   int frames, channels, samples, grid_rows, grid_cols, nchunks, lists_per_frame;
   size_t entries_per_frame;
-  int coil_group;
+  int coil_group, coil_parts;
   int out_cols, inter_pitch, kb, image_cols;
   FftPlan plan;
 };
@@ -545,7 +552,7 @@ __global__ void __launch_bounds__(kThreads, kBlocks) k_rows(RowsArgs a) {
   // independent, so parts of one list run on different warps with every cell
   // still summed in sample order; tasks are taken longest list first from a
   // shared counter, so one long list does not leave the other warps idle.
-  const int parts = cg >= 32 ? 2 : 1;
+  const int parts = a.coil_parts;
   const int cpart = cg / parts;
   const int ntasks = a.nchunks * parts;
   __shared__ int task_order[2 * (kMaxGrid / kChunk)];
@@ -983,6 +990,7 @@ ksj_gpu_status launch_all(const Shape& s, const Layout& l, const ksj_gpu_griddin
   r.lists_per_frame = s.lists_per_frame;
   r.entries_per_frame = s.entries_per_frame;
   r.coil_group = s.coil_group;
+  r.coil_parts = s.coil_parts;
   r.out_cols = s.out_cols;
   r.inter_pitch = s.inter_pitch;
   r.kb = s.kb ? 1 : 0;
@@ -1184,14 +1192,17 @@ extern "C" ksj_gpu_status ksj_gpu_gridding_tune(const ksj_gpu_gridding_desc* des
     if (cg * 4 < desc->channels && cg < 8) continue;
     for (uint32_t cb : {4u, 8u, 16u})
     for (uint32_t fpp : {0u, 12u})
-    for (uint32_t rb : {1u, 2u}) {
+    for (uint32_t rb : {1u, 2u})
+    for (uint32_t parts : {1u, 2u}) {
       if (fpp >= desc->frames) continue;
+      if (parts > 1 && cg < 16) continue;
       ksj_gpu_gridding_tuning t{};
       t.struct_size = sizeof(t);
       t.coil_group = cg;
       t.column_block = cb;
       t.frames_per_pass = fpp;
       t.rows_blocks_per_sm = rb;
+      t.coil_parts = parts;
       Shape s{};
       if (make_shape(desc, &t, &s) != KSJ_GPU_OK) continue;
       if (workspace_bytes < make_layout(s, desc).total) continue;
