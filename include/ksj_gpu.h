@@ -161,6 +161,33 @@ KSJ_GPU_API ksj_gpu_status ksj_gpu_direct_adjoint(uint32_t rows, uint32_t cols, 
                                                   const float* d_traj, void* d_out, void* d_workspace,
                                                   size_t workspace_bytes, void* stream);
 
+/* The direct NUDFT adjoint above without a caller workspace and without any
+ * allocation.  No counterpart in the reference: its direct adjoint
+ * (libs/numerics/kspacejet-nufft/src/eigen/eigen_nufft_direct_nudft.cpp:77-97)
+ * is a CPU loop writing the image in place.  For callers that cannot allocate device memory at call
+ * time: hosts that bind only this C ABI and own no device allocator, and
+ * latency-bound loops where cudaMalloc/cudaFree would synchronise the device
+ * and stall every other stream.  Same kernels and same output as
+ * ksj_gpu_direct_adjoint.
+ *   - The coil-major intermediate lives in a file-scope device array of
+ *     ksj_gpu_direct_static_scratch_bytes() = 8 MiB per device, so
+ *     rows * cols * channels <= 1,048,576 (e.g. 128 x 128 x 64, 256 x 256 x 16);
+ *     larger requests return KSJ_GPU_ERROR_WORKSPACE before any device work.
+ *   - Nothing needs to start at zero: every scratch element the call reads
+ *     was written earlier in the same call.
+ *   - The first call on each device (with that device current) looks up the
+ *     array's address, which may load the module; make that first call before
+ *     any stream capture.  The device used is the current device; `stream`
+ *     must belong to it.
+ *   - All calls on one device share the one array: calls that overlap in time
+ *     (different streams, or host threads without ordering) race on it and
+ *     give wrong results.  Serialise them, e.g. on one stream. */
+KSJ_GPU_API size_t ksj_gpu_direct_static_scratch_bytes(void);
+KSJ_GPU_API ksj_gpu_status ksj_gpu_direct_adjoint_static(uint32_t rows, uint32_t cols, double row_origin,
+                                                         double col_origin, uint32_t channels, uint32_t samples,
+                                                         const void* d_kspace, const float* d_traj, void* d_out,
+                                                         void* stream);
+
 /* --------------------------------------------------------------- combine */
 
 /* Root-sum-of-squares over the channel (last) axis:

@@ -354,3 +354,69 @@ extern "C" uint32_t ksj_gpu_timing_read(uint32_t max_entries, char* names, uint6
   }
   return static_cast<uint32_t>(g_totals.size());
 }
+
+// --------------------------------------- direct NUDFT, static device scratch
+//
+// ksj_gpu_direct_adjoint_static runs the kernels of ksj_gpu_direct_adjoint
+// with the coil-major intermediate in a file-scope device array instead of a
+// caller workspace, so the call itself allocates nothing.  The array's address
+// is looked up once per device (with that device current) and kept.
+
+namespace ksj_gpu {
+namespace {
+constexpr size_t kDirectStaticScratchBytes = size_t(8) << 20;  // rows x cols x channels x 8 B at most
+__device__ __align__(256) unsigned char g_direct_scratch[kDirectStaticScratchBytes];
+constexpr int kStaticScratchDevices = 64;
+std::mutex g_direct_scratch_mutex;
+void* g_direct_scratch_ptr[kStaticScratchDevices] = {};
+}  // namespace
+}  // namespace ksj_gpu
+
+extern "C" size_t ksj_gpu_direct_static_scratch_bytes(void) { return kDirectStaticScratchBytes; }
+
+extern "C" ksj_gpu_status ksj_gpu_direct_adjoint_static(uint32_t rows, uint32_t cols, double row_origin,
+                                                        double col_origin, uint32_t channels, uint32_t samples,
+                                                        const void* d_kspace, const float* d_traj, void* d_out,
+                                                        void* stream) {
+  if (rows == 0 || cols == 0 || channels == 0 || samples == 0 || d_kspace == nullptr || d_traj == nullptr ||
+      d_out == nullptr)
+    return KSJ_GPU_ERROR_INVALID_ARGUMENT;
+  if (rows > 8192 || cols > 8192 || static_cast<uint64_t>(rows) * cols > (1u << 26))
+    return KSJ_GPU_ERROR_UNSUPPORTED;
+  const float ro = static_cast<float>(row_origin), co = static_cast<float>(col_origin);
+  if (static_cast<double>(ro) != row_origin || static_cast<double>(co) != col_origin)
+    return KSJ_GPU_ERROR_UNSUPPORTED;
+  // the intermediate must fit the static array: rejected before any device work
+  if (static_cast<uint64_t>(rows) * cols * channels * sizeof(float2) > kDirectStaticScratchBytes)
+    return KSJ_GPU_ERROR_WORKSPACE;
+  int device = 0;
+  if (cudaGetDevice(&device) != cudaSuccess) return KSJ_GPU_ERROR_CUDA;
+  if (device < 0 || device >= kStaticScratchDevices) return KSJ_GPU_ERROR_UNSUPPORTED;
+  void* scratch = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_direct_scratch_mutex);
+    if (g_direct_scratch_ptr[device] == nullptr) {
+      void* p = nullptr;
+      if (cudaGetSymbolAddress(&p, g_direct_scratch) != cudaSuccess || p == nullptr) return KSJ_GPU_ERROR_CUDA;
+      g_direct_scratch_ptr[device] = p;
+    }
+    scratch = g_direct_scratch_ptr[device];
+  }
+  cudaStream_t cs = static_cast<cudaStream_t>(stream);
+  float2* tmp = static_cast<float2*>(scratch);
+  const int pixels = static_cast<int>(rows * cols);
+  const dim3 grid((pixels + kDirectPixels - 1) / kDirectPixels, (channels + kDirectCoils - 1) / kDirectCoils);
+  {
+    LaunchScope scope("k_direct_adjoint", cs);
+    k_direct_adjoint<<<grid, kDirectPixels, 0, cs>>>(static_cast<const float2*>(d_kspace),
+                                                     reinterpret_cast<const float2*>(d_traj), tmp,
+                                                     static_cast<int>(rows), static_cast<int>(cols), ro, co,
+                                                     static_cast<int>(channels), static_cast<int>(samples));
+  }
+  const dim3 tg((pixels + 31) / 32, (channels + 31) / 32, 1);
+  LaunchScope scope("k_images_coil_last", cs);
+  k_transpose<unsigned long long><<<tg, dim3(32, 8), 0, cs>>>(reinterpret_cast<const unsigned long long*>(tmp),
+                                                              static_cast<unsigned long long*>(d_out),
+                                                              static_cast<int>(channels), pixels);
+  return check_launch();
+}
