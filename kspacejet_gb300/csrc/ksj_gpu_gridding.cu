@@ -18,12 +18,15 @@
 //              32-column chunk of the row and its sorted list and accumulates
 //              lane-per-coil into shared memory with no atomics (a cell is
 //              only ever touched by its owning warp, in list order); the block
-//              then runs the row inverse FFT in shared memory and writes only
-//              the columns the image keeps
-//   k_cols     per (frame, column block): column inverse FFT per coil in
-//              shared memory, crop, deapodise, then write coil images or
-//              accumulate the RSS over coils in channel order
-//   k_coil_last  coil-major -> coil-last transpose for the reference layout
+//              then runs the row inverse FFT of every coil line in place and
+//              writes only the columns the image keeps, coil-last
+//              ([frame][grid row][column][channel]), so the column pass
+//              reads every coil of a column as one tile
+//   k_cols     per (frame, column block): one TMA tile of all grid rows x
+//              columns x a group of coils, column inverse FFT in place, crop,
+//              deapodise, then write coil-last images or sum |x|^2 over coils
+//              in channel order (the reference RSS order and rounding)
+//   k_images_coil_major  coil-last -> coil-major transpose when asked for
 //
 // Binning lists are (frame, grid row, 32-column chunk); a sample is listed
 // once per row its stencil covers and per chunk its W columns fall into
@@ -53,8 +56,8 @@ namespace {
 constexpr int kChunk = 32;        // grid columns per binning list
 constexpr int kMaxWidth = 8;      // largest Kaiser-Bessel width
 constexpr int kMaxGrid = 512;
-constexpr int kEmax = 8;          // complex values per thread per FFT stage
 constexpr int kMaxThreads = 512;
+constexpr int kColsThreads = 256;  // k_cols block size
 constexpr int kAhead = 4;        // coil loads in flight per warp in k_rows
 constexpr uint32_t kFlagBytes = 256;
 
@@ -77,17 +80,18 @@ struct Shape {
   int lists_per_frame;     // grid_rows * nchunks
   size_t entries_per_frame;
   int out_rows, out_cols;  // kept image region
-  int inter_pitch;         // row pitch (elements) of the row-transformed grid: out_cols rounded to 2 (16 B)
+  int col_group;           // coils per column-pass tile: a power of two >= 2, <= 32
+  int cpitch;              // channel pitch of the row-transformed grid: channels rounded up to col_group
   bool kb;
   float beta, inv_i0_beta;
   float row_origin, col_origin;
   float phase_row, phase_col, phase_sign;  // origin-phase coefficients
   int coil_group, column_block, list_capacity, frames_per_pass, rows_blocks, coil_parts;
-  FftPlan plan_rows, plan_cols;
+  DifPlan plan_rows, plan_cols;
 };
 
 struct Layout {
-  size_t flags, records, counts, cursor, offsets, entries, samples_t, inter, coil_major, tables, total;
+  size_t flags, records, counts, cursor, offsets, entries, samples_t, inter, coil_last, tables, total;
 };
 
 size_t record_bytes(int width) {
@@ -100,8 +104,8 @@ size_t record_bytes(int width) {
 }
 
 bool is_fft_size(uint32_t n) {
-  FftPlan p;
-  return n >= 2 && n <= kMaxGrid && make_fft_plan(static_cast<int>(n), &p);
+  DifPlan p;
+  return n >= 2 && n <= kMaxGrid && make_dif_plan(static_cast<int>(n), &p);
 }
 
 ksj_gpu_status make_shape(const ksj_gpu_gridding_desc* d, const ksj_gpu_gridding_tuning* t, Shape* s) {
@@ -140,7 +144,9 @@ ksj_gpu_status make_shape(const ksj_gpu_gridding_desc* d, const ksj_gpu_gridding
   s->entries_per_frame = static_cast<size_t>(s->samples) * s->width * 2;
   s->out_rows = s->rows;
   s->out_cols = s->cols;
-  s->inter_pitch = (s->cols + 1) & ~1;
+  s->col_group = 2;
+  while (s->col_group < s->channels && s->col_group < 32) s->col_group <<= 1;
+  s->cpitch = (s->channels + s->col_group - 1) / s->col_group * s->col_group;
   s->row_origin = static_cast<float>(d->row_origin);
   s->col_origin = static_cast<float>(d->col_origin);
   if (s->kb) {
@@ -172,8 +178,8 @@ ksj_gpu_status make_shape(const ksj_gpu_gridding_desc* d, const ksj_gpu_gridding
     if (static_cast<double>(s->row_origin) != d->row_origin || static_cast<double>(s->col_origin) != d->col_origin)
       return KSJ_GPU_ERROR_UNSUPPORTED;  // origins must be exact floats (the reference casts them, :320-321)
   }
-  make_fft_plan(s->grid_rows, &s->plan_rows);
-  make_fft_plan(s->grid_cols, &s->plan_cols);
+  make_dif_plan(s->grid_rows, &s->plan_rows);
+  make_dif_plan(s->grid_cols, &s->plan_cols);
 
   // tuning
   int cg = t && t->coil_group ? static_cast<int>(t->coil_group) : 0;
@@ -192,12 +198,20 @@ ksj_gpu_status make_shape(const ksj_gpu_gridding_desc* d, const ksj_gpu_gridding
     while (cg > 1 && rows_smem(cg) > 110 * 1024) cg >>= 1;
   }
   if (cg < 1 || cg > 32 || (cg & (cg - 1)) != 0 || rows_smem(cg) > smem_limit) return KSJ_GPU_ERROR_INVALID_ARGUMENT;
+  // column pass: cb columns x col_group coils per tile (a power of two
+  // number of lines, at most the block's threads), double-buffered when the
+  // channels take more than one tile
+  const int cgroups = s->cpitch / s->col_group;
+  auto cols_tile = [&](int b) {
+    return static_cast<size_t>(s->grid_rows) * b * s->col_group * sizeof(float2) * (cgroups > 1 ? 2 : 1);
+  };
   if (cb == 0) {
-    cb = 16;
-    while (cb > 4 && static_cast<long>(s->grid_rows) * cb > static_cast<long>(kEmax) * kMaxThreads) cb >>= 1;
+    cb = std::max(1, 32 / s->col_group);
+    while (cb > 1 && (cols_tile(cb) > 110 * 1024 || cb > s->out_cols)) cb >>= 1;
   }
-  if (cb < 4 || cb > 32 || (cb & (cb - 1)) != 0) return KSJ_GPU_ERROR_INVALID_ARGUMENT;
-  if (static_cast<long>(s->grid_rows) * cb > static_cast<long>(kEmax) * kMaxThreads) return KSJ_GPU_ERROR_INVALID_ARGUMENT;
+  if (cb < 1 || cb > 32 || (cb & (cb - 1)) != 0 || cb > s->out_cols || cb * s->col_group > kColsThreads ||
+      cols_tile(cb) > smem_limit)
+    return KSJ_GPU_ERROR_INVALID_ARGUMENT;
   s->coil_group = cg;
   s->column_block = cb;
   s->list_capacity = cap;
@@ -239,13 +253,14 @@ Layout make_layout(const Shape& s, const ksj_gpu_gridding_desc* d) {
   l.offsets = take((nl + s.frames) * 4);
   l.entries = take(static_cast<size_t>(s.frames) * s.entries_per_frame * 4);
   l.samples_t = take(fm * s.channels * sample_bytes(d->sample_format));
-  l.inter = take(static_cast<size_t>(s.frames) * s.channels * s.grid_rows * s.inter_pitch * sizeof(float2));
-  l.coil_major = d->output == KSJ_GPU_OUTPUT_COIL_LAST
-                     ? take(static_cast<size_t>(s.frames) * s.channels * s.out_rows * s.out_cols * sizeof(float2))
-                     : off;
-  // tables: twiddles for rows and cols, inverse deapodisation for rows and cols
+  l.inter = take(static_cast<size_t>(s.frames) * s.grid_rows * s.out_cols * s.cpitch * sizeof(float2));
+  l.coil_last = d->output == KSJ_GPU_OUTPUT_COIL_MAJOR
+                    ? take(static_cast<size_t>(s.frames) * s.channels * s.out_rows * s.out_cols * sizeof(float2))
+                    : off;
+  // tables: twiddles for rows and cols, inverse deapodisation for rows and
+  // cols, and the FFT output position of every kept row and column
   l.tables = take((static_cast<size_t>(s.grid_rows) + s.grid_cols) * sizeof(float2) +
-                  (static_cast<size_t>(s.out_rows) + s.out_cols) * sizeof(float));
+                  (static_cast<size_t>(s.out_rows) + s.out_cols) * (sizeof(float) + sizeof(int)));
   l.total = off;
   return l;
 }
@@ -256,9 +271,18 @@ Layout make_layout(const Shape& s, const ksj_gpu_gridding_desc* d) {
 // factors 1 / psi(q), q = p - n/2, psi the continuous Fourier transform of the
 // normalised Kaiser-Bessel kernel: W sinh(z)/z / I0(beta),
 // z = sqrt(beta^2 - (pi W q / g)^2) (Jackson et al. 1991).  FP64 here only.
+//
+// pos_rows[p] / pos_cols[p]: where the in-place DIF leaves the frequency
+// index that kept image row / column p takes: p itself for the linear
+// operator (no oversampling), (p - n/2) mod g for Kaiser-Bessel (the image is
+// centred on q = p - n/2).
 __global__ void k_tables(float2* tw_rows, int grid_rows, float2* tw_cols, int grid_cols, float* inv_dr, int out_rows,
-                         float* inv_dc, int out_cols, int kb, int width, double beta, double i0_beta) {
+                         float* inv_dc, int out_cols, int* pos_rows, int* pos_cols, DifPlan plan_rows,
+                         DifPlan plan_cols, int kb, int width, double beta, double i0_beta) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  auto source = [&](int p, int n, int g) { return kb ? (p - n / 2 + g) % g : p; };
+  if (i < out_rows) pos_rows[i] = dif_position(plan_rows, source(i, out_rows, grid_rows));
+  if (i < out_cols) pos_cols[i] = dif_position(plan_cols, source(i, out_cols, grid_cols));
   if (i < grid_rows) tw_rows[i] = twiddle(i, grid_rows);
   if (i < grid_cols) tw_cols[i] = twiddle(i, grid_cols);
   auto inv_psi = [&](int p, int n, int g) -> float {
@@ -509,22 +533,22 @@ struct RowsArgs {
   const uint32_t* offsets;
   const uint32_t* entries;
   const float2* tw_cols;
-  float2* inter;
+  const int* pos_cols;    // DIF output position of each kept column
+  float2* inter;          // [frame][grid_row][out_col][cpitch]
   uint32_t* flags;
   int frames, channels, samples, grid_rows, grid_cols, nchunks, lists_per_frame;
   size_t entries_per_frame;
   int coil_group, coil_parts;
-  int out_cols, inter_pitch, kb, image_cols;
-  FftPlan plan;
+  int out_cols, cpitch;
+  DifPlan plan;
 };
 
-// Accumulator layout [column][coil] with the coil index XOR-swizzled by the
-// column so that both a warp of consecutive coils at one column (gridding,
-// FFT) and a warp of consecutive columns for one coil (write-out) hit
-// distinct banks.
+// Accumulator layout [column][coil]: gridding, the row FFT and the write-out
+// all put consecutive coils on consecutive lanes at one column, so every
+// shared-memory access of the block reads or writes contiguous float2s.
 struct AccAddr {
   int cg;
-  __device__ __forceinline__ int operator()(int coil, int col) const { return col * cg + (coil ^ (col & (cg - 1))); }
+  __device__ __forceinline__ int operator()(int coil, int col) const { return col * cg + coil; }
 };
 
 // kBlocks CTAs per SM: 2 for rows of up to 384 columns (384 threads), 1
@@ -549,33 +573,12 @@ __global__ void __launch_bounds__(kThreads, kBlocks) k_rows(RowsArgs a) {
 
   // ---- gridding.  A task is (column chunk, coil part): the chunk's sorted
   // list applied to a subset of the coil group.  Cells of different coils are
-  // independent, so parts of one list run on different warps with every cell
-  // still summed in sample order; tasks are taken longest list first from a
-  // shared counter, so one long list does not leave the other warps idle.
+  // independent, so parts of one list may run on different warps with every
+  // cell still summed in sample order.  Warps take tasks round-robin.
   const int parts = a.coil_parts;
   const int cpart = cg / parts;
   const int ntasks = a.nchunks * parts;
-  __shared__ int task_order[2 * (kMaxGrid / kChunk)];
-  __shared__ int task_next;
   const uint32_t* off = a.offsets + static_cast<size_t>(f) * (a.lists_per_frame + 1);
-  if (tid == 0) {
-    int order[kMaxGrid / kChunk];
-    int len[kMaxGrid / kChunk];
-    for (int k = 0; k < a.nchunks; ++k) {
-      const int list = row * a.nchunks + k;
-      len[k] = static_cast<int>(off[list + 1] - off[list]);
-      int i = k;
-      while (i > 0 && len[order[i - 1]] < len[k]) {
-        order[i] = order[i - 1];
-        --i;
-      }
-      order[i] = k;
-    }
-    for (int i = 0; i < a.nchunks; ++i)
-      for (int p = 0; p < parts; ++p) task_order[i * parts + p] = order[i] * parts + p;
-    task_next = 0;
-  }
-  __syncthreads();
   {
     const SampleRecord<W>* recs =
         reinterpret_cast<const SampleRecord<W>*>(a.records) + static_cast<size_t>(f) * a.samples;
@@ -586,13 +589,10 @@ __global__ void __launch_bounds__(kThreads, kBlocks) k_rows(RowsArgs a) {
     const int my_group = lane / cpp;
     bool bad = false;
     const void* ks = a.samples_t;
-    for (;;) {
-      int task = 0;
-      if (lane == 0) task = atomicAdd(&task_next, 1);
-      task = __shfl_sync(0xffffffffu, task, 0);
-      if (task >= ntasks) break;
-      const int chunk = task_order[task] / parts;
-      const int part = task_order[task] - chunk * parts;
+    const int nwarps = nthreads >> 5;
+    for (int task = tid >> 5; task < ntasks; task += nwarps) {
+      const int chunk = task / parts;
+      const int part = task - chunk * parts;
       const int list = row * a.nchunks + chunk;
       const uint32_t begin = off[list];
       const int n = static_cast<int>(off[list + 1] - begin);
@@ -671,32 +671,17 @@ __global__ void __launch_bounds__(kThreads, kBlocks) k_rows(RowsArgs a) {
   }
   __syncthreads();
 
-  // ---- row inverse FFT of every coil line, in place, in batches of lines
-  {
-    int lg_batch = ilog2(max(1, min(cg, kEmax * nthreads / a.grid_cols)));
-    const int batch = 1 << lg_batch;
-    for (int l0 = 0; l0 < cg; l0 += batch) {
-      struct Shifted {
-        AccAddr base;
-        int l0;
-        __device__ __forceinline__ int operator()(int l, int i) const { return base(l + l0, i); }
-      } shifted{addr, l0};
-      fft_lines<kEmax>(acc, shifted, a.plan, lg_batch, tw, tid, nthreads);
-    }
-  }
+  // ---- row inverse FFT of every coil line, in place (output digit-reversed)
+  const int lg_cg = ilog2(cg);
+  dif_lines(acc, lg_cg, a.plan, tw, tid, nthreads);
 
-  // ---- write the kept columns: [frame][coil][grid_row][out_col]
-  const int coils_here = min(cg, a.channels - cgi * cg);
-  for (int i = tid; i < coils_here * a.out_cols; i += nthreads) {
-    const int c = i / a.out_cols;
-    const int pc = i - c * a.out_cols;
-    int src = pc;
-    if (a.kb) {
-      src = pc - a.image_cols / 2;
-      if (src < 0) src += a.grid_cols;
-    }
-    const size_t o = ((static_cast<size_t>(f) * a.channels + cgi * cg + c) * a.grid_rows + row) * a.inter_pitch + pc;
-    a.inter[o] = acc[addr(c, src)];
+  // ---- write the kept columns, coil-last: [frame][grid_row][out_col][channel]
+  const int coil = tid & (cg - 1);
+  const int gc = cgi * cg + coil;
+  if (gc < a.channels) {
+    float2* dst = a.inter + (static_cast<size_t>(f) * a.grid_rows + row) * a.out_cols * a.cpitch + gc;
+    for (int pc = tid >> lg_cg; pc < a.out_cols; pc += nthreads >> lg_cg)
+      dst[static_cast<size_t>(pc) * a.cpitch] = acc[(__ldg(a.pos_cols + pc) << lg_cg) + coil];
   }
 }
 
@@ -704,107 +689,126 @@ struct ColsArgs {
   const float2* tw_rows;
   const float* inv_dr;
   const float* inv_dc;
+  const int* pos_rows;  // DIF output position of each kept row
   void* out;
   uint32_t* flags;
   int frame0;  // first frame of this pass
-  int frames, channels, grid_rows, out_rows, out_cols, column_block, kb, image_rows;
-  int box_rows, boxes;  // TMA boxes of box_rows x column_block cover one column tile
-  uint32_t output;      // RSS or COIL_MAJOR (COIL_LAST goes through COIL_MAJOR + transpose)
-  FftPlan plan;
-};
-
-struct TileAddr {
-  int pitch;
-  __device__ __forceinline__ int operator()(int line, int index) const { return index * pitch + line; }
+  int frames, channels, grid_rows, out_rows, out_cols, kb;
+  int column_block, col_group, groups;  // tile: column_block columns x col_group coils; groups tiles per block
+  int box_rows, boxes;                  // TMA boxes of box_rows rows cover one tile
+  uint32_t output;                      // RSS or COIL_LAST (COIL_MAJOR goes through COIL_LAST + transpose)
+  DifPlan plan;
 };
 
 constexpr uint32_t kWaitLimit = 1u << 22;  // mbarrier polls before a tile wait gives up
 
 // One CTA per (frame, column block).  The row-transformed grid
-// [frame][coil][grid_row][out_col] is read one coil tile (grid_rows x
-// column_block) at a time by TMA into a double buffer: while the block
-// transforms coil c, the copy of coil c+1 is in flight.  Each tile is
-// inverse-transformed along rows in place, cropped, deapodised, and either
-// written (coil-major) or squared into the channel-order RSS accumulators.
-template <int kOutPerThread>
-__global__ void __launch_bounds__(kMaxThreads) k_cols(const __grid_constant__ CUtensorMap inter_map, ColsArgs a) {
+// [frame][grid_row][out_col][channel] is read one tile (grid_rows x
+// column_block columns x col_group coils, coils contiguous) at a time by
+// TMA; with more than one coil group the next tile's copy is in flight while
+// the block transforms the current one.  Each tile is inverse-transformed
+// along rows in place (lines = (column, coil) pairs), cropped and
+// deapodised; then either written coil-last or squared in place and summed
+// over coils in channel order per pixel.  The channel-order sum runs lane =
+// pixel with lane j reading coil t - j at step t, so the 32 lanes read 32
+// different coils (distinct banks) while each pixel still adds its coils
+// 0, 1, 2, ... in order: the result is bit-identical to the RSS of the coil
+// images.
+__global__ void __launch_bounds__(kColsThreads) k_cols(const __grid_constant__ CUtensorMap inter_map, ColsArgs a) {
   extern __shared__ __align__(16) unsigned char smem_cols[];
   unsigned char* smem_raw = smem_cols;
   const int cb = a.column_block;
+  const int cgc = a.col_group;
+  const int lines = cb * cgc;
+  const int lg_lines = ilog2(lines);
+  const int lg_cgc = ilog2(cgc);
+  const int lg_cb = ilog2(cb);
   const int col0 = blockIdx.x * cb;
-  const int f = blockIdx.y;
-  const int fg = a.frame0 + f;
+  const int fg = a.frame0 + blockIdx.y;
   const int tid = threadIdx.x;
   const int nthreads = blockDim.x;
+  const int lane = tid & 31;
+  const int warp = tid >> 5;
+  const int nbuf = a.groups > 1 ? 2 : 1;
   // each tile buffer starts on a 128-byte boundary (TMA destination)
-  const size_t tile_elems = (static_cast<size_t>(a.grid_rows) * cb + 15) & ~static_cast<size_t>(15);
+  const size_t tile_elems = (static_cast<size_t>(a.grid_rows) * lines + 15) & ~static_cast<size_t>(15);
   float2* tiles = reinterpret_cast<float2*>(smem_raw + ((128u - (smem_addr(smem_raw) & 127u)) & 127u));
-  float2* tw = tiles + 2 * tile_elems;
-  uint64_t* bars = reinterpret_cast<uint64_t*>(tw + a.grid_rows);
-  const TileAddr addr{cb};
-  const uint32_t tile_bytes = static_cast<uint32_t>(static_cast<size_t>(a.grid_rows) * cb * sizeof(float2));
+  float2* tw = tiles + nbuf * tile_elems;
+  float* rss = reinterpret_cast<float*>(tw + a.grid_rows);
+  const int npix = a.out_rows * cb;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(rss + ((npix + 1) & ~1));
+  const uint32_t tile_bytes = static_cast<uint32_t>(static_cast<size_t>(a.grid_rows) * lines * sizeof(float2));
   if (tid == 0) {
     mbar_init(&bars[0], 1);
     mbar_init(&bars[1], 1);
     mbar_init_fence();
   }
   for (int i = tid; i < a.grid_rows; i += nthreads) tw[i] = a.tw_rows[i];
+  for (int i = tid; i < npix; i += nthreads) rss[i] = 0.0f;
   __syncthreads();
-  auto issue = [&](int c, int b) {
+  auto issue = [&](int g, int b) {
     float2* dst = tiles + b * tile_elems;
     mbar_arrive_expect_tx(&bars[b], tile_bytes);
     for (int k = 0; k < a.boxes; ++k)
-      tma_load_3d(dst + static_cast<size_t>(k) * a.box_rows * cb, &inter_map, col0, k * a.box_rows,
-                  fg * a.channels + c, &bars[b]);
+      tma_load_3d(dst + static_cast<size_t>(k) * a.box_rows * lines, &inter_map, g * cgc, col0,
+                  fg * a.grid_rows + k * a.box_rows, &bars[b]);
   };
   if (tid == 0) issue(0, 0);
-  const int ncols = min(cb, a.out_cols - col0);
-  const int nout = a.out_rows * cb;
-  float rss[kOutPerThread];
-#pragma unroll
-  for (int k = 0; k < kOutPerThread; ++k) rss[k] = 0.0f;
+  const int line = tid & (lines - 1);
+  const int lcol = line >> lg_cgc;   // column within the block
+  const int lcoil = line & (cgc - 1);
+  const bool col_ok = col0 + lcol < a.out_cols;
   bool ok = true;
   int issued = 1;
-  for (int c = 0; c < a.channels; ++c) {
-    const int b = c & 1;
-    if (tid == 0 && c + 1 < a.channels) {
-      fence_proxy_async_shared();  // this buffer was last written by the FFT (generic proxy)
-      issue(c + 1, b ^ 1);
+  for (int g = 0; g < a.groups; ++g) {
+    const int b = nbuf > 1 ? (g & 1) : 0;
+    const uint32_t parity = static_cast<uint32_t>((nbuf > 1 ? (g >> 1) : g) & 1);
+    if (tid == 0 && g + 1 < a.groups) {
+      fence_proxy_async_shared();  // this buffer was last written by the generic proxy
+      issue(g + 1, b ^ 1);
       ++issued;
     }
-    const bool mine = mbar_wait_bounded(&bars[b], static_cast<uint32_t>((c >> 1) & 1), kWaitLimit);
+    const bool mine = mbar_wait_bounded(&bars[b], parity, kWaitLimit);
     if (!__syncthreads_and(mine)) {
       ok = false;
       break;
     }
     float2* tile = tiles + b * tile_elems;
-    fft_lines<kEmax>(tile, addr, a.plan, ilog2(cb), tw, tid, nthreads);
-#pragma unroll
-    for (int k = 0; k < kOutPerThread; ++k) {
-      const int i = tid + k * nthreads;
-      if (i < nout) {
-        const int pr = i / cb;
-        const int l = i - pr * cb;
-        if (l < ncols) {
-          int sr = pr;
-          if (a.kb) {
-            sr = pr - a.image_rows / 2;
-            if (sr < 0) sr += a.grid_rows;
-          }
-          float2 x = tile[sr * cb + l];
-          if (a.kb) {
-            const float sc = a.inv_dr[pr] * a.inv_dc[col0 + l];
-            x.x *= sc;
-            x.y *= sc;
-          }
-          if (a.output == KSJ_GPU_OUTPUT_RSS) {
-            // channel-order float sum of re^2 + im^2 (reductions.hpp:972-982)
-            rss[k] = __fadd_rn(rss[k], __fadd_rn(__fmul_rn(x.x, x.x), __fmul_rn(x.y, x.y)));
-          } else {
-            float2* o = static_cast<float2*>(a.out);
-            o[((static_cast<size_t>(fg) * a.channels + c) * a.out_rows + pr) * a.out_cols + col0 + l] = x;
-          }
+    dif_lines(tile, lg_lines, a.plan, tw, tid, nthreads);
+    // crop and deapodise; coil-last images are written from here, RSS
+    // inputs are squared in place
+    const int gc = g * cgc + lcoil;
+    for (int pr = tid >> lg_lines; pr < a.out_rows; pr += nthreads >> lg_lines) {
+      if (!col_ok || gc >= a.channels) continue;
+      float2* e = tile + (static_cast<size_t>(__ldg(a.pos_rows + pr)) << lg_lines) + line;
+      float2 x = *e;
+      if (a.kb) {
+        const float sc = a.inv_dr[pr] * a.inv_dc[col0 + lcol];
+        x.x *= sc;
+        x.y *= sc;
+      }
+      if (a.output == KSJ_GPU_OUTPUT_RSS) {
+        e->x = __fadd_rn(__fmul_rn(x.x, x.x), __fmul_rn(x.y, x.y));
+      } else {
+        float2* o = static_cast<float2*>(a.out);
+        o[((static_cast<size_t>(fg) * a.out_rows + pr) * a.out_cols + col0 + lcol) * a.channels + gc] = x;
+      }
+    }
+    if (a.output == KSJ_GPU_OUTPUT_RSS) {
+      __syncthreads();
+      // channel-order sum per pixel (reductions.hpp:972-982)
+      const int live_coils = min(cgc, a.channels - g * cgc);
+      for (int q0 = warp * 32; q0 < npix; q0 += nthreads) {
+        const int q = q0 + lane;
+        const bool live = q < npix && col0 + (q & (cb - 1)) < a.out_cols;
+        const int pr = q >> lg_cb;
+        const int base = live ? (__ldg(a.pos_rows + pr) << lg_lines) + ((q & (cb - 1)) << lg_cgc) : 0;
+        float total = live ? rss[q] : 0.0f;
+        for (int t = 0; t < live_coils + 31; ++t) {
+          const int c = t - lane;
+          if (live && c >= 0 && c < live_coils) total = __fadd_rn(total, tile[base + c].x);
         }
+        if (live) rss[q] = total;
       }
     }
     __syncthreads();
@@ -814,20 +818,20 @@ __global__ void __launch_bounds__(kMaxThreads) k_cols(const __grid_constant__ CU
     // a bounded chance to land before the block's shared memory is released
     if (tid == 0) {
       atomicOr(a.flags, KSJ_GPU_FLAG_WAIT_TIMEOUT);
-      for (int u = 0; u < issued; ++u) mbar_wait_bounded(&bars[u & 1], static_cast<uint32_t>((u >> 1) & 1), kWaitLimit);
+      for (int u = 0; u < issued; ++u) {
+        const int bb = nbuf > 1 ? (u & 1) : 0;
+        const uint32_t par = static_cast<uint32_t>((nbuf > 1 ? (u >> 1) : u) & 1);
+        mbar_wait_bounded(&bars[bb], par, kWaitLimit);
+      }
     }
     return;
   }
   if (a.output == KSJ_GPU_OUTPUT_RSS) {
     float* o = static_cast<float*>(a.out);
-#pragma unroll
-    for (int k = 0; k < kOutPerThread; ++k) {
-      const int i = tid + k * nthreads;
-      if (i < nout) {
-        const int pr = i / cb;
-        const int l = i - pr * cb;
-        if (l < ncols) o[(static_cast<size_t>(fg) * a.out_rows + pr) * a.out_cols + col0 + l] = __fsqrt_rn(rss[k]);
-      }
+    for (int q = tid; q < npix; q += nthreads) {
+      const int pr = q >> lg_cb;
+      const int l = q & (cb - 1);
+      if (col0 + l < a.out_cols) o[(static_cast<size_t>(fg) * a.out_rows + pr) * a.out_cols + col0 + l] = __fsqrt_rn(rss[q]);
     }
   }
 }
@@ -839,8 +843,12 @@ size_t rows_smem_bytes(const Shape& s) {
 }
 
 size_t cols_smem_bytes(const Shape& s) {
-  const size_t tile = (static_cast<size_t>(s.grid_rows) * s.column_block + 15) & ~static_cast<size_t>(15);
-  return 128 + 2 * tile * sizeof(float2) + s.grid_rows * sizeof(float2) + 2 * sizeof(uint64_t);
+  const size_t lines = static_cast<size_t>(s.column_block) * s.col_group;
+  const size_t tile = (static_cast<size_t>(s.grid_rows) * lines + 15) & ~static_cast<size_t>(15);
+  const int nbuf = s.cpitch / s.col_group > 1 ? 2 : 1;
+  const size_t npix = static_cast<size_t>(s.out_rows) * s.column_block;
+  return 128 + nbuf * tile * sizeof(float2) + s.grid_rows * sizeof(float2) + ((npix + 1) & ~size_t{1}) * sizeof(float) +
+         2 * sizeof(uint64_t);
 }
 
 using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
@@ -859,8 +867,8 @@ EncodeTiledFn encode_tiled() {
   return fn;
 }
 
-// Tensor map over the row-transformed grid [frame*coil][grid_row][out_col]
-// of 8-byte elements, box (column_block, box_rows, 1).
+// Tensor map over the row-transformed grid [frame*grid_row][out_col][cpitch]
+// of 8-byte elements, box (col_group coils, column_block columns, box_rows rows).
 bool make_inter_map(const Shape& s, void* inter, CUtensorMap* map, int* box_rows, int* boxes) {
   EncodeTiledFn enc = encode_tiled();
   if (enc == nullptr) return false;
@@ -868,22 +876,16 @@ bool make_inter_map(const Shape& s, void* inter, CUtensorMap* map, int* box_rows
   while (s.grid_rows / nb > 256 || s.grid_rows % nb != 0) ++nb;
   *boxes = nb;
   *box_rows = s.grid_rows / nb;
-  const cuuint64_t dims[3] = {static_cast<cuuint64_t>(s.out_cols), static_cast<cuuint64_t>(s.grid_rows),
-                              static_cast<cuuint64_t>(s.frames) * s.channels};
-  const cuuint64_t strides[2] = {static_cast<cuuint64_t>(s.inter_pitch) * 8,
-                                 static_cast<cuuint64_t>(s.inter_pitch) * s.grid_rows * 8};
-  const cuuint32_t box[3] = {static_cast<cuuint32_t>(s.column_block), static_cast<cuuint32_t>(*box_rows), 1};
+  const cuuint64_t dims[3] = {static_cast<cuuint64_t>(s.cpitch), static_cast<cuuint64_t>(s.out_cols),
+                              static_cast<cuuint64_t>(s.frames) * s.grid_rows};
+  const cuuint64_t strides[2] = {static_cast<cuuint64_t>(s.cpitch) * 8,
+                                 static_cast<cuuint64_t>(s.cpitch) * s.out_cols * 8};
+  const cuuint32_t box[3] = {static_cast<cuuint32_t>(s.col_group), static_cast<cuuint32_t>(s.column_block),
+                             static_cast<cuuint32_t>(*box_rows)};
   const cuuint32_t estr[3] = {1, 1, 1};
   return enc(map, CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, inter, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
              CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
-}
-
-int cols_threads(const Shape& s) {
-  const int elems = s.grid_rows * s.column_block;
-  int t = (elems + kEmax - 1) / kEmax;
-  t = (t + 31) / 32 * 32;
-  return std::max(64, std::min(kMaxThreads, t));
 }
 
 template <int W, uint32_t kFormat>
@@ -901,6 +903,8 @@ ksj_gpu_status launch_all(const Shape& s, const Layout& l, const ksj_gpu_griddin
   float2* tw_cols = tw_rows + s.grid_rows;
   float* inv_dr = reinterpret_cast<float*>(tw_cols + s.grid_cols);
   float* inv_dc = inv_dr + s.out_rows;
+  int* pos_rows = reinterpret_cast<int*>(inv_dc + s.out_cols);
+  int* pos_cols = pos_rows + s.out_rows;
   const size_t nl = static_cast<size_t>(s.frames) * s.lists_per_frame;
 
   if (cudaMemsetAsync(flags, 0, kFlagBytes, stream) != cudaSuccess) return KSJ_GPU_ERROR_CUDA;
@@ -912,7 +916,8 @@ ksj_gpu_status launch_all(const Shape& s, const Layout& l, const ksj_gpu_griddin
     const double beta = s.beta;
     LaunchScope scope("k_tables", stream);
     k_tables<<<(n + 255) / 256, 256, 0, stream>>>(tw_rows, s.grid_rows, tw_cols, s.grid_cols, inv_dr, s.out_rows,
-                                                  inv_dc, s.out_cols, s.kb ? 1 : 0, s.width, beta,
+                                                  inv_dc, s.out_cols, pos_rows, pos_cols, s.plan_rows, s.plan_cols,
+                                                  s.kb ? 1 : 0, s.width, beta,
                                                   s.kb ? std::cyl_bessel_i(0.0, beta) : 1.0);
   }
   const size_t fm = static_cast<size_t>(s.frames) * s.samples;
@@ -979,6 +984,7 @@ ksj_gpu_status launch_all(const Shape& s, const Layout& l, const ksj_gpu_griddin
   r.offsets = offsets;
   r.entries = entries;
   r.tw_cols = tw_cols;
+  r.pos_cols = pos_cols;
   r.inter = inter;
   r.flags = flags;
   r.frames = s.frames;
@@ -992,9 +998,7 @@ ksj_gpu_status launch_all(const Shape& s, const Layout& l, const ksj_gpu_griddin
   r.coil_group = s.coil_group;
   r.coil_parts = s.coil_parts;
   r.out_cols = s.out_cols;
-  r.inter_pitch = s.inter_pitch;
-  r.kb = s.kb ? 1 : 0;
-  r.image_cols = s.cols;
+  r.cpitch = s.cpitch;
   r.plan = s.plan_cols;
   const size_t rows_smem = rows_smem_bytes(s);
   const int rows_threads = std::max(64, s.nchunks * 32);
@@ -1009,32 +1013,27 @@ ksj_gpu_status launch_all(const Shape& s, const Layout& l, const ksj_gpu_griddin
   c.tw_rows = tw_rows;
   c.inv_dr = inv_dr;
   c.inv_dc = inv_dc;
+  c.pos_rows = pos_rows;
   c.flags = flags;
   c.frames = s.frames;
   c.channels = s.channels;
   c.grid_rows = s.grid_rows;
   c.out_rows = s.out_rows;
   c.out_cols = s.out_cols;
-  c.column_block = s.column_block;
   c.kb = s.kb ? 1 : 0;
-  c.image_rows = s.rows;
+  c.column_block = s.column_block;
+  c.col_group = s.col_group;
+  c.groups = s.cpitch / s.col_group;
   c.plan = s.plan_rows;
-  const bool coil_last = d->output == KSJ_GPU_OUTPUT_COIL_LAST;
-  c.output = d->output == KSJ_GPU_OUTPUT_RSS ? KSJ_GPU_OUTPUT_RSS : KSJ_GPU_OUTPUT_COIL_MAJOR;
-  c.out = coil_last ? static_cast<void*>(ws + l.coil_major) : d_out;
+  const bool coil_major = d->output == KSJ_GPU_OUTPUT_COIL_MAJOR;
+  c.output = d->output == KSJ_GPU_OUTPUT_RSS ? KSJ_GPU_OUTPUT_RSS : KSJ_GPU_OUTPUT_COIL_LAST;
+  c.out = coil_major ? static_cast<void*>(ws + l.coil_last) : d_out;
   CUtensorMap map;
   if (!make_inter_map(s, inter, &map, &c.box_rows, &c.boxes)) return KSJ_GPU_ERROR_CUDA;
-  const int cols_thr = cols_threads(s);
-  const int per = (s.out_rows * s.column_block + cols_thr - 1) / cols_thr;
   const size_t cols_smem = cols_smem_bytes(s);
-  void (*cols_kernel)(const __grid_constant__ CUtensorMap, ColsArgs) = nullptr;
-  if (per <= 4) cols_kernel = k_cols<4>;
-  else if (per <= 8) cols_kernel = k_cols<8>;
-  else if (per <= 16) cols_kernel = k_cols<16>;
-  else return KSJ_GPU_ERROR_UNSUPPORTED;
-  if (cudaFuncSetAttribute(cols_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(cols_smem)) !=
+  if (cudaFuncSetAttribute(k_cols, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(cols_smem)) !=
           cudaSuccess ||
-      cudaFuncSetAttribute(cols_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100) != cudaSuccess)
+      cudaFuncSetAttribute(k_cols, cudaFuncAttributePreferredSharedMemoryCarveout, 100) != cudaSuccess)
     return KSJ_GPU_ERROR_CUDA;
 
   // frames in passes sized so one pass's row-transformed grid stays in L2
@@ -1050,16 +1049,17 @@ ksj_gpu_status launch_all(const Shape& s, const Layout& l, const ksj_gpu_griddin
     {
       LaunchScope scope("k_cols", stream);
       const dim3 grid((s.out_cols + s.column_block - 1) / s.column_block, nf);
-      cols_kernel<<<grid, cols_thr, cols_smem, stream>>>(map, c);
+      k_cols<<<grid, kColsThreads, cols_smem, stream>>>(map, c);
     }
   }
-  if (coil_last) {
+  if (coil_major) {
+    // [frame][pixel][channel] -> [frame][channel][pixel]
     const int pixels = s.out_rows * s.out_cols;
-    const dim3 tg((pixels + 31) / 32, (s.channels + 31) / 32, s.frames);
-    LaunchScope scope("k_images_coil_last", stream);
+    const dim3 tg((s.channels + 31) / 32, (pixels + 31) / 32, s.frames);
+    LaunchScope scope("k_images_coil_major", stream);
     k_transpose<unsigned long long><<<tg, dim3(32, 8), 0, stream>>>(
-        reinterpret_cast<const unsigned long long*>(ws + l.coil_major), static_cast<unsigned long long*>(d_out),
-        s.channels, pixels);
+        reinterpret_cast<const unsigned long long*>(ws + l.coil_last), static_cast<unsigned long long*>(d_out),
+        pixels, s.channels);
   }
   return check_launch();
 }
@@ -1190,7 +1190,7 @@ extern "C" ksj_gpu_status ksj_gpu_gridding_tune(const ksj_gpu_gridding_desc* des
   for (uint32_t cg : {32u, 16u, 8u, 4u, 2u, 1u}) {
     if (cg > 1 && cg / 2 >= desc->channels) continue;
     if (cg * 4 < desc->channels && cg < 8) continue;
-    for (uint32_t cb : {4u, 8u, 16u})
+    for (uint32_t cbm : {1u, 2u})
     for (uint32_t fpp : {0u, 12u})
     for (uint32_t rb : {1u, 2u})
     for (uint32_t parts : {1u, 2u}) {
@@ -1198,8 +1198,10 @@ extern "C" ksj_gpu_status ksj_gpu_gridding_tune(const ksj_gpu_gridding_desc* des
       if (parts > 1 && cg < 16) continue;
       ksj_gpu_gridding_tuning t{};
       t.struct_size = sizeof(t);
+      uint32_t gcols = 2;
+      while (gcols < desc->channels && gcols < 32) gcols <<= 1;
       t.coil_group = cg;
-      t.column_block = cb;
+      t.column_block = cbm * std::max(1u, 32u / gcols);
       t.frames_per_pass = fpp;
       t.rows_blocks_per_sm = rb;
       t.coil_parts = parts;

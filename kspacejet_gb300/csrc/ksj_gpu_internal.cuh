@@ -217,14 +217,46 @@ __device__ __forceinline__ void dft_inverse<8>(float2* v) {
   }
 }
 
-// A radix plan for n = 2^a 3^b (b <= 1): radices in execution order.
-struct FftPlan {
+template <>
+__device__ __forceinline__ void dft_inverse<6>(float2* v) {
+  // 2-point DFTs of (x_j, x_{j+3}); the sums give the even outputs through a
+  // 3-point DFT, the differences times exp(i pi j / 3) the odd ones
+  constexpr float kS3 = 0.8660254037844386f;  // sin(pi / 3)
+  float2 e[3], o[3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    e[j] = cadd(v[j], v[j + 3]);
+    o[j] = csub(v[j], v[j + 3]);
+  }
+  o[1] = make_float2(0.5f * o[1].x - kS3 * o[1].y, kS3 * o[1].x + 0.5f * o[1].y);
+  o[2] = make_float2(-0.5f * o[2].x - kS3 * o[2].y, kS3 * o[2].x - 0.5f * o[2].y);
+  dft_inverse<3>(e);
+  dft_inverse<3>(o);
+  v[0] = e[0];
+  v[1] = o[0];
+  v[2] = e[1];
+  v[3] = o[1];
+  v[4] = e[2];
+  v[5] = o[2];
+}
+
+// In-place mixed-radix decimation-in-frequency plan for n = 2^a 3^b (b <= 1):
+// a factor 3 first (as radix 6 when n is even), then radix-8 stages, then a
+// final 4 or 2, so every block length after the first stage is a power of
+// two.  Stage s splits blocks of length m[s] * radix[s] into radix[s]
+// sub-blocks of length m[s] = 2^lg_m[s]; its twiddles are
+// exp(2 pi i (i * d * tw_stride[s]) / n).  The output X[k] ends at
+// dif_position(k) (digit reversal).
+struct DifPlan {
   int n;
   int stages;
   int radix[12];
+  int lg_m[12];
+  int nbf[12];        // butterflies per line: n / radix
+  int tw_stride[12];  // n / block length
 };
 
-inline bool make_fft_plan(int n, FftPlan* plan) {
+inline bool make_dif_plan(int n, DifPlan* p) {
   if (n < 2 || n > 4096) return false;
   int m = n, threes = 0;
   while (m % 3 == 0) {
@@ -232,86 +264,109 @@ inline bool make_fft_plan(int n, FftPlan* plan) {
     ++threes;
   }
   if (threes > 1 || (m & (m - 1)) != 0) return false;
-  plan->n = n;
-  plan->stages = 0;
+  int rad[12];
+  int ns = 0;
+  if (threes) {
+    if (m >= 2) {
+      rad[ns++] = 6;
+      m /= 2;
+    } else {
+      rad[ns++] = 3;
+    }
+  }
   while (m >= 8) {
-    plan->radix[plan->stages++] = 8;
+    rad[ns++] = 8;
     m /= 8;
   }
-  if (m == 4) plan->radix[plan->stages++] = 4;
-  if (m == 2) plan->radix[plan->stages++] = 2;
-  if (threes) plan->radix[plan->stages++] = 3;
+  if (m == 4) rad[ns++] = 4;
+  if (m == 2) rad[ns++] = 2;
+  p->n = n;
+  p->stages = ns;
+  int len = n;
+  for (int s = 0; s < ns; ++s) {
+    const int sub = len / rad[s];
+    int lg = 0;
+    while ((1 << lg) < sub) ++lg;
+    p->radix[s] = rad[s];
+    p->lg_m[s] = lg;
+    p->nbf[s] = n / rad[s];
+    p->tw_stride[s] = n / len;
+    len = sub;
+  }
   return true;
 }
 
-// One Stockham stage over `nlines` = 2^lg_lines lines of length n held in
-// shared memory; element (line, index) lives at smem[addr(line, index)].
-// Threads map line-fastest so that a warp touches consecutive lines of one
-// index (the layouts below put those in distinct banks).  Every thread first
-// loads all of its butterflies' inputs, the block synchronises, then all
-// outputs are stored: the stage is in place with one buffer.  The plan puts
-// the radix-3 stage last, so the span ns = 2^lg_ns is always a power of two.
-// Requires n * nlines <= kEmax * nthreads.
-template <int R, int kEmax, class Addr>
-__device__ __forceinline__ void fft_stage(float2* smem, const Addr& addr, int n, int lg_lines, int lg_ns,
-                                          const float2* __restrict__ tw, int tid, int nthreads) {
-  constexpr int K = (kEmax + R - 1) / R;
-  const int nbf = n / R;
-  const int total = nbf << lg_lines;
-  const int lmask = (1 << lg_lines) - 1;
-  float2 v[K][R];
-#pragma unroll
-  for (int k = 0; k < K; ++k) {
-    const int t = tid + k * nthreads;
-    if (t < total) {
-      const int l = t & lmask;
-      const int j = t >> lg_lines;
-#pragma unroll
-      for (int r = 0; r < R; ++r) v[k][r] = smem[addr(l, j + r * nbf)];
-    }
+// Position of output X[k] after all stages of `p`.
+__host__ __device__ inline int dif_position(const DifPlan& p, int k) {
+  int pos = 0, len = p.n;
+  for (int s = 0; s < p.stages; ++s) {
+    const int r = p.radix[s];
+    len /= r;
+    pos += (k % r) * len;
+    k /= r;
   }
-  __syncthreads();
-  const int ns = 1 << lg_ns;
-  const int step = nbf >> lg_ns;  // n / (ns * R)
-#pragma unroll
-  for (int k = 0; k < K; ++k) {
-    const int t = tid + k * nthreads;
-    if (t < total) {
-      const int l = t & lmask;
-      const int j = t >> lg_lines;
-      const int kk = j & (ns - 1);
-      if (lg_ns > 0) {
-#pragma unroll
-        for (int r = 1; r < R; ++r) v[k][r] = cmul(v[k][r], tw[r * kk * step]);
-      }
-      dft_inverse<R>(v[k]);
-      const int dst = ((j >> lg_ns) << lg_ns) * R + kk;
-#pragma unroll
-      for (int r = 0; r < R; ++r) smem[addr(l, dst + r * ns)] = v[k][r];
-    }
-  }
-  __syncthreads();
+  return pos;
 }
 
-// Unnormalised inverse FFT of 2^lg_lines lines (tw[t] = exp(2 pi i t / n)).
-template <int kEmax, class Addr>
-__device__ __forceinline__ void fft_lines(float2* smem, const Addr& addr, const FftPlan& plan, int lg_lines,
+// One DIF stage over 2^lg_lines lines held line-contiguous in shared memory:
+// element (line, index) at smem[(index << lg_lines) + line].  A thread keeps
+// one line (tid mod lines) and walks that line's butterflies, two at a time
+// so that both sets of loads are in flight together; a butterfly reads and
+// writes the same radix elements, so no thread needs another's result
+// within the stage.
+template <int R>
+__device__ __forceinline__ void dif_stage(float2* smem, int lg_lines, int nbf, int lg_m, int tws,
                                           const float2* __restrict__ tw, int tid, int nthreads) {
-  int lg_ns = 0;
-  for (int s = 0; s < plan.stages; ++s) {
-    const int r = plan.radix[s];
-    if (r == 8) {
-      fft_stage<8, kEmax>(smem, addr, plan.n, lg_lines, lg_ns, tw, tid, nthreads);
-      lg_ns += 3;
-    } else if (r == 4) {
-      fft_stage<4, kEmax>(smem, addr, plan.n, lg_lines, lg_ns, tw, tid, nthreads);
-      lg_ns += 2;
-    } else if (r == 2) {
-      fft_stage<2, kEmax>(smem, addr, plan.n, lg_lines, lg_ns, tw, tid, nthreads);
-      lg_ns += 1;
-    } else {
-      fft_stage<3, kEmax>(smem, addr, plan.n, lg_lines, lg_ns, tw, tid, nthreads);
+  const int line = tid & ((1 << lg_lines) - 1);
+  const int step = nthreads >> lg_lines;
+  const int mmask = (1 << lg_m) - 1;
+  auto base_of = [&](int u) { return (((u >> lg_m) * R) << lg_m) + (u & mmask); };
+  auto finish = [&](float2* v, int u, int base) {
+    dft_inverse<R>(v);
+    const int i = u & mmask;
+    if (i != 0) {
+#pragma unroll
+      for (int d = 1; d < R; ++d) v[d] = cmul(v[d], tw[i * d * tws]);
     }
+#pragma unroll
+    for (int d = 0; d < R; ++d) smem[((base + (d << lg_m)) << lg_lines) + line] = v[d];
+  };
+  int u = tid >> lg_lines;
+  for (; u + step < nbf; u += 2 * step) {
+    const int ba = base_of(u), bb = base_of(u + step);
+    float2 va[R], vb[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      va[r] = smem[((ba + (r << lg_m)) << lg_lines) + line];
+      vb[r] = smem[((bb + (r << lg_m)) << lg_lines) + line];
+    }
+    finish(va, u, ba);
+    finish(vb, u + step, bb);
+  }
+  if (u < nbf) {
+    const int ba = base_of(u);
+    float2 va[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) va[r] = smem[((ba + (r << lg_m)) << lg_lines) + line];
+    finish(va, u, ba);
+  }
+}
+
+// Unnormalised inverse FFT (exp(+2 pi i n k / N)) of every line, in place,
+// output digit-reversed; tw[t] = exp(2 pi i t / n).  Requires nthreads to be
+// a multiple of the line count.  Synchronises the block after each stage.
+__device__ __forceinline__ void dif_lines(float2* smem, int lg_lines, const DifPlan& p,
+                                          const float2* __restrict__ tw, int tid, int nthreads) {
+  for (int s = 0; s < p.stages; ++s) {
+    const int nbf = p.nbf[s], lg_m = p.lg_m[s], tws = p.tw_stride[s];
+    switch (p.radix[s]) {
+      case 8: dif_stage<8>(smem, lg_lines, nbf, lg_m, tws, tw, tid, nthreads); break;
+      case 6: dif_stage<6>(smem, lg_lines, nbf, lg_m, tws, tw, tid, nthreads); break;
+      case 4: dif_stage<4>(smem, lg_lines, nbf, lg_m, tws, tw, tid, nthreads); break;
+      case 3: dif_stage<3>(smem, lg_lines, nbf, lg_m, tws, tw, tid, nthreads); break;
+      default: dif_stage<2>(smem, lg_lines, nbf, lg_m, tws, tw, tid, nthreads); break;
+    }
+    __syncthreads();
   }
 }
 

@@ -191,6 +191,56 @@ def test_rss_epilogue_equals_rss_of_coil_images(native, cuda, orc):
     assert orc.rss(outs[gpu.OUTPUT_COIL_LAST]).tobytes() == outs[gpu.OUTPUT_RSS].tobytes()
 
 
+@pytest.mark.parametrize("channels", [1, 3, 40])
+def test_tunings_are_byte_identical(native, cuda, orc, channels):
+    """Every coil grouping, column block, coil split, occupancy and frame
+    pass gives the same bytes: each cell sums in sample order and each line's
+    FFT does not depend on which block runs it.  40 channels take two coil
+    tiles in the column pass (double-buffered); the RSS still adds them in
+    channel order.  The default tuning is also checked against FP64."""
+    import ctypes
+
+    import torch
+    from kspacejet_gb300 import gpu
+
+    tr, ks = _kb_case(orc, 32, 64, 4, channels=channels, spokes=24, seed=5)
+    frames = 2
+    k = torch.from_numpy(np.stack([ks, ks[:, ::-1].copy()])).to(cuda)
+    t = torch.from_numpy(np.stack([tr, tr[::-1].copy()])).to(cuda)
+    outs = {}
+    for mode in (gpu.OUTPUT_RSS, gpu.OUTPUT_COIL_LAST, gpu.OUTPUT_COIL_MAJOR):
+        g = gpu.kb_gridding(image=32, grid=64, channels=channels, samples=tr.shape[0], frames=frames, output=mode)
+        ws = g.new_workspace(cuda)
+        base = g.new_output(cuda)
+        g.run(k, t, base, ws)
+        want = base.cpu().numpy()
+        outs[mode] = want
+        gcols = 2
+        while gcols < channels and gcols < 32:
+            gcols *= 2
+        for cg in (1, 2, 8, 32):
+            for cb in (max(1, 32 // gcols), 2 * max(1, 32 // gcols)):
+                for parts, rb, fpp in ((1, 1, 0), (2, 2, 1), (1, 2, 1)):
+                    if parts > cg:
+                        continue
+                    tun = gpu.GriddingTuning(ctypes.sizeof(gpu.GriddingTuning), cg, cb, 0, fpp, rb, parts)
+                    try:
+                        need = g.workspace_bytes()
+                        o = g.new_output(cuda)
+                        o.fill_(float("nan")) if o.dtype == torch.float32 else o.real.fill_(float("nan"))
+                        g.run(k, t, o, ws, tuning=tun)
+                    except gpu.GpuError:
+                        continue  # a combination this shape cannot take (shared memory)
+                    got = o.cpu().numpy()
+                    assert got.tobytes() == want.tobytes(), (mode, cg, cb, parts, rb, fpp, need)
+    assert orc.rss(outs[gpu.OUTPUT_COIL_LAST][0]).tobytes() == outs[gpu.OUTPUT_RSS][0].tobytes()
+    np.testing.assert_array_equal(outs[gpu.OUTPUT_COIL_MAJOR], np.moveaxis(outs[gpu.OUTPUT_COIL_LAST], -1, 1))
+    d64 = np.hypot(tr[:, 0].astype(np.float64), tr[:, 1].astype(np.float64))
+    for c in range(min(channels, 3)):
+        ref = orc.kb_gridding(64, 32, ks[c].astype(np.complex128), tr.astype(np.float64), d64, width=4)
+        assert oracle.rel_l2(outs[gpu.OUTPUT_COIL_MAJOR][0, c], ref) <= TOL_FP64
+
+
 def test_bf16_sample_storage_bound(native, cuda, orc):
     """BF16 sample storage, FP32 arithmetic: stated bound 1e-2 rel L2 against
     the FP32-storage result (bfloat16 keeps 8 mantissa bits: ~2e-3 per value)."""
