@@ -45,6 +45,7 @@
 #include <mutex>
 #include <map>
 #include <tuple>
+#include <type_traits>
 #include <vector>
 
 #include "ksj_gpu.h"
@@ -53,12 +54,12 @@
 namespace ksj_gpu {
 namespace {
 
-constexpr int kChunk = 32;        // grid columns per binning list
+constexpr int kChunk = 16;        // grid columns per binning list (<= 32 lists per row)
 constexpr int kMaxWidth = 8;      // largest Kaiser-Bessel width
 constexpr int kMaxGrid = 512;
 constexpr int kMaxThreads = 512;
 constexpr int kColsThreads = 256;  // k_cols block size
-constexpr int kAhead = 4;        // coil loads in flight per warp in k_rows
+constexpr int kAhead = 8;         // coil loads in flight per warp in k_rows
 constexpr uint32_t kFlagBytes = 256;
 
 // Per (frame, sample) record written by k_prepare, read by k_rows.
@@ -70,6 +71,21 @@ struct alignas(16) SampleRecord {
   float wr[W];
   float wc[W];
 };
+
+// k_rows stages, per warp, the list entries of its current batch in shared
+// memory: {c0, sample, scale} and the W column weights times the row weight,
+// in 16-byte vectors read back as warp-wide broadcasts.
+__host__ __device__ constexpr int meta_vecs(int w) { return 1 + (w + 3) / 4; }
+__host__ __device__ constexpr int meta_batch(int w) { return w <= 4 ? 32 : 16; }
+
+// Shared memory of one k_rows block: accumulators, twiddles, the list
+// offsets of the row and the per-warp entry batches.
+inline size_t rows_smem_for(int grid_cols, int cg, int width, int threads) {
+  const int nchunks = (grid_cols + kChunk - 1) / kChunk;
+  const size_t head = static_cast<size_t>(grid_cols) * (cg + 1) * 8 + static_cast<size_t>(nchunks + 1) * 4;
+  return ((head + 15) & ~size_t{15}) + static_cast<size_t>(threads / 32) * meta_batch(width) * meta_vecs(width) * 16;
+}
+inline int rows_threads_for(int grid_cols) { return std::max(64, (grid_cols + 31) / 32 * 32); }
 
 struct Shape {
   int frames, channels, samples;
@@ -91,7 +107,7 @@ struct Shape {
 };
 
 struct Layout {
-  size_t flags, records, counts, cursor, offsets, entries, samples_t, inter, coil_last, tables, total;
+  size_t flags, records, counts, cursor, offsets, entries, expanded, samples_t, inter, coil_last, tables, total;
 };
 
 size_t record_bytes(int width) {
@@ -189,13 +205,14 @@ ksj_gpu_status make_shape(const ksj_gpu_gridding_desc* d, const ksj_gpu_gridding
   if (cap < 64 || cap > 2048 || (cap & (cap - 1)) != 0) return KSJ_GPU_ERROR_INVALID_ARGUMENT;
   const size_t smem_limit = 200 * 1024;
   auto rows_smem = [&](int g) {
-    return static_cast<size_t>(s->grid_cols) * g * sizeof(float2) + static_cast<size_t>(s->grid_cols) * sizeof(float2);
+    return rows_smem_for(s->grid_cols, g, s->width, rows_threads_for(s->grid_cols));
   };
   if (cg == 0) {
     int want = 1;
     while (want < s->channels && want < 32) want <<= 1;
     cg = want;
-    while (cg > 1 && rows_smem(cg) > 110 * 1024) cg >>= 1;
+    // two row blocks per SM when they fit: (228 KiB - 2 x 1 KiB reserved) / 2
+    while (cg > 1 && rows_smem(cg) > 115712) cg >>= 1;
   }
   if (cg < 1 || cg > 32 || (cg & (cg - 1)) != 0 || rows_smem(cg) > smem_limit) return KSJ_GPU_ERROR_INVALID_ARGUMENT;
   // column pass: cb columns x col_group coils per tile (a power of two
@@ -252,6 +269,7 @@ Layout make_layout(const Shape& s, const ksj_gpu_gridding_desc* d) {
   l.cursor = take(nl * 4);
   l.offsets = take((nl + s.frames) * 4);
   l.entries = take(static_cast<size_t>(s.frames) * s.entries_per_frame * 4);
+  l.expanded = take(static_cast<size_t>(s.frames) * s.entries_per_frame * meta_vecs(s.width) * 16);
   l.samples_t = take(fm * s.channels * sample_bytes(d->sample_format));
   l.inter = take(static_cast<size_t>(s.frames) * s.grid_rows * s.out_cols * s.cpitch * sizeof(float2));
   l.coil_last = d->output == KSJ_GPU_OUTPUT_COIL_MAJOR
@@ -502,36 +520,152 @@ __device__ __forceinline__ void warp_sort(uint32_t* buf, int n, int lane) {
 
 // One warp per list: sort its sample indices ascending, in shared memory
 // when the list fits the per-warp buffer, in place in global memory otherwise.
-__global__ void __launch_bounds__(256) k_sort(const uint32_t* offsets, uint32_t* entries, int frames,
-                                              int lists_per_frame, size_t entries_per_frame, int capacity) {
+// One list entry as k_rows consumes it (meta_vecs(W) 16-byte vectors):
+//   v0 = {tap word, sample index, scale.re, scale.im}, v1.. = the W column
+//   weights times this row's weight (zero padded).
+// The tap word holds the mask of taps that land in the list's column chunk
+// (bits 0-7) and the column of tap 0 as seen from the chunk (bits 9 up, one
+// row-length lower when the taps reaching the chunk wrapped past the last
+// column); bit 8 marks a one-chunk row that sees both ends of a wrap, whose
+// taps are wrapped one by one.
+template <int W>
+__device__ __forceinline__ void expand_entry(const SampleRecord<W>* recs, uint32_t sidx, int row, int col_lo,
+                                             int col_hi, int grid_rows, int grid_cols, float4* out) {
+  constexpr int kRV = static_cast<int>(sizeof(SampleRecord<W>) / 16);
+  constexpr int kMV = meta_vecs(W);
+  float4 q[kRV];
+  const float4* rp = reinterpret_cast<const float4*>(recs + sidx);
+#pragma unroll
+  for (int v = 0; v < kRV; ++v) q[v] = __ldg(rp + v);
+  const float* w = reinterpret_cast<const float*>(q);
+  int ta = row - __float_as_int(w[0]);
+  if (ta < 0) ta += grid_rows;
+  float wr = 0.0f;
+#pragma unroll
+  for (int j = 0; j < W; ++j)
+    if (j == ta) wr = w[4 + j];
+  const int c0 = __float_as_int(w[1]);
+  const int cb0 = c0 >= col_hi ? c0 - grid_cols : c0;
+  uint32_t in_chunk = 0, straight = 0;
+#pragma unroll
+  for (int j = 0; j < W; ++j) {
+    int col = c0 + j;
+    if (col >= grid_cols) col -= grid_cols;
+    if (col >= col_lo && col < col_hi) in_chunk |= 1u << j;
+    if (cb0 + j >= col_lo && cb0 + j < col_hi) straight |= 1u << j;
+  }
+  const int word0 = in_chunk == straight ? ((cb0 * 512) | static_cast<int>(in_chunk))
+                                         : ((c0 * 512) | 256 | static_cast<int>(in_chunk));
+  out[0] = make_float4(__int_as_float(word0), __uint_as_float(sidx), w[2], w[3]);
+#pragma unroll
+  for (int v = 1; v < kMV; ++v) {
+    float t4[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int j = 4 * (v - 1) + u;
+      t4[u] = j < W ? wr * w[4 + W + j] : 0.0f;
+    }
+    out[v] = make_float4(t4[0], t4[1], t4[2], t4[3]);
+  }
+}
+
+struct SortArgs {
+  const uint32_t* offsets;
+  uint32_t* entries;
+  const unsigned char* records;
+  float4* expanded;
+  int frames, samples, lists_per_frame, nchunks, grid_rows, grid_cols, capacity;
+  size_t entries_per_frame;
+};
+
+// Per list (one warp): sort the sample indices, then write every entry in
+// its expanded form (the dependent record loads happen here, across many
+// lists in flight, not in the row pass).
+template <int W>
+__global__ void __launch_bounds__(256) k_sort(SortArgs a) {
   extern __shared__ uint32_t sort_buf[];
+  constexpr int kMV = meta_vecs(W);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const size_t gl = static_cast<size_t>(blockIdx.x) * (blockDim.x >> 5) + warp;
-  if (gl >= static_cast<size_t>(frames) * lists_per_frame) return;
-  const int f = static_cast<int>(gl / lists_per_frame);
-  const int l = static_cast<int>(gl - static_cast<size_t>(f) * lists_per_frame);
-  const uint32_t* off = offsets + static_cast<size_t>(f) * (lists_per_frame + 1);
+  if (gl >= static_cast<size_t>(a.frames) * a.lists_per_frame) return;
+  const int f = static_cast<int>(gl / a.lists_per_frame);
+  const int l = static_cast<int>(gl - static_cast<size_t>(f) * a.lists_per_frame);
+  const uint32_t* off = a.offsets + static_cast<size_t>(f) * (a.lists_per_frame + 1);
   const uint32_t begin = off[l];
   const int n = static_cast<int>(off[l + 1] - begin);
-  if (n < 2) return;
-  uint32_t* ent = entries + static_cast<size_t>(f) * entries_per_frame + begin;
-  if (n <= capacity) {
-    uint32_t* buf = sort_buf + static_cast<size_t>(warp) * capacity;
-    for (int i = lane; i < n; i += 32) buf[i] = ent[i];
+  if (n == 0) return;
+  uint32_t* ent = a.entries + static_cast<size_t>(f) * a.entries_per_frame + begin;
+  const uint32_t* sorted = ent;
+  if (n >= 2) {
+    if (n <= a.capacity) {
+      uint32_t* buf = sort_buf + static_cast<size_t>(warp) * a.capacity;
+      for (int i = lane; i < n; i += 32) buf[i] = ent[i];
+      __syncwarp();
+      warp_sort(buf, n, lane);
+      for (int i = lane; i < n; i += 32) ent[i] = buf[i];
+      sorted = buf;
+    } else {
+      warp_sort(ent, n, lane);
+    }
     __syncwarp();
-    warp_sort(buf, n, lane);
-    for (int i = lane; i < n; i += 32) ent[i] = buf[i];
-  } else {
-    warp_sort(ent, n, lane);
+  }
+  const int row = l / a.nchunks;
+  const int col_lo = (l - row * a.nchunks) * kChunk;
+  const int col_hi = min(col_lo + kChunk, a.grid_cols);
+  const SampleRecord<W>* recs = reinterpret_cast<const SampleRecord<W>*>(a.records) + static_cast<size_t>(f) * a.samples;
+  float4* out = a.expanded + (static_cast<size_t>(f) * a.entries_per_frame + begin) * kMV;
+  for (int i = lane; i < n; i += 32) {
+    float4 e[kMV];
+    expand_entry<W>(recs, sorted[i], row, col_lo, col_hi, a.grid_rows, a.grid_cols, e);
+#pragma unroll
+    for (int v = 0; v < kMV; ++v) out[static_cast<size_t>(i) * kMV + v] = e[v];
+  }
+}
+
+// [frame][channel][sample] -> [frame][sample][channel] through a 32x33
+// shared tile (launch (32, 8) threads, grid (ceil(samples/32),
+// ceil(channels/32), frames)), checking every sample on the way: a
+// non-finite value (either component; bf16 exponent all ones) raises
+// KSJ_GPU_FLAG_NONFINITE_SAMPLE.
+template <uint32_t kFormat>
+__global__ void __launch_bounds__(256) k_samples_coil_last(const void* in_raw, void* out_raw, int channels,
+                                                           int samples, uint32_t* flags) {
+  using T = typename std::conditional<kFormat == KSJ_GPU_SAMPLES_BF16, uint32_t, unsigned long long>::type;
+  __shared__ T t[32][33];
+  const T* in = static_cast<const T*>(in_raw);
+  T* out = static_cast<T*>(out_raw);
+  const int f = blockIdx.z;
+  const int s0 = blockIdx.x * 32;
+  const int c0 = blockIdx.y * 32;
+  const T* src = in + static_cast<size_t>(f) * channels * samples;
+  T* dst = out + static_cast<size_t>(f) * channels * samples;
+  bool bad = false;
+  for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+    const int c = c0 + y, sm = s0 + threadIdx.x;
+    if (c < channels && sm < samples) {
+      const T v = src[static_cast<size_t>(c) * samples + sm];
+      if (kFormat == KSJ_GPU_SAMPLES_BF16) {
+        const uint32_t u = static_cast<uint32_t>(v);
+        bad |= (u & 0x7f80u) == 0x7f80u || (u & 0x7f800000u) == 0x7f800000u;
+      } else {
+        const uint64_t u = static_cast<uint64_t>(v);
+        bad |= (u & 0x7f800000ull) == 0x7f800000ull || (u & 0x7f80000000000000ull) == 0x7f80000000000000ull;
+      }
+      t[y][threadIdx.x] = v;
+    }
+  }
+  if (__syncthreads_or(bad) && threadIdx.x == 0 && threadIdx.y == 0) atomicOr(flags, KSJ_GPU_FLAG_NONFINITE_SAMPLE);
+  for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+    const int sm = s0 + y, c = c0 + threadIdx.x;
+    if (c < channels && sm < samples) dst[static_cast<size_t>(sm) * channels + c] = t[threadIdx.x][y];
   }
 }
 
 struct RowsArgs {
   int frame0;             // first frame of this pass
   const void* samples_t;  // [frame][sample][channel]
-  const unsigned char* records;
   const uint32_t* offsets;
-  const uint32_t* entries;
+  const float4* expanded;  // sorted list entries, expanded (meta_vecs(W) vectors each)
   const float2* tw_cols;
   const int* pos_cols;    // DIF output position of each kept column
   float2* inter;          // [frame][grid_row][out_col][cpitch]
@@ -565,8 +699,41 @@ __global__ void __launch_bounds__(kThreads, kBlocks) k_rows(RowsArgs a) {
   const int lane = tid & 31;
   float2* acc = reinterpret_cast<float2*>(smem_raw);
   float2* tw = acc + static_cast<size_t>(a.grid_cols) * cg;
+  uint32_t* offs = reinterpret_cast<uint32_t*>(tw + a.grid_cols);  // this row's list offsets
+  constexpr int kMV = meta_vecs(W);
+  constexpr int kBatch = meta_batch(W);
+  const int warp = tid >> 5;
+  // offsets from the shared array itself keep every access a shared-memory one
+  const size_t meta_off = (static_cast<size_t>(a.grid_cols) * (cg + 1) * sizeof(float2) +
+                           static_cast<size_t>(a.nchunks + 1) * sizeof(uint32_t) + 15) & ~static_cast<size_t>(15);
+  float4* meta = reinterpret_cast<float4*>(smem_raw + meta_off) + warp * kBatch * kMV;
   const AccAddr addr{cg};
 
+  const uint32_t* off = a.offsets + static_cast<size_t>(f) * (a.lists_per_frame + 1) + row * a.nchunks;
+  for (int i = tid; i <= a.nchunks; i += nthreads) offs[i] = __ldg(off + i);
+  // task order: the row's lists longest first (a bitonic sort across warp 0,
+  // one key per lane: length << 8 | chunk), taken from a shared counter
+  __shared__ int task_chunk[kMaxGrid / kChunk];
+  __shared__ int task_next;
+  if (warp == 0) {
+    int key = -1;
+    if (lane < a.nchunks) {
+      const uint32_t len = min(__ldg(off + lane + 1) - __ldg(off + lane), 1u << 22);
+      key = static_cast<int>(len << 8) | lane;
+    }
+#pragma unroll
+    for (int k = 2; k <= 32; k <<= 1) {
+#pragma unroll
+      for (int j = k >> 1; j > 0; j >>= 1) {
+        const int other = __shfl_xor_sync(0xffffffffu, key, j);
+        const bool lower = (lane & j) == 0;
+        const bool desc = (lane & k) == 0;
+        key = (lower == desc) ? max(key, other) : min(key, other);
+      }
+    }
+    if (lane < a.nchunks) task_chunk[lane] = key & 255;
+    if (lane == 0) task_next = 0;
+  }
   for (int i = tid; i < a.grid_cols * cg; i += nthreads) acc[i] = make_float2(0.0f, 0.0f);
   for (int i = tid; i < a.grid_cols; i += nthreads) tw[i] = a.tw_cols[i];
   __syncthreads();
@@ -575,85 +742,98 @@ __global__ void __launch_bounds__(kThreads, kBlocks) k_rows(RowsArgs a) {
   // list applied to a subset of the coil group.  Cells of different coils are
   // independent, so parts of one list may run on different warps with every
   // cell still summed in sample order.  Warps take tasks round-robin.
+  //
+  // Per batch of list entries, lane i loads entry i's sample index and record
+  // (vector loads), folds the row weight into the W column weights and stages
+  // them in the warp's shared batch; then the warp walks the batch in order
+  // with the coil loads of the next kAhead samples always in flight.
   const int parts = a.coil_parts;
   const int cpart = cg / parts;
   const int ntasks = a.nchunks * parts;
-  const uint32_t* off = a.offsets + static_cast<size_t>(f) * (a.lists_per_frame + 1);
   {
-    const SampleRecord<W>* recs =
-        reinterpret_cast<const SampleRecord<W>*>(a.records) + static_cast<size_t>(f) * a.samples;
     // lanes: coil = lane % cpp, tap group = lane / cpp
     int cpp = 1;
     while (cpp < cpart) cpp <<= 1;
     const int ngroups = 32 / cpp;
-    const int my_group = lane / cpp;
-    bool bad = false;
+    // taps j this lane applies: j mod ngroups equal to its tap group
+    uint32_t my_taps = 0;
+#pragma unroll
+    for (int j = 0; j < W; ++j)
+      if ((j & (ngroups - 1)) == lane / cpp) my_taps |= 1u << j;
     const void* ks = a.samples_t;
-    const int nwarps = nthreads >> 5;
-    for (int task = tid >> 5; task < ntasks; task += nwarps) {
-      const int chunk = task / parts;
-      const int part = task - chunk * parts;
-      const int list = row * a.nchunks + chunk;
-      const uint32_t begin = off[list];
-      const int n = static_cast<int>(off[list + 1] - begin);
-      const uint32_t* ent = a.entries + static_cast<size_t>(f) * a.entries_per_frame + begin;
+    for (;;) {
+      int task = 0;
+      if (lane == 0) task = atomicAdd(&task_next, 1);
+      task = __shfl_sync(0xffffffffu, task, 0);
+      if (task >= ntasks) break;
+      const int rank = task / parts;
+      const int chunk = task_chunk[rank];
+      const int part = task - rank * parts;
+      const uint32_t begin = offs[chunk];
+      const int n = static_cast<int>(offs[chunk + 1] - begin);
+      const float4* xent = a.expanded + (static_cast<size_t>(f) * a.entries_per_frame + begin) * kMV;
       const int col_lo = chunk * kChunk;
       const int col_hi = min(col_lo + kChunk, a.grid_cols);
       const int my_coil = part * cpart + lane % cpp;  // coil index within the group
       const int coil_global = cgi * cg + my_coil;
       const bool coil_ok = (lane % cpp) < cpart && coil_global < a.channels;
       const size_t sample_base = static_cast<size_t>(f) * a.samples * a.channels + (coil_ok ? coil_global : 0);
-      for (int base = 0; base < n; base += 32) {
-        const int cnt = min(32, n - base);
-        // lane i owns list entry base + i: its sample index, first tap column,
-        // the W tap weights of this row (row weight folded in) and dcf * phase
-        uint32_t my_s = 0;
-        int my_c0 = 0;
-        float2 my_scale = make_float2(0.0f, 0.0f);
-        float my_w[W];
-#pragma unroll
-        for (int j = 0; j < W; ++j) my_w[j] = 0.0f;
+      for (int base = 0; base < n; base += kBatch) {
+        const int cnt = min(kBatch, n - base);
         if (lane < cnt) {
-          my_s = __ldg(ent + base + lane);
-          const SampleRecord<W>& r = recs[my_s];
-          int ta = row - r.r0;
-          if (ta < 0) ta += a.grid_rows;
-          const float wr = r.wr[ta];
-          my_c0 = r.c0;
-          my_scale = r.scale;
+          const float4* src = xent + static_cast<size_t>(base + lane) * kMV;
+          float4* m = meta + lane * kMV;
 #pragma unroll
-          for (int j = 0; j < W; ++j) my_w[j] = wr * r.wc[j];
+          for (int v = 0; v < kMV; ++v) m[v] = __ldg(src + v);
         }
-        // groups of kAhead samples: all their coil loads in flight before the first use
-        for (int i0 = 0; i0 < cnt; i0 += kAhead) {
-          float2 yv[kAhead];
+        __syncwarp();
+        auto fetch = [&](int i) {
+          const uint32_t sk = __float_as_uint(meta[i * kMV].y);
+          return load_sample<kFormat>(ks, sample_base + static_cast<size_t>(sk) * a.channels);
+        };
+        float2 yv[kAhead];
 #pragma unroll
-          for (int k = 0; k < kAhead; ++k) {
-            const uint32_t sk = __shfl_sync(0xffffffffu, my_s, (i0 + k) & 31);
-            yv[k] = (coil_ok && i0 + k < cnt)
-                        ? load_sample<kFormat>(ks, sample_base + static_cast<size_t>(sk) * a.channels)
-                        : make_float2(0.0f, 0.0f);
-          }
+        for (int k = 0; k < kAhead; ++k) yv[k] = (coil_ok && k < cnt) ? fetch(k) : make_float2(0.0f, 0.0f);
+        for (int i0 = 0; i0 < cnt; i0 += kAhead) {
 #pragma unroll
           for (int k = 0; k < kAhead; ++k) {
             const int i = i0 + k;
             if (i >= cnt) break;
-            const int c0 = __shfl_sync(0xffffffffu, my_c0, i);
-            float2 sc;
-            sc.x = __shfl_sync(0xffffffffu, my_scale.x, i);
-            sc.y = __shfl_sync(0xffffffffu, my_scale.y, i);
-            float wt[W];
+            const float2 y = yv[k];
+            yv[k] = (coil_ok && i + kAhead < cnt) ? fetch(i + kAhead) : make_float2(0.0f, 0.0f);
+            const float4 m0 = meta[i * kMV];
+            float wt[4 * (kMV - 1)];
 #pragma unroll
-            for (int j = 0; j < W; ++j) wt[j] = __shfl_sync(0xffffffffu, my_w[j], i);
+            for (int v = 1; v < kMV; ++v) {
+              const float4 mv = meta[i * kMV + v];
+              wt[4 * (v - 1)] = mv.x;
+              wt[4 * (v - 1) + 1] = mv.y;
+              wt[4 * (v - 1) + 2] = mv.z;
+              wt[4 * (v - 1) + 3] = mv.w;
+            }
+            const int word0 = __float_as_int(m0.x);
+            const int cbase = word0 >> 9;  // arithmetic shift: may be negative
+            const uint32_t mask = static_cast<uint32_t>(word0) & my_taps;
             if (coil_ok) {
-              bad |= !(isfinite(yv[k].x) && isfinite(yv[k].y));
-              const float2 v = cmul(yv[k], sc);
+              const float2 v = cmul(y, make_float2(m0.z, m0.w));
+              if (!(word0 & 256)) {
+                // taps j of the mask are the consecutive cells cbase + j
+                const int base = addr(my_coil, cbase);
 #pragma unroll
-              for (int j = 0; j < W; ++j) {
-                if (j % ngroups != my_group) continue;
-                int col = c0 + j;
-                if (col >= a.grid_cols) col -= a.grid_cols;
-                if (col >= col_lo && col < col_hi) {
+                for (int j = 0; j < W; ++j) {
+                  if (!((mask >> j) & 1u)) continue;
+                  float2* cell = acc + (base + j * cg);
+                  float2 c = *cell;
+                  c.x = fmaf(v.x, wt[j], c.x);
+                  c.y = fmaf(v.y, wt[j], c.y);
+                  *cell = c;
+                }
+              } else {
+#pragma unroll
+                for (int j = 0; j < W; ++j) {
+                  if (!((mask >> j) & 1u)) continue;
+                  int col = cbase + j;
+                  if (col >= a.grid_cols) col -= a.grid_cols;
                   float2* cell = acc + addr(my_coil, col);
                   float2 c = *cell;
                   c.x = fmaf(v.x, wt[j], c.x);
@@ -662,12 +842,12 @@ __global__ void __launch_bounds__(kThreads, kBlocks) k_rows(RowsArgs a) {
                 }
               }
             }
-            __syncwarp();
+            // tap groups of one lane set may meet in a cell across samples
+            if (ngroups > 1) __syncwarp();
           }
         }
       }
     }
-    if (bad) atomicOr(a.flags, KSJ_GPU_FLAG_NONFINITE_SAMPLE);
   }
   __syncthreads();
 
@@ -839,7 +1019,7 @@ __global__ void __launch_bounds__(kColsThreads) k_cols(const __grid_constant__ C
 // ------------------------------------------------------------------ driver
 
 size_t rows_smem_bytes(const Shape& s) {
-  return static_cast<size_t>(s.grid_cols) * s.coil_group * sizeof(float2) + s.grid_cols * sizeof(float2);
+  return rows_smem_for(s.grid_cols, s.coil_group, s.width, rows_threads_for(s.grid_cols));
 }
 
 size_t cols_smem_bytes(const Shape& s) {
@@ -958,31 +1138,35 @@ ksj_gpu_status launch_all(const Shape& s, const Layout& l, const ksj_gpu_griddin
   }
   {
     const size_t smem = static_cast<size_t>(8) * s.list_capacity * 4;
-    if (cudaFuncSetAttribute(k_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)) !=
+    if (cudaFuncSetAttribute(k_sort<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)) !=
         cudaSuccess)
       return KSJ_GPU_ERROR_CUDA;
+    SortArgs sa{};
+    sa.offsets = offsets;
+    sa.entries = entries;
+    sa.records = records;
+    sa.expanded = reinterpret_cast<float4*>(ws + l.expanded);
+    sa.frames = s.frames;
+    sa.samples = s.samples;
+    sa.lists_per_frame = s.lists_per_frame;
+    sa.nchunks = s.nchunks;
+    sa.grid_rows = s.grid_rows;
+    sa.grid_cols = s.grid_cols;
+    sa.capacity = s.list_capacity;
+    sa.entries_per_frame = s.entries_per_frame;
     LaunchScope scope("k_sort", stream);
-    k_sort<<<static_cast<unsigned>((nl + 7) / 8), 256, smem, stream>>>(offsets, entries, s.frames,
-                                                                        s.lists_per_frame, s.entries_per_frame,
-                                                                        s.list_capacity);
+    k_sort<W><<<static_cast<unsigned>((nl + 7) / 8), 256, smem, stream>>>(sa);
   }
   {
     const dim3 tg((s.samples + 31) / 32, (s.channels + 31) / 32, s.frames);
     LaunchScope scope("k_samples_coil_last", stream);
-    if (kFormat == KSJ_GPU_SAMPLES_BF16)
-      k_transpose<uint32_t><<<tg, dim3(32, 8), 0, stream>>>(static_cast<const uint32_t*>(d_kspace),
-                                                            reinterpret_cast<uint32_t*>(ws + l.samples_t),
-                                                            s.channels, s.samples);
-    else
-      k_transpose<unsigned long long><<<tg, dim3(32, 8), 0, stream>>>(
-          static_cast<const unsigned long long*>(d_kspace), reinterpret_cast<unsigned long long*>(ws + l.samples_t),
-          s.channels, s.samples);
+    k_samples_coil_last<kFormat><<<tg, dim3(32, 8), 0, stream>>>(d_kspace, ws + l.samples_t, s.channels, s.samples,
+                                                                 flags);
   }
   RowsArgs r{};
   r.samples_t = ws + l.samples_t;
-  r.records = records;
   r.offsets = offsets;
-  r.entries = entries;
+  r.expanded = reinterpret_cast<const float4*>(ws + l.expanded);
   r.tw_cols = tw_cols;
   r.pos_cols = pos_cols;
   r.inter = inter;
@@ -1001,7 +1185,7 @@ ksj_gpu_status launch_all(const Shape& s, const Layout& l, const ksj_gpu_griddin
   r.cpitch = s.cpitch;
   r.plan = s.plan_cols;
   const size_t rows_smem = rows_smem_bytes(s);
-  const int rows_threads = std::max(64, s.nchunks * 32);
+  const int rows_threads = rows_threads_for(s.grid_cols);
   auto rows_kernel = (rows_threads <= 384 && s.rows_blocks == 2) ? k_rows<W, kFormat, 384, 2>
                                                                  : k_rows<W, kFormat, kMaxThreads, 1>;
   if (cudaFuncSetAttribute(rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(rows_smem)) !=

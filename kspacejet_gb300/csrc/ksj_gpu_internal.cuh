@@ -352,6 +352,44 @@ __device__ __forceinline__ void dif_stage(float2* smem, int lg_lines, int nbf, i
   }
 }
 
+// The same stage with two adjacent lines per thread: one 16-byte access
+// moves an element of both lines, and the lines share the twiddle loads and
+// the index arithmetic.  Needs an even line count (16-byte aligned smem).
+template <int R>
+__device__ __forceinline__ void dif_stage_pairs(float2* smem, int lg_lines, int nbf, int lg_m, int tws,
+                                                const float2* __restrict__ tw, int tid, int nthreads) {
+  const int lg_pairs = lg_lines - 1;
+  const int lp = tid & ((1 << lg_pairs) - 1);
+  const int step = nthreads >> lg_pairs;
+  const int mmask = (1 << lg_m) - 1;
+  float4* s4 = reinterpret_cast<float4*>(smem);  // elements (2 lp, 2 lp + 1) of index x at s4[(x << lg_pairs) + lp]
+  for (int u = tid >> lg_pairs; u < nbf; u += step) {
+    const int base = (((u >> lg_m) * R) << lg_m) + (u & mmask);
+    float4* e = s4 + (base << lg_pairs) + lp;
+    const int stride = 1 << (lg_m + lg_pairs);
+    float2 va[R], vb[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const float4 q = e[r * stride];
+      va[r] = make_float2(q.x, q.y);
+      vb[r] = make_float2(q.z, q.w);
+    }
+    dft_inverse<R>(va);
+    dft_inverse<R>(vb);
+    const int i = u & mmask;
+    if (i != 0) {
+#pragma unroll
+      for (int d = 1; d < R; ++d) {
+        const float2 w = tw[i * d * tws];
+        va[d] = cmul(va[d], w);
+        vb[d] = cmul(vb[d], w);
+      }
+    }
+#pragma unroll
+    for (int d = 0; d < R; ++d) e[d * stride] = make_float4(va[d].x, va[d].y, vb[d].x, vb[d].y);
+  }
+}
+
 // Unnormalised inverse FFT (exp(+2 pi i n k / N)) of every line, in place,
 // output digit-reversed; tw[t] = exp(2 pi i t / n).  Requires nthreads to be
 // a multiple of the line count.  Synchronises the block after each stage.
@@ -359,12 +397,22 @@ __device__ __forceinline__ void dif_lines(float2* smem, int lg_lines, const DifP
                                           const float2* __restrict__ tw, int tid, int nthreads) {
   for (int s = 0; s < p.stages; ++s) {
     const int nbf = p.nbf[s], lg_m = p.lg_m[s], tws = p.tw_stride[s];
-    switch (p.radix[s]) {
-      case 8: dif_stage<8>(smem, lg_lines, nbf, lg_m, tws, tw, tid, nthreads); break;
-      case 6: dif_stage<6>(smem, lg_lines, nbf, lg_m, tws, tw, tid, nthreads); break;
-      case 4: dif_stage<4>(smem, lg_lines, nbf, lg_m, tws, tw, tid, nthreads); break;
-      case 3: dif_stage<3>(smem, lg_lines, nbf, lg_m, tws, tw, tid, nthreads); break;
-      default: dif_stage<2>(smem, lg_lines, nbf, lg_m, tws, tw, tid, nthreads); break;
+    if (lg_lines >= 1) {
+      switch (p.radix[s]) {
+        case 8: dif_stage_pairs<8>(smem, lg_lines, nbf, lg_m, tws, tw, tid, nthreads); break;
+        case 6: dif_stage_pairs<6>(smem, lg_lines, nbf, lg_m, tws, tw, tid, nthreads); break;
+        case 4: dif_stage_pairs<4>(smem, lg_lines, nbf, lg_m, tws, tw, tid, nthreads); break;
+        case 3: dif_stage_pairs<3>(smem, lg_lines, nbf, lg_m, tws, tw, tid, nthreads); break;
+        default: dif_stage_pairs<2>(smem, lg_lines, nbf, lg_m, tws, tw, tid, nthreads); break;
+      }
+    } else {
+      switch (p.radix[s]) {
+        case 8: dif_stage<8>(smem, lg_lines, nbf, lg_m, tws, tw, tid, nthreads); break;
+        case 6: dif_stage<6>(smem, lg_lines, nbf, lg_m, tws, tw, tid, nthreads); break;
+        case 4: dif_stage<4>(smem, lg_lines, nbf, lg_m, tws, tw, tid, nthreads); break;
+        case 3: dif_stage<3>(smem, lg_lines, nbf, lg_m, tws, tw, tid, nthreads); break;
+        default: dif_stage<2>(smem, lg_lines, nbf, lg_m, tws, tw, tid, nthreads); break;
+      }
     }
     __syncthreads();
   }
