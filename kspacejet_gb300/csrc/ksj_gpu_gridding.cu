@@ -687,13 +687,16 @@ struct AccAddr {
 
 // kBlocks CTAs per SM: 2 for rows of up to 384 columns (384 threads), 1
 // above; two resident CTAs let one block's FFT overlap another's gridding.
-template <int W, uint32_t kFormat, int kThreads, int kBlocks>
+// kCG = 32 fixes a 32-coil group taken whole by one warp (coil_parts 1):
+// lane = coil, no tap groups, every tap offset a constant; kCG = 0 reads the
+// group and the split from the arguments.
+template <int W, uint32_t kFormat, int kThreads, int kBlocks, int kCG>
 __global__ void __launch_bounds__(kThreads, kBlocks) k_rows(RowsArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int row = blockIdx.x;
   const int cgi = blockIdx.y;
   const int f = a.frame0 + blockIdx.z;
-  const int cg = a.coil_group;
+  const int cg = kCG ? kCG : a.coil_group;
   const int tid = threadIdx.x;
   const int nthreads = blockDim.x;
   const int lane = tid & 31;
@@ -747,7 +750,7 @@ __global__ void __launch_bounds__(kThreads, kBlocks) k_rows(RowsArgs a) {
   // (vector loads), folds the row weight into the W column weights and stages
   // them in the warp's shared batch; then the warp walks the batch in order
   // with the coil loads of the next kAhead samples always in flight.
-  const int parts = a.coil_parts;
+  const int parts = kCG ? 1 : a.coil_parts;
   const int cpart = cg / parts;
   const int ntasks = a.nchunks * parts;
   {
@@ -1186,8 +1189,10 @@ ksj_gpu_status launch_all(const Shape& s, const Layout& l, const ksj_gpu_griddin
   r.plan = s.plan_cols;
   const size_t rows_smem = rows_smem_bytes(s);
   const int rows_threads = rows_threads_for(s.grid_cols);
-  auto rows_kernel = (rows_threads <= 384 && s.rows_blocks == 2) ? k_rows<W, kFormat, 384, 2>
-                                                                 : k_rows<W, kFormat, kMaxThreads, 1>;
+  const bool whole32 = s.coil_group == 32 && s.coil_parts == 1;
+  auto rows_kernel = (rows_threads <= 384 && s.rows_blocks == 2)
+                         ? (whole32 ? k_rows<W, kFormat, 384, 2, 32> : k_rows<W, kFormat, 384, 2, 0>)
+                         : (whole32 ? k_rows<W, kFormat, kMaxThreads, 1, 32> : k_rows<W, kFormat, kMaxThreads, 1, 0>);
   if (cudaFuncSetAttribute(rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(rows_smem)) !=
           cudaSuccess ||
       cudaFuncSetAttribute(rows_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100) != cudaSuccess)
