@@ -48,8 +48,8 @@ WORKLOAD = "batched dynamic 2D radial adjoint (KB W=4, sigma=2) + RSS"
 def workload_config(extra: dict | None = None) -> dict:
     cfg = {"workload": WORKLOAD, "frames": FRAMES, "spokes_per_frame": SPOKES, "readout": READOUT, "coils": COILS,
            "image": IMAGE, "grid": GRID, "kernel": "kaiser_bessel", "kernel_width": WIDTH, "oversampling": 2.0,
-           "dcf": "analytic ramp (Ram-Lak)", "output": "rss float32 [96,192,192]",
-           "l2": "inputs larger than L2 (321 MB samples)"}
+           "dcf": "analytic ramp (Ram-Lak)", "output": f"rss float32 [{FRAMES},{IMAGE},{IMAGE}]",
+           "l2": f"inputs larger than L2 ({FRAMES * SPOKES * READOUT * COILS * 8 / 1e6:.0f} MB samples)"}
     if extra:
         cfg.update(extra)
     return cfg
@@ -69,15 +69,20 @@ class ClockSampler:
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
+    """nvidia-smi sampled every 25 ms from before the first timed region to after
+    the last; summary() keeps the samples that arrived inside the timed windows
+    (host monotonic clock, 60 ms of slack for the tool's reporting delay)."""
+
     def __init__(self, device_index: int):
         self.device_index = device_index
         self.proc = None
-        self.lines: list[str] = []
+        self.lines: list[tuple[float, str]] = []
+        self.windows: list[tuple[float, float]] = []
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device_index}", f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                          "--format=csv,noheader,nounits", "-lms", "25"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
@@ -87,7 +92,7 @@ class ClockSampler:
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.monotonic(), line.strip()))
 
     def __exit__(self, *a):
         if self.proc is not None:
@@ -97,10 +102,23 @@ class ClockSampler:
             except subprocess.TimeoutExpired:
                 self.proc.kill()
 
+    def window(self):
+        """Context manager marking one timed region."""
+        sampler = self
+
+        class _W:
+            def __enter__(self):
+                self.t0 = time.monotonic()
+
+            def __exit__(self, *a):
+                sampler.windows.append((self.t0, time.monotonic()))
+        return _W()
+
     def summary(self) -> dict:
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in self.lines:
+        inside = [ln for t, ln in self.lines if any(a <= t <= b + 0.06 for a, b in self.windows)]
+        for line in inside:
             parts = [p.strip() for p in line.split(",")]
             if len(parts) < 9:
                 continue
@@ -116,7 +134,7 @@ class ClockSampler:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
         loaded = [s for s in sm if s > 0.5 * max(sm)] or sm
         return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "timed_windows": len(self.windows)}
 
 
 # --------------------------------------------------------- CPU baseline
@@ -190,11 +208,13 @@ def kernel_bytes(g, entries: int) -> dict:
     """Algorithmic HBM bytes per launch of each kernel of one call."""
     F, C, M = g.frames, g.channels, g.samples
     N, G = IMAGE, GRID
-    rec = 16 + 8 * WIDTH
-    inter = F * C * G * N * 8
+    rec = 16 + 8 * WIDTH                      # per-sample record written by k_prepare
+    expanded = 16 * (1 + (WIDTH + 3) // 4)    # per list entry as the row pass reads it
+    inter = F * C * G * N * 8                 # row-transformed grid, kept columns only
     return {
-        "k_rows": F * M * C * 8 + F * M * rec + entries * 4 + inter,
+        "k_rows": F * M * C * 8 + entries * expanded + inter,
         "k_cols": inter + F * N * N * 4,
+        "k_sort": entries * (4 + 4 + expanded) + F * M * rec,
         "k_samples_coil_last": 2 * F * C * M * 8,
         "k_prepare": F * M * 8 + F * M * rec,
     }
@@ -218,6 +238,7 @@ def run_ours(args) -> dict | None:
     out = g.new_output(dev)
     ws = g.new_workspace(dev)
     stream = torch.cuda.current_stream()
+    clocks = ClockSampler(local_rank).__enter__()
     tuning = g.tune(k, t, out, ws)
     for _ in range(args.warmup):
         g.run(k, t, out, ws, tuning=tuning)
@@ -257,7 +278,7 @@ def run_ours(args) -> dict | None:
     # ---- value: device-resident inputs
     barrier()
     torch.cuda.synchronize()
-    with ClockSampler(local_rank) as clocks:
+    with clocks.window():
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
@@ -276,11 +297,14 @@ def run_ours(args) -> dict | None:
     l0 = gpu.launch_count()
     d0 = torch.cuda.Event(enable_timing=True)
     d1 = torch.cuda.Event(enable_timing=True)
-    d0.record(stream)
-    for _ in range(args.steps):
-        g.run(k, t, out, ws, tuning=tuning)
-    d1.record(stream)
-    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_push("ksj_timed")  # ncu --nvtx --nvtx-include ksj_timed/ lists exactly these launches
+    with clocks.window():
+        d0.record(stream)
+        for _ in range(args.steps):
+            g.run(k, t, out, ws, tuning=tuning)
+        d1.record(stream)
+        torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
     per_call_launches = (gpu.launch_count() - l0) // args.steps
     gpu.timing_enable(False)
     kernels = gpu.timing_read()
@@ -317,14 +341,16 @@ def run_ours(args) -> dict | None:
     torch.cuda.synchronize()
     x0 = torch.cuda.Event(enable_timing=True)
     x1 = torch.cuda.Event(enable_timing=True)
-    x0.record(stream)
-    for _ in range(args.steps):
-        k.copy_(kh, non_blocking=True)
-        t.copy_(th, non_blocking=True)
-        g.run(k, t, out, ws, tuning=tuning)
-        oh.copy_(out, non_blocking=True)
-    x1.record(stream)
-    torch.cuda.synchronize()
+    with clocks.window():
+        x0.record(stream)
+        for _ in range(args.steps):
+            k.copy_(kh, non_blocking=True)
+            t.copy_(th, non_blocking=True)
+            g.run(k, t, out, ws, tuning=tuning)
+            oh.copy_(out, non_blocking=True)
+        x1.record(stream)
+        torch.cuda.synchronize()
+    clocks.__exit__(None, None, None)
     barrier()
     e2e_ms = x0.elapsed_time(x1) / args.steps
     if not np.isfinite(oh.numpy()).all():
@@ -510,16 +536,20 @@ def run_serve(args) -> dict:
 
 
 def main() -> int:
+    global FRAMES
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--frames", type=int, default=FRAMES,
+                    help="frames per call (default: the 96-frame workload; fewer only for small profiling cases)")
     ap.add_argument("--serve", action="store_true", help="served-stream benchmark (separate JSON line)")
     ap.add_argument("--serve-requests", type=int, default=160)
     ap.add_argument("--serve-slots", type=int, default=4)
     ap.add_argument("--serve-cap-gib", type=int, default=24)
     args = ap.parse_args()
+    FRAMES = args.frames
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
     if args.serve:
