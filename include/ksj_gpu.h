@@ -149,6 +149,25 @@ KSJ_GPU_API ksj_gpu_status ksj_gpu_gridding_tune(const ksj_gpu_gridding_desc* de
                                                  void* d_workspace, size_t workspace_bytes, void* stream,
                                                  ksj_gpu_gridding_tuning* tuning);
 
+/* ------------------------------------------------- Pipe-Menon density weights */
+
+/* Iterative density compensation (Pipe and Menon, MRM 41:179-186, 1999; no
+ * counterpart in the reference) for the Kaiser-Bessel gridding of `desc`
+ * (kernel KSJ_GPU_KERNEL_KAISER_BESSEL; grid, width, beta, frames and samples
+ * are used, channels and output are not):
+ *   w = 1; repeat `iterations` times:
+ *     c = grid of w through phi (every cell sums its samples in increasing order),
+ *     d_s = c read back through sample s's taps, w_s = w_s / d_s (0 if d_s <= 0),
+ * phi the same tap set and kernel as the gridding, all in double precision.
+ *   d_traj [frame][sample][2] float32 radians per pixel
+ *   d_dcf  [frame][sample] float32 out: the final weights, usable as
+ *          KSJ_GPU_DCF_EXTERNAL for the same gridding
+ * Workspace: ksj_gpu_pipe_menon_workspace_bytes (0 on a bad desc). */
+KSJ_GPU_API size_t ksj_gpu_pipe_menon_workspace_bytes(const ksj_gpu_gridding_desc* desc);
+KSJ_GPU_API ksj_gpu_status ksj_gpu_pipe_menon_dcf(const ksj_gpu_gridding_desc* desc, uint32_t iterations,
+                                                  const float* d_traj, float* d_dcf, void* d_workspace,
+                                                  size_t workspace_bytes, void* stream);
+
 /* ----------------------------------------------------------- direct NUDFT */
 
 /* Exact direct adjoint NUDFT, no DCF:

@@ -609,6 +609,7 @@ __global__ void __launch_bounds__(256) k_sort(SortArgs a) {
     }
     __syncwarp();
   }
+  if (a.expanded == nullptr) return;  // lists only (density compensation)
   const int row = l / a.nchunks;
   const int col_lo = (l - row * a.nchunks) * kChunk;
   const int col_hi = min(col_lo + kChunk, a.grid_cols);
@@ -1071,38 +1072,16 @@ bool make_inter_map(const Shape& s, void* inter, CUtensorMap* map, int* box_rows
              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-template <int W, uint32_t kFormat>
-ksj_gpu_status launch_all(const Shape& s, const Layout& l, const ksj_gpu_gridding_desc* d, const void* d_kspace,
-                          const float* d_traj, const float* d_dcf, void* d_out, unsigned char* ws,
-                          cudaStream_t stream) {
-  uint32_t* flags = reinterpret_cast<uint32_t*>(ws + l.flags);
-  unsigned char* records = ws + l.records;
-  uint32_t* counts = reinterpret_cast<uint32_t*>(ws + l.counts);
-  uint32_t* cursor = reinterpret_cast<uint32_t*>(ws + l.cursor);
-  uint32_t* offsets = reinterpret_cast<uint32_t*>(ws + l.offsets);
-  uint32_t* entries = reinterpret_cast<uint32_t*>(ws + l.entries);
-  float2* inter = reinterpret_cast<float2*>(ws + l.inter);
-  float2* tw_rows = reinterpret_cast<float2*>(ws + l.tables);
-  float2* tw_cols = tw_rows + s.grid_rows;
-  float* inv_dr = reinterpret_cast<float*>(tw_cols + s.grid_cols);
-  float* inv_dc = inv_dr + s.out_rows;
-  int* pos_rows = reinterpret_cast<int*>(inv_dc + s.out_cols);
-  int* pos_cols = pos_rows + s.out_rows;
+// The binning lists of one call: per-sample records, list counts, offsets,
+// the scattered entries and their sort (and, when `expanded` is given, the
+// expanded entries the row pass reads).  `flags` must already be cleared.
+template <int W>
+ksj_gpu_status build_lists(const Shape& s, const ksj_gpu_gridding_desc* d, const float* d_traj, const float* d_dcf,
+                           uint32_t* flags, unsigned char* records, uint32_t* counts, uint32_t* cursor,
+                           uint32_t* offsets, uint32_t* entries, float4* expanded, cudaStream_t stream) {
   const size_t nl = static_cast<size_t>(s.frames) * s.lists_per_frame;
-
-  if (cudaMemsetAsync(flags, 0, kFlagBytes, stream) != cudaSuccess) return KSJ_GPU_ERROR_CUDA;
   if (cudaMemsetAsync(counts, 0, nl * 4, stream) != cudaSuccess) return KSJ_GPU_ERROR_CUDA;
   if (cudaMemsetAsync(cursor, 0, nl * 4, stream) != cudaSuccess) return KSJ_GPU_ERROR_CUDA;
-
-  {
-    const int n = std::max(std::max(s.grid_rows, s.grid_cols), std::max(s.out_rows, s.out_cols));
-    const double beta = s.beta;
-    LaunchScope scope("k_tables", stream);
-    k_tables<<<(n + 255) / 256, 256, 0, stream>>>(tw_rows, s.grid_rows, tw_cols, s.grid_cols, inv_dr, s.out_rows,
-                                                  inv_dc, s.out_cols, pos_rows, pos_cols, s.plan_rows, s.plan_cols,
-                                                  s.kb ? 1 : 0, s.width, beta,
-                                                  s.kb ? std::cyl_bessel_i(0.0, beta) : 1.0);
-  }
   const size_t fm = static_cast<size_t>(s.frames) * s.samples;
   {
     PrepareArgs p{};
@@ -1148,7 +1127,7 @@ ksj_gpu_status launch_all(const Shape& s, const Layout& l, const ksj_gpu_griddin
     sa.offsets = offsets;
     sa.entries = entries;
     sa.records = records;
-    sa.expanded = reinterpret_cast<float4*>(ws + l.expanded);
+    sa.expanded = expanded;
     sa.frames = s.frames;
     sa.samples = s.samples;
     sa.lists_per_frame = s.lists_per_frame;
@@ -1159,6 +1138,42 @@ ksj_gpu_status launch_all(const Shape& s, const Layout& l, const ksj_gpu_griddin
     sa.entries_per_frame = s.entries_per_frame;
     LaunchScope scope("k_sort", stream);
     k_sort<W><<<static_cast<unsigned>((nl + 7) / 8), 256, smem, stream>>>(sa);
+  }
+  return KSJ_GPU_OK;
+}
+
+template <int W, uint32_t kFormat>
+ksj_gpu_status launch_all(const Shape& s, const Layout& l, const ksj_gpu_gridding_desc* d, const void* d_kspace,
+                          const float* d_traj, const float* d_dcf, void* d_out, unsigned char* ws,
+                          cudaStream_t stream) {
+  uint32_t* flags = reinterpret_cast<uint32_t*>(ws + l.flags);
+  unsigned char* records = ws + l.records;
+  uint32_t* counts = reinterpret_cast<uint32_t*>(ws + l.counts);
+  uint32_t* cursor = reinterpret_cast<uint32_t*>(ws + l.cursor);
+  uint32_t* offsets = reinterpret_cast<uint32_t*>(ws + l.offsets);
+  uint32_t* entries = reinterpret_cast<uint32_t*>(ws + l.entries);
+  float2* inter = reinterpret_cast<float2*>(ws + l.inter);
+  float2* tw_rows = reinterpret_cast<float2*>(ws + l.tables);
+  float2* tw_cols = tw_rows + s.grid_rows;
+  float* inv_dr = reinterpret_cast<float*>(tw_cols + s.grid_cols);
+  float* inv_dc = inv_dr + s.out_rows;
+  int* pos_rows = reinterpret_cast<int*>(inv_dc + s.out_cols);
+  int* pos_cols = pos_rows + s.out_rows;
+
+  if (cudaMemsetAsync(flags, 0, kFlagBytes, stream) != cudaSuccess) return KSJ_GPU_ERROR_CUDA;
+  {
+    const int n = std::max(std::max(s.grid_rows, s.grid_cols), std::max(s.out_rows, s.out_cols));
+    const double beta = s.beta;
+    LaunchScope scope("k_tables", stream);
+    k_tables<<<(n + 255) / 256, 256, 0, stream>>>(tw_rows, s.grid_rows, tw_cols, s.grid_cols, inv_dr, s.out_rows,
+                                                  inv_dc, s.out_cols, pos_rows, pos_cols, s.plan_rows, s.plan_cols,
+                                                  s.kb ? 1 : 0, s.width, beta,
+                                                  s.kb ? std::cyl_bessel_i(0.0, beta) : 1.0);
+  }
+  {
+    const ksj_gpu_status st = build_lists<W>(s, d, d_traj, d_dcf, flags, records, counts, cursor, offsets, entries,
+                                             reinterpret_cast<float4*>(ws + l.expanded), stream);
+    if (st != KSJ_GPU_OK) return st;
   }
   {
     const dim3 tg((s.samples + 31) / 32, (s.channels + 31) / 32, s.frames);
@@ -1249,6 +1264,194 @@ ksj_gpu_status launch_all(const Shape& s, const Layout& l, const ksj_gpu_griddin
     k_transpose<unsigned long long><<<tg, dim3(32, 8), 0, stream>>>(
         reinterpret_cast<const unsigned long long*>(ws + l.coil_last), static_cast<unsigned long long*>(d_out),
         pixels, s.channels);
+  }
+  return check_launch();
+}
+
+// ------------------------------------------------- Pipe-Menon density weights
+//
+// w <- w / ((w * phi) sampled back through phi), phi the Kaiser-Bessel
+// gridding kernel, 10 iterations by default, in double precision (Pipe and
+// Menon, MRM 1999; grid-based form).  The binning lists of the gridding path
+// give, per (row, 16-column chunk), the samples touching it in increasing
+// order, so each grid cell sums its samples in that order: deterministic.
+
+template <int W>
+struct PmRecord {
+  int r0, c0;  // first tap row and column (wrapped)
+  double wr[W];
+  double wc[W];
+};
+
+__device__ __forceinline__ double kb_weight64(double d, int width, double beta, double inv_i0_beta) {
+  const double t = 2.0 * d / static_cast<double>(width);
+  if (t * t > 1.0) return 0.0;
+  return cyl_bessel_i0(beta * sqrt(1.0 - t * t)) * inv_i0_beta;
+}
+
+// Per sample: the double-precision tap weights and w = 1.  The coordinate
+// u = k g / (2 pi) is formed in double (an exact product, one rounded
+// division); a sample the gridding checks rejected gets w = 0.
+template <int W>
+__global__ void __launch_bounds__(256) k_pm_prepare(const float* traj, PmRecord<W>* pm, double* w, size_t total,
+                                                    int grid_rows, int grid_cols, double beta, double inv_i0_beta,
+                                                    int require_nyquist) {
+  const size_t idx = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (idx >= total) return;
+  const float2 k = __ldg(reinterpret_cast<const float2*>(traj) + idx);
+  bool ok = isfinite(k.x) && isfinite(k.y);
+  if (ok && require_nyquist) ok = k.x >= -kPiF && k.x <= kPiF && k.y >= -kPiF && k.y <= kPiF;
+  if (ok && !require_nyquist) ok = fabsf(k.x) < 1.0e4f && fabsf(k.y) < 1.0e4f;
+  PmRecord<W> r;
+  constexpr double kTwoPiD = 6.283185307179586476925286766559;
+  if (ok) {
+    const double ur = static_cast<double>(k.x) * grid_rows / kTwoPiD;
+    const double uc = static_cast<double>(k.y) * grid_cols / kTwoPiD;
+    const int tr = static_cast<int>(floor(ur)) - W / 2 + 1;
+    const int tc = static_cast<int>(floor(uc)) - W / 2 + 1;
+    r.r0 = wrap_index(tr, grid_rows);
+    r.c0 = wrap_index(tc, grid_cols);
+#pragma unroll
+    for (int j = 0; j < W; ++j) {
+      r.wr[j] = kb_weight64(static_cast<double>(tr + j) - ur, W, beta, inv_i0_beta);
+      r.wc[j] = kb_weight64(static_cast<double>(tc + j) - uc, W, beta, inv_i0_beta);
+    }
+  } else {
+    r.r0 = 0;
+    r.c0 = 0;
+#pragma unroll
+    for (int j = 0; j < W; ++j) {
+      r.wr[j] = 0.0;
+      r.wc[j] = 0.0;
+    }
+  }
+  pm[idx] = r;
+  w[idx] = ok ? 1.0 : 0.0;
+}
+
+// One half-warp per list; lane l % 16 is the list's column chunk * 16 + l % 16.
+// Every cell of the grid belongs to exactly one list, so every cell is written.
+template <int W>
+__global__ void __launch_bounds__(256) k_pm_grid(const uint32_t* offsets, const uint32_t* entries,
+                                                 const PmRecord<W>* pm, const double* w, double* grid, int frames,
+                                                 int samples, int grid_rows, int grid_cols, int nchunks,
+                                                 int lists_per_frame, size_t entries_per_frame) {
+  const size_t hw = (static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 4;
+  const int sub = threadIdx.x & 15;
+  if (hw >= static_cast<size_t>(frames) * lists_per_frame) return;
+  const int f = static_cast<int>(hw / lists_per_frame);
+  const int l = static_cast<int>(hw - static_cast<size_t>(f) * lists_per_frame);
+  const int row = l / nchunks;
+  const int col = (l - row * nchunks) * kChunk + sub;
+  const uint32_t* off = offsets + static_cast<size_t>(f) * (lists_per_frame + 1);
+  const uint32_t begin = off[l], end = off[l + 1];
+  const uint32_t* ent = entries + static_cast<size_t>(f) * entries_per_frame;
+  const PmRecord<W>* rec = pm + static_cast<size_t>(f) * samples;
+  const double* wf = w + static_cast<size_t>(f) * samples;
+  double acc = 0.0;
+  for (uint32_t e = begin; e < end; ++e) {
+    const uint32_t sidx = __ldg(ent + e);
+    const PmRecord<W>& r = rec[sidx];
+    int dc = col - r.c0;
+    if (dc < 0) dc += grid_cols;
+    int dr = row - r.r0;
+    if (dr < 0) dr += grid_rows;
+    if (dc < W && dr < W) acc += wf[sidx] * (r.wr[dr] * r.wc[dc]);
+  }
+  if (col < grid_cols) grid[(static_cast<size_t>(f) * grid_rows + row) * grid_cols + col] = acc;
+}
+
+// Per sample: d = the grid read back through the sample's taps (row-major),
+// w = w / d (0 when d is not positive); the last iteration also writes the
+// float weights.
+template <int W>
+__global__ void __launch_bounds__(256) k_pm_update(const PmRecord<W>* pm, const double* grid, double* w, float* out,
+                                                   size_t total, int samples, int grid_rows, int grid_cols) {
+  const size_t idx = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (idx >= total) return;
+  const size_t f = idx / samples;
+  const PmRecord<W> r = pm[idx];
+  const double* g = grid + f * grid_rows * grid_cols;
+  double d = 0.0;
+#pragma unroll
+  for (int a = 0; a < W; ++a) {
+    int rr = r.r0 + a;
+    if (rr >= grid_rows) rr -= grid_rows;
+#pragma unroll
+    for (int b = 0; b < W; ++b) {
+      int cc = r.c0 + b;
+      if (cc >= grid_cols) cc -= grid_cols;
+      d += g[static_cast<size_t>(rr) * grid_cols + cc] * (r.wr[a] * r.wc[b]);
+    }
+  }
+  const double nw = d > 0.0 ? w[idx] / d : 0.0;
+  w[idx] = nw;
+  if (out != nullptr) out[idx] = static_cast<float>(nw);
+}
+
+struct PmLayout {
+  size_t flags, records, counts, cursor, offsets, entries, pm, w, grid, total;
+};
+
+PmLayout make_pm_layout(const Shape& s) {
+  PmLayout l{};
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    const size_t at = off;
+    off = align_up(off + bytes, 256);
+    return at;
+  };
+  const size_t fm = static_cast<size_t>(s.frames) * s.samples;
+  const size_t nl = static_cast<size_t>(s.frames) * s.lists_per_frame;
+  l.flags = take(kFlagBytes);
+  l.records = take(fm * record_bytes(s.width));
+  l.counts = take(nl * 4);
+  l.cursor = take(nl * 4);
+  l.offsets = take((nl + s.frames) * 4);
+  l.entries = take(static_cast<size_t>(s.frames) * s.entries_per_frame * 4);
+  l.pm = take(fm * (8 + 16 * static_cast<size_t>(s.width)));
+  l.w = take(fm * sizeof(double));
+  l.grid = take(static_cast<size_t>(s.frames) * s.grid_rows * s.grid_cols * sizeof(double));
+  l.total = off;
+  return l;
+}
+
+template <int W>
+ksj_gpu_status launch_pipe_menon(const Shape& s, const PmLayout& l, const ksj_gpu_gridding_desc* d,
+                                 uint32_t iterations, const float* d_traj, float* d_dcf, unsigned char* ws,
+                                 cudaStream_t stream) {
+  static_assert(sizeof(PmRecord<W>) == 8 + 16 * W, "PmRecord layout");
+  uint32_t* flags = reinterpret_cast<uint32_t*>(ws + l.flags);
+  if (cudaMemsetAsync(flags, 0, kFlagBytes, stream) != cudaSuccess) return KSJ_GPU_ERROR_CUDA;
+  ksj_gpu_gridding_desc dd = *d;
+  dd.dcf_mode = KSJ_GPU_DCF_NONE;
+  const ksj_gpu_status st =
+      build_lists<W>(s, &dd, d_traj, nullptr, flags, ws + l.records, reinterpret_cast<uint32_t*>(ws + l.counts),
+                     reinterpret_cast<uint32_t*>(ws + l.cursor), reinterpret_cast<uint32_t*>(ws + l.offsets),
+                     reinterpret_cast<uint32_t*>(ws + l.entries), nullptr, stream);
+  if (st != KSJ_GPU_OK) return st;
+  const size_t fm = static_cast<size_t>(s.frames) * s.samples;
+  PmRecord<W>* pm = reinterpret_cast<PmRecord<W>*>(ws + l.pm);
+  double* w = reinterpret_cast<double*>(ws + l.w);
+  double* grid = reinterpret_cast<double*>(ws + l.grid);
+  const double beta = s.beta;
+  {
+    LaunchScope scope("k_pm_prepare", stream);
+    k_pm_prepare<W><<<static_cast<unsigned>((fm + 255) / 256), 256, 0, stream>>>(
+        d_traj, pm, w, fm, s.grid_rows, s.grid_cols, beta, 1.0 / std::cyl_bessel_i(0.0, beta), d->require_nyquist);
+  }
+  const size_t half_warps = static_cast<size_t>(s.frames) * s.lists_per_frame;
+  for (uint32_t it = 0; it < iterations; ++it) {
+    {
+      LaunchScope scope("k_pm_grid", stream);
+      k_pm_grid<W><<<static_cast<unsigned>((half_warps * 16 + 255) / 256), 256, 0, stream>>>(
+          reinterpret_cast<const uint32_t*>(ws + l.offsets), reinterpret_cast<const uint32_t*>(ws + l.entries), pm,
+          w, grid, s.frames, s.samples, s.grid_rows, s.grid_cols, s.nchunks, s.lists_per_frame,
+          s.entries_per_frame);
+    }
+    LaunchScope scope("k_pm_update", stream);
+    k_pm_update<W><<<static_cast<unsigned>((fm + 255) / 256), 256, 0, stream>>>(
+        pm, grid, w, it + 1 == iterations ? d_dcf : nullptr, fm, s.samples, s.grid_rows, s.grid_cols);
   }
   return check_launch();
 }
@@ -1422,4 +1625,36 @@ extern "C" ksj_gpu_status ksj_gpu_gridding_tune(const ksj_gpu_gridding_desc* des
   }
   *tuning = best;
   return KSJ_GPU_OK;
+}
+
+extern "C" size_t ksj_gpu_pipe_menon_workspace_bytes(const ksj_gpu_gridding_desc* desc) {
+  Shape s{};
+  if (desc == nullptr || desc->kernel != KSJ_GPU_KERNEL_KAISER_BESSEL || make_shape(desc, nullptr, &s) != KSJ_GPU_OK)
+    return 0;
+  return make_pm_layout(s).total;
+}
+
+extern "C" ksj_gpu_status ksj_gpu_pipe_menon_dcf(const ksj_gpu_gridding_desc* desc, uint32_t iterations,
+                                                 const float* d_traj, float* d_dcf, void* d_workspace,
+                                                 size_t workspace_bytes, void* stream) {
+  if (desc == nullptr || desc->kernel != KSJ_GPU_KERNEL_KAISER_BESSEL || iterations == 0 || iterations > 1000)
+    return KSJ_GPU_ERROR_INVALID_ARGUMENT;
+  Shape s{};
+  const ksj_gpu_status st = make_shape(desc, nullptr, &s);
+  if (st != KSJ_GPU_OK) return st;
+  if (d_traj == nullptr || d_dcf == nullptr || (reinterpret_cast<uintptr_t>(d_traj) & 7u) != 0 ||
+      (reinterpret_cast<uintptr_t>(d_dcf) & 3u) != 0)
+    return KSJ_GPU_ERROR_INVALID_ARGUMENT;
+  const PmLayout l = make_pm_layout(s);
+  if (d_workspace == nullptr || (reinterpret_cast<uintptr_t>(d_workspace) & 255u) != 0 || workspace_bytes < l.total)
+    return KSJ_GPU_ERROR_WORKSPACE;
+  unsigned char* ws = static_cast<unsigned char*>(d_workspace);
+  cudaStream_t cs = static_cast<cudaStream_t>(stream);
+  switch (s.width) {
+    case 2: return launch_pipe_menon<2>(s, l, desc, iterations, d_traj, d_dcf, ws, cs);
+    case 4: return launch_pipe_menon<4>(s, l, desc, iterations, d_traj, d_dcf, ws, cs);
+    case 6: return launch_pipe_menon<6>(s, l, desc, iterations, d_traj, d_dcf, ws, cs);
+    case 8: return launch_pipe_menon<8>(s, l, desc, iterations, d_traj, d_dcf, ws, cs);
+    default: return KSJ_GPU_ERROR_UNSUPPORTED;
+  }
 }

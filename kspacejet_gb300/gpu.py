@@ -74,6 +74,10 @@ def lib() -> ctypes.CDLL:
         L.ksj_gpu_direct_adjoint.restype = ctypes.c_int32
         L.ksj_gpu_direct_adjoint.argtypes = [u32, u32, ctypes.c_double, ctypes.c_double, u32, u32, vp, vp, vp, vp,
                                              sz, vp]
+        L.ksj_gpu_pipe_menon_workspace_bytes.restype = sz
+        L.ksj_gpu_pipe_menon_workspace_bytes.argtypes = [ctypes.POINTER(GriddingDesc)]
+        L.ksj_gpu_pipe_menon_dcf.restype = ctypes.c_int32
+        L.ksj_gpu_pipe_menon_dcf.argtypes = [ctypes.POINTER(GriddingDesc), u32, vp, vp, vp, sz, vp]
         L.ksj_gpu_rss_coil_last.restype = ctypes.c_int32
         L.ksj_gpu_rss_coil_last.argtypes = [u64, u32, vp, vp, vp]
         L.ksj_gpu_launch_count.restype = u64
@@ -222,6 +226,25 @@ def kb_gridding(image: int, grid: int, channels: int, samples: int, frames: int 
     return Gridding(image=(image, image), channels=channels, samples=samples, frames=frames,
                     kernel=KERNEL_KAISER_BESSEL, grid=(grid, grid), width=width, dcf=dcf, output=output,
                     sample_format=sample_format, require_nyquist=False)
+
+
+def pipe_menon_dcf(traj: torch.Tensor, image: int, grid: int, width: int = 4, iterations: int = 10,
+                   stream=None) -> torch.Tensor:
+    """Pipe-Menon density weights for Kaiser-Bessel gridding on a square grid:
+    traj [F, M, 2] (or [M, 2]) float32 on the GPU -> float32 [F, M] (or [M])."""
+    t = traj if traj.dim() == 3 else traj.unsqueeze(0)
+    f, m, _ = t.shape
+    g = kb_gridding(image, grid, 1, m, frames=f, width=width)
+    d = g.desc()
+    L = lib()
+    n = int(L.ksj_gpu_pipe_menon_workspace_bytes(ctypes.byref(d)))
+    if n == 0:
+        raise GpuError(1, "pipe_menon_workspace_bytes")
+    ws = torch.empty(n, dtype=torch.uint8, device=t.device)
+    out = torch.empty((f, m), dtype=torch.float32, device=t.device)
+    _check(L.ksj_gpu_pipe_menon_dcf(ctypes.byref(d), iterations, t.contiguous().data_ptr(), out.data_ptr(),
+                                    ws.data_ptr(), ws.numel(), _stream(stream)), "pipe_menon_dcf")
+    return out if traj.dim() == 3 else out[0]
 
 
 def direct_adjoint(kspace: torch.Tensor, traj: torch.Tensor, rows: int, cols: int,

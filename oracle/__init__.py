@@ -200,6 +200,19 @@ class Oracle(_Base):
         return out
 
 
+    def pipe_menon_dcf(self, traj: np.ndarray, grid_rows: int, grid_cols: int, width: int = 4,
+                       beta: float | None = None, sigma: float = 2.0, iterations: int = 10) -> np.ndarray:
+        """Pipe-Menon density compensation, grid-based, double precision (one frame)."""
+        traj = np.ascontiguousarray(traj, dtype=np.float32).reshape(-1, 2)
+        if beta is None:
+            beta = self.kb_beta(width, sigma)
+        out = np.zeros(traj.shape[0], dtype=np.float64)
+        fn = self._fn("pipe_menon_dcf2_f64", ctypes.c_int, [_i64, _i64, ctypes.c_int, _dbl, _ptr, _i64, ctypes.c_int, _ptr])
+        if fn(grid_rows, grid_cols, width, beta, _p(traj), traj.shape[0], iterations, _p(out)) != 0:
+            raise OracleError("Pipe-Menon rejected its configuration")
+        return out
+
+
 class Reference(_Base):
     """The reference's own numerics compiled from its sources (``oracle/_ref``).
     Raises ``FileNotFoundError`` where the reference was not built."""

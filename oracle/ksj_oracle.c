@@ -569,3 +569,66 @@ KSJO_EXPORT int ksjo_kb_gridding2_adjoint_f64(int64_t g, int64_t n, int width, d
   free(grid);
   return 0;
 }
+
+/* ------------------------------------------------------------ Pipe-Menon */
+
+/* Iterative density compensation (Pipe & Menon, MRM 41:179-186, 1999) in
+ * its grid-based form, with the Kaiser-Bessel kernel phi of the gridding path
+ * (ksjo_kb_kernel, taps floor(u) - W/2 + 1 ... floor(u) + W/2, u = k g / 2 pi,
+ * indices mod g).  No reference counterpart.  Starting from w = 1 every
+ * iteration
+ *   grids w:          c[cell] = sum_s w_s * (phi_r * phi_c), samples in index order,
+ *   interpolates back: d_s = sum over the sample's taps (row-major) of c[cell] * (phi_r * phi_c),
+ *   and updates        w_s = w_s / d_s (0 when d_s is not positive).
+ * Double precision throughout.  traj [m][2] float32; out [m] double. */
+KSJO_EXPORT int ksjo_pipe_menon_dcf2_f64(int64_t g_rows, int64_t g_cols, int width, double beta, const float* traj,
+                                         int64_t m, int iterations, double* out) {
+  if (width < 2 || width > 16 || g_rows < width || g_cols < width) return -1;
+  double* grid = (double*)malloc((size_t)(g_rows * g_cols) * sizeof(double));
+  int64_t* r0 = (int64_t*)malloc((size_t)m * sizeof(int64_t));
+  int64_t* c0 = (int64_t*)malloc((size_t)m * sizeof(int64_t));
+  double* wr = (double*)malloc((size_t)(m * width) * sizeof(double));
+  double* wc = (double*)malloc((size_t)(m * width) * sizeof(double));
+  if (!grid || !r0 || !c0 || !wr || !wc) return -2;
+  for (int64_t s = 0; s < m; ++s) {
+    const double ur = (double)traj[2 * s] * (double)g_rows / (2.0 * kPiD);
+    const double uc = (double)traj[2 * s + 1] * (double)g_cols / (2.0 * kPiD);
+    const int64_t tr = (int64_t)floor(ur) - width / 2 + 1;
+    const int64_t tc = (int64_t)floor(uc) - width / 2 + 1;
+    r0[s] = ((tr % g_rows) + g_rows) % g_rows;
+    c0[s] = ((tc % g_cols) + g_cols) % g_cols;
+    for (int j = 0; j < width; ++j) {
+      wr[s * width + j] = ksjo_kb_kernel((double)(tr + j) - ur, width, beta);
+      wc[s * width + j] = ksjo_kb_kernel((double)(tc + j) - uc, width, beta);
+    }
+    out[s] = 1.0;
+  }
+  for (int it = 0; it < iterations; ++it) {
+    memset(grid, 0, (size_t)(g_rows * g_cols) * sizeof(double));
+    for (int64_t s = 0; s < m; ++s)
+      for (int a = 0; a < width; ++a) {
+        const int64_t rr = (r0[s] + a) % g_rows;
+        for (int b = 0; b < width; ++b) {
+          const int64_t cc = (c0[s] + b) % g_cols;
+          grid[rr * g_cols + cc] += out[s] * (wr[s * width + a] * wc[s * width + b]);
+        }
+      }
+    for (int64_t s = 0; s < m; ++s) {
+      double d = 0.0;
+      for (int a = 0; a < width; ++a) {
+        const int64_t rr = (r0[s] + a) % g_rows;
+        for (int b = 0; b < width; ++b) {
+          const int64_t cc = (c0[s] + b) % g_cols;
+          d += grid[rr * g_cols + cc] * (wr[s * width + a] * wc[s * width + b]);
+        }
+      }
+      out[s] = d > 0.0 ? out[s] / d : 0.0;
+    }
+  }
+  free(grid);
+  free(r0);
+  free(c0);
+  free(wr);
+  free(wc);
+  return 0;
+}

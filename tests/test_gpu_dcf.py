@@ -1,0 +1,55 @@
+"""Pipe-Menon density weights (ksj_gpu_pipe_menon_dcf) against the FP64
+oracle restatement of the same grid-based iteration.  Both run in double
+precision with the same tap sets and per-cell summation order; they differ
+only in the Bessel I0 evaluation and in fused multiply-adds (~1e-15); the
+output is float32, so the bound is 1e-7 relative L2 (float32 rounding of the
+weights alone is ~3e-8)."""
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-7  # rel L2 of the float32 weights against the FP64 oracle
+
+
+def _traj(readout, spokes, frames):
+    from kspacejet_gb300 import synth
+
+    return np.stack([synth.golden_angle_radial(readout, spokes, first_spoke=spokes * f) for f in range(frames)])
+
+
+@pytest.mark.parametrize("image,grid,width,iterations", [(32, 64, 4, 10), (48, 96, 6, 10), (32, 64, 4, 1),
+                                                         (64, 96, 4, 5)])
+def test_pipe_menon_matches_fp64_oracle(native, cuda, orc, image, grid, width, iterations):
+    import torch
+    from kspacejet_gb300 import gpu
+
+    tr = _traj(grid, 30, 2)
+    got = gpu.pipe_menon_dcf(torch.from_numpy(tr).to(cuda), image, grid, width=width,
+                             iterations=iterations).cpu().numpy()
+    for f in range(tr.shape[0]):
+        want = orc.pipe_menon_dcf(tr[f], grid, grid, width, sigma=grid / image, iterations=iterations)
+        err = oracle.rel_l2(got[f].astype(np.float64), want)
+        print(f"Pipe-Menon {grid} W={width} it={iterations} frame {f}: rel L2 {err:.2e}")
+        assert err <= TOL
+        assert np.all(got[f] > 0)
+
+
+def test_pipe_menon_is_deterministic_and_converges(native, cuda, orc):
+    """Byte-identical repeats; and at the benchmark's frame shape (34 spokes x
+    384, grid 384) the relative change of the weights between iterations falls
+    (the fixed point w * (phi conv phi) = 1 is approached)."""
+    import torch
+    from kspacejet_gb300 import gpu
+
+    tr = torch.from_numpy(_traj(384, 34, 2)).to(cuda)
+    a = gpu.pipe_menon_dcf(tr, 192, 384, iterations=10).cpu().numpy()
+    b = gpu.pipe_menon_dcf(tr, 192, 384, iterations=10).cpu().numpy()
+    assert a.tobytes() == b.tobytes()
+    steps = [gpu.pipe_menon_dcf(tr, 192, 384, iterations=i).cpu().numpy().astype(np.float64) for i in (2, 3, 9, 10)]
+    early = np.linalg.norm(steps[1] - steps[0]) / np.linalg.norm(steps[0])
+    late = np.linalg.norm(steps[3] - steps[2]) / np.linalg.norm(steps[2])
+    print(f"relative change: iteration 2->3 {early:.2e}, 9->10 {late:.2e}")
+    assert late < early
