@@ -215,6 +215,47 @@ KSJ_GPU_API ksj_gpu_status ksj_gpu_direct_adjoint_static(uint32_t rows, uint32_t
 KSJ_GPU_API ksj_gpu_status ksj_gpu_rss_coil_last(uint64_t pixels, uint32_t channels, const void* d_coil_last,
                                                  float* d_out, void* stream);
 
+/* Adaptive coil combination (Walsh, Gmitro, Marcellin, MRM 2000; no
+ * counterpart in the reference): for every pixel, the coil covariance of the
+ * window x window neighbourhood (clipped at the image border), its dominant
+ * eigenvector v by `iterations` power iterations from the pixel's own coil
+ * vector, phase-referenced so that v[0] is real and non-negative; out = v^H x.
+ * d_coil_last complex64 [rows][cols][channels] -> d_out complex64 [rows][cols].
+ * channels 1..8 (apply after coil compression); window odd, <= 9. */
+KSJ_GPU_API ksj_gpu_status ksj_gpu_walsh_combine(uint32_t rows, uint32_t cols, uint32_t channels, uint32_t window,
+                                                 uint32_t iterations, const void* d_coil_last, void* d_out,
+                                                 void* stream);
+
+/* ----------------------------------------------------- coil compression */
+
+/* Coil covariance R = (1/M) X X^H of channel-major k-space X complex64
+ * [channels][samples] (coil_compression_basis_estimate.cpp:207-227; the 1/M
+ * is applied in float as there): d_cov complex64 [channels][channels], full
+ * Hermitian.  On the tensor cores: each element of [Re X; Im X] is split into
+ * bf16 hi + lo and hi hi^T + lo hi^T + (lo hi^T)^T is accumulated in FP32
+ * (tcgen05), stated bound 1e-4 relative Frobenius error against FP64.
+ * channels <= 32.  Workspace: ksj_gpu_coil_covariance_workspace_bytes. */
+KSJ_GPU_API size_t ksj_gpu_coil_covariance_workspace_bytes(uint32_t channels, uint32_t samples);
+KSJ_GPU_API ksj_gpu_status ksj_gpu_coil_covariance(uint32_t channels, uint32_t samples, const void* d_kspace,
+                                                   void* d_cov, void* d_workspace, size_t workspace_bytes,
+                                                   void* stream);
+
+/* Host: the compression basis of a covariance (host complex64 [C][C], lower
+ * triangle read and mirrored as the reference does): conj of the eigenvectors
+ * of the largest `virtual_channels` eigenvalues, largest first
+ * (coil_compression_basis_estimate.cpp:228-239), by double-precision cyclic
+ * Jacobi.  basis: host complex64 [virtual_channels][channels]; eigenvalues
+ * (optional, host float [channels]) in decreasing order. */
+KSJ_GPU_API ksj_gpu_status ksj_coil_compression_basis(uint32_t channels, uint32_t virtual_channels,
+                                                      const void* covariance, void* basis, float* eigenvalues);
+
+/* Y = B X (noncartesian_coil_compress.cpp:143-148): d_basis complex64
+ * [virtual][channels], d_kspace complex64 [channels][samples] ->
+ * d_out complex64 [virtual][samples].  channels <= 32, virtual <= 16. */
+KSJ_GPU_API ksj_gpu_status ksj_gpu_coil_compress(uint32_t channels, uint32_t virtual_channels, uint32_t samples,
+                                                 const void* d_basis, const void* d_kspace, void* d_out,
+                                                 void* stream);
+
 /* --------------------------------------------------------------- context */
 
 /* A device, a non-blocking stream and a grow-only device workspace; used by

@@ -78,6 +78,16 @@ def lib() -> ctypes.CDLL:
         L.ksj_gpu_pipe_menon_workspace_bytes.argtypes = [ctypes.POINTER(GriddingDesc)]
         L.ksj_gpu_pipe_menon_dcf.restype = ctypes.c_int32
         L.ksj_gpu_pipe_menon_dcf.argtypes = [ctypes.POINTER(GriddingDesc), u32, vp, vp, vp, sz, vp]
+        L.ksj_gpu_walsh_combine.restype = ctypes.c_int32
+        L.ksj_gpu_walsh_combine.argtypes = [u32, u32, u32, u32, u32, vp, vp, vp]
+        L.ksj_gpu_coil_covariance_workspace_bytes.restype = sz
+        L.ksj_gpu_coil_covariance_workspace_bytes.argtypes = [u32, u32]
+        L.ksj_gpu_coil_covariance.restype = ctypes.c_int32
+        L.ksj_gpu_coil_covariance.argtypes = [u32, u32, vp, vp, vp, sz, vp]
+        L.ksj_coil_compression_basis.restype = ctypes.c_int32
+        L.ksj_coil_compression_basis.argtypes = [u32, u32, vp, vp, vp]
+        L.ksj_gpu_coil_compress.restype = ctypes.c_int32
+        L.ksj_gpu_coil_compress.argtypes = [u32, u32, u32, vp, vp, vp, vp]
         L.ksj_gpu_rss_coil_last.restype = ctypes.c_int32
         L.ksj_gpu_rss_coil_last.argtypes = [u64, u32, vp, vp, vp]
         L.ksj_gpu_launch_count.restype = u64
@@ -257,6 +267,52 @@ def direct_adjoint(kspace: torch.Tensor, traj: torch.Tensor, rows: int, cols: in
     out = torch.empty((rows, cols, c), dtype=torch.complex64, device=kspace.device)
     _check(L.ksj_gpu_direct_adjoint(rows, cols, ro, co, c, m, kspace.data_ptr(), traj.data_ptr(), out.data_ptr(),
                                     ws.data_ptr(), ws.numel(), _stream(stream)), "direct_adjoint")
+    return out
+
+
+def walsh_combine(coil_last: torch.Tensor, window: int = 7, iterations: int = 24, stream=None) -> torch.Tensor:
+    """[rows, cols, C] complex64 (C <= 8) -> [rows, cols] complex64 adaptive combination."""
+    rows, cols, c = coil_last.shape
+    out = torch.empty((rows, cols), dtype=torch.complex64, device=coil_last.device)
+    _check(lib().ksj_gpu_walsh_combine(rows, cols, c, window, iterations, coil_last.contiguous().data_ptr(),
+                                       out.data_ptr(), _stream(stream)), "walsh_combine")
+    return out
+
+
+def coil_covariance(kspace: torch.Tensor, stream=None) -> torch.Tensor:
+    """[C, M] complex64 channel-major k-space -> [C, C] complex64 covariance (tensor cores)."""
+    c, m = kspace.shape
+    L = lib()
+    n = int(L.ksj_gpu_coil_covariance_workspace_bytes(c, m))
+    if n == 0:
+        raise GpuError(1, "coil_covariance_workspace_bytes")
+    ws = torch.empty(n, dtype=torch.uint8, device=kspace.device)
+    out = torch.empty((c, c), dtype=torch.complex64, device=kspace.device)
+    _check(L.ksj_gpu_coil_covariance(c, m, kspace.contiguous().data_ptr(), out.data_ptr(), ws.data_ptr(), ws.numel(),
+                                     _stream(stream)), "coil_covariance")
+    return out
+
+
+def compression_basis(covariance, virtual_channels: int):
+    """Host: covariance [C, C] complex64 (numpy) -> (basis [V, C] complex64, eigenvalues [C] float32)."""
+    import numpy as np
+
+    cov = np.ascontiguousarray(covariance, dtype=np.complex64)
+    c = cov.shape[0]
+    basis = np.zeros((virtual_channels, c), dtype=np.complex64)
+    ev = np.zeros(c, dtype=np.float32)
+    _check(lib().ksj_coil_compression_basis(c, virtual_channels, cov.ctypes.data, basis.ctypes.data, ev.ctypes.data),
+           "compression_basis")
+    return basis, ev
+
+
+def coil_compress(basis: torch.Tensor, kspace: torch.Tensor, stream=None) -> torch.Tensor:
+    """basis [V, C], kspace [C, M] complex64 on the GPU -> [V, M]."""
+    v, c = basis.shape
+    _, m = kspace.shape
+    out = torch.empty((v, m), dtype=torch.complex64, device=kspace.device)
+    _check(lib().ksj_gpu_coil_compress(c, v, m, basis.contiguous().data_ptr(), kspace.contiguous().data_ptr(),
+                                       out.data_ptr(), _stream(stream)), "coil_compress")
     return out
 
 

@@ -213,6 +213,17 @@ class Oracle(_Base):
         return out
 
 
+    def coil_covariance(self, x: np.ndarray, double: bool = False) -> np.ndarray:
+        """Coil covariance of channel-major k-space x complex64 [C, M]: the
+        reference's float arithmetic, or double precision."""
+        x = np.ascontiguousarray(x, dtype=np.complex64)
+        c, m = x.shape
+        out = np.zeros((c, c), dtype=np.complex128 if double else np.complex64)
+        name = "coil_covariance_f64" if double else "coil_covariance_f32"
+        self._fn(name, None, [_i64, _i64, _ptr, _ptr])(c, m, _p(x), _p(out))
+        return out
+
+
 class Reference(_Base):
     """The reference's own numerics compiled from its sources (``oracle/_ref``).
     Raises ``FileNotFoundError`` where the reference was not built."""

@@ -632,3 +632,51 @@ KSJO_EXPORT int ksjo_pipe_menon_dcf2_f64(int64_t g_rows, int64_t g_cols, int wid
   free(wc);
   return 0;
 }
+
+/* ------------------------------------------------------ coil covariance */
+
+/* coil_compression_basis_estimate.cpp:207-227 in float, operation for
+ * operation: lower triangle sum over samples of x_row * conj(x_col) (complex
+ * float multiply and add, rounded separately), times the float reciprocal of
+ * the sample count, upper triangle the conjugate.  x complex64 [c][m];
+ * out complex64 [c][c]. */
+KSJO_EXPORT void ksjo_coil_covariance_f32(int64_t c, int64_t m, const float* x_in, float* out_raw) {
+  const cf32* x = (const cf32*)x_in;
+  cf32* out = (cf32*)out_raw;
+  for (int64_t i = 0; i < c * c; ++i) out[i] = (cf32){0.0f, 0.0f};
+  for (int64_t s = 0; s < m; ++s)
+    for (int64_t r = 0; r < c; ++r)
+      for (int64_t col = 0; col <= r; ++col) {
+        const cf32 a = x[r * m + s], b = x[col * m + s];
+        const cf32 p = cmul_f(a, (cf32){b.re, -b.im});
+        out[r * c + col] = (cf32){out[r * c + col].re + p.re, out[r * c + col].im + p.im};
+      }
+  const float inv = 1.0f / (float)m;
+  for (int64_t r = 0; r < c; ++r) {
+    out[r * c + r] = (cf32){out[r * c + r].re * inv, out[r * c + r].im * inv};
+    for (int64_t col = 0; col < r; ++col) {
+      out[r * c + col] = (cf32){out[r * c + col].re * inv, out[r * c + col].im * inv};
+      out[col * c + r] = (cf32){out[r * c + col].re, -out[r * c + col].im};
+    }
+  }
+}
+
+/* The same covariance in double precision (the accuracy reference). */
+KSJO_EXPORT void ksjo_coil_covariance_f64(int64_t c, int64_t m, const float* x_in, double* out_raw) {
+  const cf32* x = (const cf32*)x_in;
+  cf64* out = (cf64*)out_raw;
+  for (int64_t i = 0; i < c * c; ++i) out[i] = (cf64){0.0, 0.0};
+  for (int64_t s = 0; s < m; ++s)
+    for (int64_t r = 0; r < c; ++r)
+      for (int64_t col = 0; col <= r; ++col) {
+        const double ar = x[r * m + s].re, ai = x[r * m + s].im, br = x[col * m + s].re, bi = x[col * m + s].im;
+        out[r * c + col].re += ar * br + ai * bi;
+        out[r * c + col].im += ai * br - ar * bi;
+      }
+  for (int64_t r = 0; r < c; ++r)
+    for (int64_t col = 0; col <= r; ++col) {
+      out[r * c + col].re /= (double)m;
+      out[r * c + col].im /= (double)m;
+      out[col * c + r] = (cf64){out[r * c + col].re, -out[r * c + col].im};
+    }
+}
