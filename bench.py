@@ -535,6 +535,108 @@ def run_serve(args) -> dict:
     return out
 
 
+# ------------------------------------------------ the other hot-path rows
+
+def _time_gpu(fn, warmup: int, steps: int) -> float:
+    """Mean ms per call of fn() over `steps` calls after `warmup`, CUDA events."""
+    import torch
+
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def run_rows(args) -> list[dict]:
+    """One JSON line per remaining hot-path row, on the shapes of the
+    configurations that use it (synthetic data of those shapes)."""
+    import torch
+    from kspacejet_gb300 import gpu, synth
+
+    dev = torch.device("cuda", 0)
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    bf16 = peaks.get("bf16_tflops", 1900.0)
+    w, s = max(args.warmup, 3), args.steps
+    lines = []
+
+    # Pipe-Menon density weights: the batched workload's trajectories (96 x 34 x 384, grid 384, W=4)
+    traj = np.stack([synth.golden_angle_radial(READOUT, SPOKES, first_spoke=SPOKES * f) for f in range(FRAMES)])
+    t = torch.from_numpy(traj).to(dev)
+    ms = _time_gpu(lambda: gpu.pipe_menon_dcf(t, IMAGE, GRID, width=WIDTH, iterations=10), w, s)
+    m = traj.shape[0] * traj.shape[1]
+    lines.append({"metric": "Pipe-Menon weights: sample-iterations/s", "value": m * 10 / (ms / 1e3),
+                  "unit": "sample-iterations/s", "ms_per_call": ms, "dtype": "f64",
+                  "config": {"workload": f"{FRAMES} frames x {SPOKES} spokes x {READOUT}, grid {GRID}, KB W={WIDTH}, "
+                                         "10 iterations", "samples": m}})
+
+    # coil covariance and compression: config 4 shape, 512 readout x 805 spokes, 32 -> 8 channels
+    mm = 512 * 805
+    rng = np.random.default_rng(3)
+    x = torch.from_numpy((rng.standard_normal((32, mm)) + 1j * rng.standard_normal((32, mm))).astype(np.complex64)).to(dev)
+    ws = torch.empty(gpu.lib().ksj_gpu_coil_covariance_workspace_bytes(32, mm), dtype=torch.uint8, device=dev)
+    cov = torch.empty((32, 32), dtype=torch.complex64, device=dev)
+    L = gpu.lib()
+
+    def covariance():
+        gpu._check(L.ksj_gpu_coil_covariance(32, mm, x.data_ptr(), cov.data_ptr(), ws.data_ptr(), ws.numel(),
+                                             torch.cuda.current_stream().cuda_stream), "coil_covariance")
+
+    gpu.timing_reset()
+    gpu.timing_enable(True)
+    ms = _time_gpu(covariance, w, s)
+    kern = {n: (c, t_) for n, c, t_ in gpu.timing_read()}
+    gpu.timing_enable(False)
+    mma_ms = kern["k_cov_mma"][1] / kern["k_cov_mma"][0]
+    kpad = (mm + 63) // 64 * 64
+    tensor_flops = 2.0 * 128 * 64 * kpad  # one M=128 N=64 contraction over the padded samples
+    lines.append({"metric": "coil covariance (tcgen05 split-BF16): samples/s", "value": mm / (ms / 1e3),
+                  "unit": "samples/s", "ms_per_call": ms, "dtype": "bf16 x3 split, f32 accumulate",
+                  "config": {"workload": "32 coils x 512 x 805 samples (complex64)"},
+                  "kernels_ms": {k: round(v[1] / v[0], 4) for k, v in kern.items()},
+                  "roofline": {"bound": "tensor", "kernel": "k_cov_mma",
+                               "achieved": round(tensor_flops / (mma_ms / 1e3) / 1e12, 2),
+                               "peak": bf16, "unit": "TFLOP/s", "frac": round(tensor_flops / (mma_ms / 1e3) / 1e12 / bf16, 4),
+                               "note": "the contraction is HBM-bound: 128 x 64 outputs per 64-sample tile"},
+                  "hbm": {"bytes": 3 * 32 * mm * 8, "GBps": round(3 * 32 * mm * 8 / (ms / 1e3) / 1e9, 1),
+                          "frac": round(3 * 32 * mm * 8 / (ms / 1e3) / 1e9 / hbm, 4)}})
+    basis, _ = gpu.compression_basis(cov.cpu().numpy(), 8)
+    bd = torch.from_numpy(basis).to(dev)
+    y = torch.empty((8, mm), dtype=torch.complex64, device=dev)
+
+    def compress():
+        gpu._check(L.ksj_gpu_coil_compress(32, 8, mm, bd.data_ptr(), x.data_ptr(), y.data_ptr(),
+                                           torch.cuda.current_stream().cuda_stream), "coil_compress")
+
+    ms = _time_gpu(compress, w, s)
+    byts = (32 + 8) * mm * 8
+    lines.append({"metric": "coil compression 32->8: samples/s", "value": mm / (ms / 1e3), "unit": "samples/s",
+                  "ms_per_call": ms, "dtype": "f32",
+                  "roofline": {"bound": "hbm", "achieved": round(byts / (ms / 1e3) / 1e9, 1), "peak": hbm,
+                               "unit": "GB/s", "frac": round(byts / (ms / 1e3) / 1e9 / hbm, 4)}})
+
+    # Walsh 7x7 on the compressed 8-coil image (256 x 256), and RSS of 32 coils
+    img = torch.from_numpy((rng.standard_normal((256, 256, 8)) + 1j * rng.standard_normal((256, 256, 8))).astype(np.complex64)).to(dev)
+    ms = _time_gpu(lambda: gpu.walsh_combine(img, window=7, iterations=24), w, s)
+    lines.append({"metric": "Walsh 7x7 combine: pixels/s", "value": 256 * 256 / (ms / 1e3), "unit": "pixels/s",
+                  "ms_per_call": ms, "dtype": "f32", "config": {"workload": "256 x 256 x 8 coils, 24 power iterations"}})
+    img32 = torch.from_numpy((rng.standard_normal((256, 256, 32)) + 1j * rng.standard_normal((256, 256, 32))).astype(np.complex64)).to(dev)
+    ms = _time_gpu(lambda: gpu.rss_coil_last(img32), w, s)
+    byts = 256 * 256 * (32 * 8 + 4)
+    lines.append({"metric": "RSS combine: pixels/s", "value": 256 * 256 / (ms / 1e3), "unit": "pixels/s",
+                  "ms_per_call": ms, "dtype": "f32",
+                  "roofline": {"bound": "hbm", "achieved": round(byts / (ms / 1e3) / 1e9, 1), "peak": hbm,
+                               "unit": "GB/s", "frac": round(byts / (ms / 1e3) / 1e9 / hbm, 4)}})
+    return lines
+
+
 def main() -> int:
     global FRAMES
     ap = argparse.ArgumentParser()
@@ -545,6 +647,7 @@ def main() -> int:
     ap.add_argument("--frames", type=int, default=FRAMES,
                     help="frames per call (default: the 96-frame workload; fewer only for small profiling cases)")
     ap.add_argument("--serve", action="store_true", help="served-stream benchmark (separate JSON line)")
+    ap.add_argument("--rows", action="store_true", help="the other hot-path rows (one JSON line each)")
     ap.add_argument("--serve-requests", type=int, default=160)
     ap.add_argument("--serve-slots", type=int, default=4)
     ap.add_argument("--serve-cap-gib", type=int, default=24)
@@ -552,6 +655,13 @@ def main() -> int:
     FRAMES = args.frames
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
+    if args.rows:
+        import kspacejet_gb300
+
+        kspacejet_gb300.build()
+        for line in run_rows(args):
+            print(json.dumps(line))
+        return 0
     if args.serve:
         import kspacejet_gb300
 

@@ -182,7 +182,7 @@ extern "C" ksj_gpu_status ksj_gpu_walsh_combine(uint32_t rows, uint32_t cols, ui
 //                 one thread issues tcgen05.mma M=128 (the whole operand), N=64 (its hi rows, the same
 //                 shared memory), K=16; the 128 x 64 FP32 accumulator lives in tensor memory and is
 //                 read out once by the four warps
-//   k_cov_reduce  sums the blocks' accumulators in block order and forms R (deterministic)
+//   k_cov_sum / k_cov_form  sum the blocks' accumulators in block order and form R (deterministic)
 
 namespace ksj_gpu {
 namespace {
@@ -370,24 +370,27 @@ __global__ void __launch_bounds__(kCovThreads) k_cov_mma(const __grid_constant__
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;" ::"r"(tmem) : "memory");
 }
 
-// One thread per covariance element (i, j): G = sum over blocks of
-// hi hi^T + lo hi^T + (lo hi^T)^T, then R = G terms times 1/M (in float, as
-// the reference scales its sums).
-__global__ void __launch_bounds__(256) k_cov_reduce(const float* partials, int blocks, int channels, float inv_m,
-                                                    float2* cov) {
+// Sum of the blocks' accumulators, one thread per accumulator element (the
+// blocks' copies of an element are 32 KiB apart: coalesced across threads),
+// in block order.
+__global__ void __launch_bounds__(256) k_cov_sum(const float* partials, int blocks, float* sum) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= kCovRows * 64) return;
+  float s = 0.0f;
+#pragma unroll 8
+  for (int b = 0; b < blocks; ++b) s += partials[static_cast<size_t>(b) * kCovRows * 64 + e];
+  sum[e] = s;
+}
+
+// One thread per covariance element: G = hi hi^T + lo hi^T + (lo hi^T)^T from
+// the summed accumulator, then R times 1/M (in float, as the reference scales
+// its sums).  The lower triangle is computed and the upper mirrored
+// (conjugate), as the reference stores it, so R is Hermitian bit for bit.
+__global__ void __launch_bounds__(256) k_cov_form(const float* d, int channels, float inv_m, float2* cov) {
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= channels * channels) return;
   const int i = idx / channels, j = idx - (idx / channels) * channels;
-  auto g = [&](int r, int c) {
-    float s = 0.0f;
-    for (int b = 0; b < blocks; ++b) {
-      const float* p = partials + static_cast<size_t>(b) * kCovRows * 64;
-      s += p[r * 64 + c] + p[(64 + r) * 64 + c] + p[(64 + c) * 64 + r];
-    }
-    return s;
-  };
-  // the lower triangle is computed and the upper mirrored (conjugate), as the
-  // reference stores it, so the result is Hermitian bit for bit
+  auto g = [&](int r, int c) { return d[r * 64 + c] + d[(64 + r) * 64 + c] + d[(64 + c) * 64 + r]; };
   const int r = i >= j ? i : j, c = i >= j ? j : i;
   const float re = g(r, c) + g(32 + r, 32 + c);
   const float im = r == c ? 0.0f : g(32 + r, c) - g(r, 32 + c);
@@ -411,7 +414,7 @@ EncodeTiled2Fn cov_encode() {
 }
 
 struct CovLayout {
-  size_t flags, operand, partials, total;
+  size_t flags, operand, partials, sum, total;
   int kpad, ktiles, blocks;
 };
 
@@ -429,6 +432,7 @@ CovLayout cov_layout(uint32_t samples) {
   l.flags = take(16);
   l.operand = take(static_cast<size_t>(kCovRows) * l.kpad * 2);
   l.partials = take(static_cast<size_t>(l.blocks) * kCovRows * 64 * sizeof(float));
+  l.sum = take(static_cast<size_t>(kCovRows) * 64 * sizeof(float));
   l.total = off;
   return l;
 }
@@ -485,11 +489,16 @@ extern "C" ksj_gpu_status ksj_gpu_coil_covariance(uint32_t channels, uint32_t sa
     LaunchScope scope("k_cov_mma", cs);
     k_cov_mma<<<l.blocks, kCovThreads, smem, cs>>>(map, args);
   }
+  float* sum = reinterpret_cast<float*>(ws + l.sum);
+  {
+    LaunchScope scope("k_cov_sum", cs);
+    k_cov_sum<<<kCovRows * 64 / 256, 256, 0, cs>>>(partials, l.blocks, sum);
+  }
   {
     const int n = static_cast<int>(channels * channels);
-    LaunchScope scope("k_cov_reduce", cs);
-    k_cov_reduce<<<(n + 255) / 256, 256, 0, cs>>>(partials, l.blocks, static_cast<int>(channels),
-                                                  1.0f / static_cast<float>(samples), static_cast<float2*>(d_cov));
+    LaunchScope scope("k_cov_form", cs);
+    k_cov_form<<<(n + 255) / 256, 256, 0, cs>>>(sum, static_cast<int>(channels), 1.0f / static_cast<float>(samples),
+                                                static_cast<float2*>(d_cov));
   }
   return check_launch();
 }

@@ -141,18 +141,35 @@ __global__ void __launch_bounds__(kDirectPixels) k_direct_adjoint(const float2* 
 // out[p] = sqrt(sum_c re^2 + im^2), a float sum in channel order with every
 // product and sum rounded separately: the order and rounding points of
 // squared_norm_across + sqrt (reductions.hpp:972-982), so equal inputs give
-// bit-identical outputs.
-__global__ void __launch_bounds__(256) k_rss(const float2* __restrict__ in, float* out, uint64_t pixels,
-                                             int channels) {
-  const uint64_t p = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (p >= pixels) return;
-  const float2* v = in + p * channels;
+// bit-identical outputs.  A warp takes 32 consecutive pixels and stages up to
+// 32 of their coils at a time in shared memory with coalesced loads (lanes
+// read consecutive coils of one pixel); then lane p adds its pixel's staged
+// coils in order.
+constexpr int kRssWarps = 8;
+__global__ void __launch_bounds__(32 * kRssWarps) k_rss(const float2* __restrict__ in, float* out, uint64_t pixels,
+                                                        int channels) {
+  __shared__ float2 tile[kRssWarps][32][33];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint64_t p0 = (static_cast<uint64_t>(blockIdx.x) * kRssWarps + warp) * 32;
+  if (p0 >= pixels) return;
+  const int np = pixels - p0 < 32 ? static_cast<int>(pixels - p0) : 32;
   float total = 0.0f;
-  for (int c = 0; c < channels; ++c) {
-    const float2 x = __ldg(v + c);
-    total = __fadd_rn(total, __fadd_rn(__fmul_rn(x.x, x.x), __fmul_rn(x.y, x.y)));
+  for (int c0 = 0; c0 < channels; c0 += 32) {
+    const int cw = min(32, channels - c0);
+    for (int i = lane; i < np * cw; i += 32) {
+      const int q = i / cw, c = i - q * cw;
+      tile[warp][q][c] = __ldg(in + (p0 + q) * channels + c0 + c);
+    }
+    __syncwarp();
+    if (lane < np) {
+      for (int c = 0; c < cw; ++c) {
+        const float2 x = tile[warp][lane][c];
+        total = __fadd_rn(total, __fadd_rn(__fmul_rn(x.x, x.x), __fmul_rn(x.y, x.y)));
+      }
+    }
+    __syncwarp();
   }
-  out[p] = __fsqrt_rn(total);
+  if (lane < np) out[p0 + lane] = __fsqrt_rn(total);
 }
 
 }  // namespace
@@ -204,8 +221,9 @@ extern "C" ksj_gpu_status ksj_gpu_rss_coil_last(uint64_t pixels, uint32_t channe
     return KSJ_GPU_ERROR_INVALID_ARGUMENT;
   cudaStream_t cs = static_cast<cudaStream_t>(stream);
   LaunchScope scope("k_rss", cs);
-  k_rss<<<static_cast<unsigned>((pixels + 255) / 256), 256, 0, cs>>>(static_cast<const float2*>(d_coil_last), d_out,
-                                                                     pixels, static_cast<int>(channels));
+  const uint64_t per_block = 32 * kRssWarps;
+  k_rss<<<static_cast<unsigned>((pixels + per_block - 1) / per_block), 32 * kRssWarps, 0, cs>>>(
+      static_cast<const float2*>(d_coil_last), d_out, pixels, static_cast<int>(channels));
   return check_launch();
 }
 
