@@ -149,6 +149,37 @@ KSJ_GPU_API ksj_gpu_status ksj_gpu_gridding_tune(const ksj_gpu_gridding_desc* de
                                                  void* d_workspace, size_t workspace_bytes, void* stream,
                                                  ksj_gpu_gridding_tuning* tuning);
 
+/* ------------------------------------------------------ 3-D gridding */
+
+/* 3-D Kaiser-Bessel adjoint gridding on a cube (no counterpart in the
+ * reference, which is 2-D only): image n^3, grid g^3 (g = 2^a 3^b <= 512,
+ * g >= n), origin (n-1)/2 on every axis, taps, weights, crop and
+ * deapodisation as the 2-D Kaiser-Bessel path along each axis. */
+typedef struct ksj_gpu_gridding3_desc {
+  uint32_t struct_size;
+  uint32_t image;          /* n */
+  uint32_t grid;           /* g */
+  uint32_t kernel_width;   /* even, 2..8 */
+  double kb_beta;          /* 0: Beatty et al. for sigma = g / n */
+  uint32_t channels;
+  uint32_t samples;
+  uint32_t dcf_mode;       /* NONE, ANALYTIC_RAMP (|k|^2, 3-D radial), EXTERNAL */
+  uint32_t output;         /* KSJ_GPU_OUTPUT_RSS (float [n][n][n]) or COIL_LAST (complex [n][n][n][C]) */
+  uint32_t sample_format;  /* KSJ_GPU_SAMPLES_CF32 or _BF16 */
+  uint32_t reserved0;
+} ksj_gpu_gridding3_desc;
+
+/* Workspace bytes for `desc` (0 on a bad desc). */
+KSJ_GPU_API size_t ksj_gpu_gridding3_workspace_bytes(const ksj_gpu_gridding3_desc* desc);
+
+/*   d_kspace [channel][sample] samples; d_traj [sample][3] float32 (k_z, k_y, k_x)
+ *   radians per voxel; d_dcf [sample] for KSJ_GPU_DCF_EXTERNAL.  The tuning
+ *   knobs are those of the 2-D call (a z-plane is one frame). */
+KSJ_GPU_API ksj_gpu_status ksj_gpu_gridding3_adjoint(const ksj_gpu_gridding3_desc* desc,
+                                                     const ksj_gpu_gridding_tuning* tuning, const void* d_kspace,
+                                                     const float* d_traj, const float* d_dcf, void* d_out,
+                                                     void* d_workspace, size_t workspace_bytes, void* stream);
+
 /* ------------------------------------------------- Pipe-Menon density weights */
 
 /* Iterative density compensation (Pipe and Menon, MRM 41:179-186, 1999; no

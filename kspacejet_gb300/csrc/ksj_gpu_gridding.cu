@@ -72,6 +72,17 @@ struct alignas(16) SampleRecord {
   float wc[W];
 };
 
+// Per sample record of the 3-D path: first tap plane/row/column (wrapped),
+// dcf * phase, and the W tap weights along z, y and x.
+template <int W>
+struct alignas(16) SampleRecord3 {
+  int z0, r0, c0, pad;
+  float2 scale;
+  float wz[W];
+  float wr[W];
+  float wc[W];
+};
+
 // k_rows stages, per warp, the list entries of its current batch in shared
 // memory: {c0, sample, scale} and the W column weights times the row weight,
 // in 16-byte vectors read back as warp-wide broadcasts.
@@ -324,6 +335,11 @@ __global__ void k_tables(float2* tw_rows, int grid_rows, float2* tw_cols, int gr
   if (i < out_cols) inv_dc[i] = inv_psi(i, out_cols, grid_cols);
 }
 
+__global__ void __launch_bounds__(256) k_fill(float* p, int n, float v) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) p[i] = v;
+}
+
 struct PrepareArgs {
   const float* traj;
   const float* dcf;
@@ -529,22 +545,9 @@ __device__ __forceinline__ void warp_sort(uint32_t* buf, int n, int lane) {
 // column); bit 8 marks a one-chunk row that sees both ends of a wrap, whose
 // taps are wrapped one by one.
 template <int W>
-__device__ __forceinline__ void expand_entry(const SampleRecord<W>* recs, uint32_t sidx, int row, int col_lo,
-                                             int col_hi, int grid_rows, int grid_cols, float4* out) {
-  constexpr int kRV = static_cast<int>(sizeof(SampleRecord<W>) / 16);
+__device__ __forceinline__ void expand_taps(uint32_t sidx, int c0, float sre, float sim, float wrow, const float* wc,
+                                            int col_lo, int col_hi, int grid_cols, float4* out) {
   constexpr int kMV = meta_vecs(W);
-  float4 q[kRV];
-  const float4* rp = reinterpret_cast<const float4*>(recs + sidx);
-#pragma unroll
-  for (int v = 0; v < kRV; ++v) q[v] = __ldg(rp + v);
-  const float* w = reinterpret_cast<const float*>(q);
-  int ta = row - __float_as_int(w[0]);
-  if (ta < 0) ta += grid_rows;
-  float wr = 0.0f;
-#pragma unroll
-  for (int j = 0; j < W; ++j)
-    if (j == ta) wr = w[4 + j];
-  const int c0 = __float_as_int(w[1]);
   const int cb0 = c0 >= col_hi ? c0 - grid_cols : c0;
   uint32_t in_chunk = 0, straight = 0;
 #pragma unroll
@@ -556,17 +559,66 @@ __device__ __forceinline__ void expand_entry(const SampleRecord<W>* recs, uint32
   }
   const int word0 = in_chunk == straight ? ((cb0 * 512) | static_cast<int>(in_chunk))
                                          : ((c0 * 512) | 256 | static_cast<int>(in_chunk));
-  out[0] = make_float4(__int_as_float(word0), __uint_as_float(sidx), w[2], w[3]);
+  out[0] = make_float4(__int_as_float(word0), __uint_as_float(sidx), sre, sim);
 #pragma unroll
   for (int v = 1; v < kMV; ++v) {
     float t4[4];
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       const int j = 4 * (v - 1) + u;
-      t4[u] = j < W ? wr * w[4 + W + j] : 0.0f;
+      t4[u] = j < W ? wrow * wc[j] : 0.0f;
     }
     out[v] = make_float4(t4[0], t4[1], t4[2], t4[3]);
   }
+}
+
+// One list entry as k_rows consumes it (meta_vecs(W) 16-byte vectors):
+//   v0 = {tap word, sample index, scale.re, scale.im}, v1.. = the W column
+//   weights times this row's weight (zero padded).
+// The tap word holds the mask of taps that land in the list's column chunk
+// (bits 0-7) and the column of tap 0 as seen from the chunk (bits 9 up, one
+// row-length lower when the taps reaching the chunk wrapped past the last
+// column); bit 8 marks a one-chunk row that sees both ends of a wrap, whose
+// taps are wrapped one by one.
+template <int W>
+__device__ __forceinline__ void expand_entry(const SampleRecord<W>* recs, uint32_t sidx, int row, int col_lo,
+                                             int col_hi, int grid_rows, int grid_cols, float4* out) {
+  constexpr int kRV = static_cast<int>(sizeof(SampleRecord<W>) / 16);
+  float4 q[kRV];
+  const float4* rp = reinterpret_cast<const float4*>(recs + sidx);
+#pragma unroll
+  for (int v = 0; v < kRV; ++v) q[v] = __ldg(rp + v);
+  const float* w = reinterpret_cast<const float*>(q);
+  int ta = row - __float_as_int(w[0]);
+  if (ta < 0) ta += grid_rows;
+  float wr = 0.0f;
+#pragma unroll
+  for (int j = 0; j < W; ++j)
+    if (j == ta) wr = w[4 + j];
+  expand_taps<W>(sidx, __float_as_int(w[1]), w[2], w[3], wr, w + 4 + W, col_lo, col_hi, grid_cols, out);
+}
+
+// The 3-D form: the list's plane and row weights folded together.
+template <int W>
+__device__ __forceinline__ void expand_entry3(const SampleRecord3<W>* recs, uint32_t sidx, int plane, int row,
+                                              int col_lo, int col_hi, int grid, float4* out) {
+  constexpr int kRV = static_cast<int>(sizeof(SampleRecord3<W>) / 16);
+  float4 q[kRV];
+  const float4* rp = reinterpret_cast<const float4*>(recs + sidx);
+#pragma unroll
+  for (int v = 0; v < kRV; ++v) q[v] = __ldg(rp + v);
+  const float* w = reinterpret_cast<const float*>(q);
+  int tz = plane - __float_as_int(w[0]);
+  if (tz < 0) tz += grid;
+  int ta = row - __float_as_int(w[1]);
+  if (ta < 0) ta += grid;
+  float wz = 0.0f, wr = 0.0f;
+#pragma unroll
+  for (int j = 0; j < W; ++j) {
+    if (j == tz) wz = w[6 + j];
+    if (j == ta) wr = w[6 + W + j];
+  }
+  expand_taps<W>(sidx, __float_as_int(w[2]), w[4], w[5], wr * wz, w + 6 + 2 * W, col_lo, col_hi, grid, out);
 }
 
 struct SortArgs {
@@ -575,7 +627,8 @@ struct SortArgs {
   const unsigned char* records;
   float4* expanded;
   int frames, samples, lists_per_frame, nchunks, grid_rows, grid_cols, capacity;
-  size_t entries_per_frame;
+  size_t entries_per_frame;  // 0 when the offsets are absolute (3-D: one entry array for all planes)
+  int dim3;                  // 3-D: frames are grid planes and the records are per sample (SampleRecord3)
 };
 
 // Per list (one warp): sort the sample indices, then write every entry in
@@ -613,8 +666,18 @@ __global__ void __launch_bounds__(256) k_sort(SortArgs a) {
   const int row = l / a.nchunks;
   const int col_lo = (l - row * a.nchunks) * kChunk;
   const int col_hi = min(col_lo + kChunk, a.grid_cols);
-  const SampleRecord<W>* recs = reinterpret_cast<const SampleRecord<W>*>(a.records) + static_cast<size_t>(f) * a.samples;
   float4* out = a.expanded + (static_cast<size_t>(f) * a.entries_per_frame + begin) * kMV;
+  if (a.dim3) {
+    const SampleRecord3<W>* recs = reinterpret_cast<const SampleRecord3<W>*>(a.records);
+    for (int i = lane; i < n; i += 32) {
+      float4 e[kMV];
+      expand_entry3<W>(recs, sorted[i], f, row, col_lo, col_hi, a.grid_cols, e);
+#pragma unroll
+      for (int v = 0; v < kMV; ++v) out[static_cast<size_t>(i) * kMV + v] = e[v];
+    }
+    return;
+  }
+  const SampleRecord<W>* recs = reinterpret_cast<const SampleRecord<W>*>(a.records) + static_cast<size_t>(f) * a.samples;
   for (int i = lane; i < n; i += 32) {
     float4 e[kMV];
     expand_entry<W>(recs, sorted[i], row, col_lo, col_hi, a.grid_rows, a.grid_cols, e);
@@ -665,6 +728,7 @@ __global__ void __launch_bounds__(256) k_samples_coil_last(const void* in_raw, v
 struct RowsArgs {
   int frame0;             // first frame of this pass
   const void* samples_t;  // [frame][sample][channel]
+  size_t sample_frame_stride;  // elements between frames of samples_t (0: one sample set for all frames)
   const uint32_t* offsets;
   const float4* expanded;  // sorted list entries, expanded (meta_vecs(W) vectors each)
   const float2* tw_cols;
@@ -781,7 +845,7 @@ __global__ void __launch_bounds__(kThreads, kBlocks) k_rows(RowsArgs a) {
       const int my_coil = part * cpart + lane % cpp;  // coil index within the group
       const int coil_global = cgi * cg + my_coil;
       const bool coil_ok = (lane % cpp) < cpart && coil_global < a.channels;
-      const size_t sample_base = static_cast<size_t>(f) * a.samples * a.channels + (coil_ok ? coil_global : 0);
+      const size_t sample_base = static_cast<size_t>(f) * a.sample_frame_stride + (coil_ok ? coil_global : 0);
       for (int base = 0; base < n; base += kBatch) {
         const int cnt = min(kBatch, n - base);
         if (lane < cnt) {
@@ -881,6 +945,7 @@ struct ColsArgs {
   int column_block, col_group, groups;  // tile: column_block columns x col_group coils; groups tiles per block
   int box_rows, boxes;                  // TMA boxes of box_rows rows cover one tile
   uint32_t output;                      // RSS or COIL_LAST (COIL_MAJOR goes through COIL_LAST + transpose)
+  int out_pitch;                        // COIL_LAST: elements between pixels of the output (>= channels)
   DifPlan plan;
 };
 
@@ -975,7 +1040,7 @@ __global__ void __launch_bounds__(kColsThreads) k_cols(const __grid_constant__ C
         e->x = __fadd_rn(__fmul_rn(x.x, x.x), __fmul_rn(x.y, x.y));
       } else {
         float2* o = static_cast<float2*>(a.out);
-        o[((static_cast<size_t>(fg) * a.out_rows + pr) * a.out_cols + col0 + lcol) * a.channels + gc] = x;
+        o[((static_cast<size_t>(fg) * a.out_rows + pr) * a.out_cols + col0 + lcol) * a.out_pitch + gc] = x;
       }
     }
     if (a.output == KSJ_GPU_OUTPUT_RSS) {
@@ -1136,6 +1201,7 @@ ksj_gpu_status build_lists(const Shape& s, const ksj_gpu_gridding_desc* d, const
     sa.grid_cols = s.grid_cols;
     sa.capacity = s.list_capacity;
     sa.entries_per_frame = s.entries_per_frame;
+    sa.dim3 = 0;
     LaunchScope scope("k_sort", stream);
     k_sort<W><<<static_cast<unsigned>((nl + 7) / 8), 256, smem, stream>>>(sa);
   }
@@ -1183,6 +1249,7 @@ ksj_gpu_status launch_all(const Shape& s, const Layout& l, const ksj_gpu_griddin
   }
   RowsArgs r{};
   r.samples_t = ws + l.samples_t;
+  r.sample_frame_stride = static_cast<size_t>(s.samples) * s.channels;
   r.offsets = offsets;
   r.expanded = reinterpret_cast<const float4*>(ws + l.expanded);
   r.tw_cols = tw_cols;
@@ -1232,6 +1299,7 @@ ksj_gpu_status launch_all(const Shape& s, const Layout& l, const ksj_gpu_griddin
   const bool coil_major = d->output == KSJ_GPU_OUTPUT_COIL_MAJOR;
   c.output = d->output == KSJ_GPU_OUTPUT_RSS ? KSJ_GPU_OUTPUT_RSS : KSJ_GPU_OUTPUT_COIL_LAST;
   c.out = coil_major ? static_cast<void*>(ws + l.coil_last) : d_out;
+  c.out_pitch = s.channels;
   CUtensorMap map;
   if (!make_inter_map(s, inter, &map, &c.box_rows, &c.boxes)) return KSJ_GPU_ERROR_CUDA;
   const size_t cols_smem = cols_smem_bytes(s);
@@ -1456,6 +1524,406 @@ ksj_gpu_status launch_pipe_menon(const Shape& s, const PmLayout& l, const ksj_gp
   return check_launch();
 }
 
+// ------------------------------------------------------------ 3-D gridding
+//
+// A g^3 grid is gridded as g z-planes of the 2-D row/column machinery: the
+// binning lists are (plane, row, 16-column chunk); an entry's row weight is
+// the sample's y weight times its z weight for that plane; every plane reads
+// the one coil-last sample array.  After the per-plane row and column passes
+// (y and x transformed, cropped, deapodised) the intermediate
+// [plane][pixel][coil] takes a third pass along z, which is the column pass
+// again with planes as rows and pixels as columns.
+
+struct Prepare3Args {
+  const float* traj;  // [M][3] (k_z, k_y, k_x)
+  const float* dcf;
+  uint32_t dcf_mode;
+  unsigned char* records;
+  uint32_t* counts;  // [plane][row * nchunks + chunk]
+  uint32_t* flags;
+  int samples, grid, nchunks, lists_per_plane;
+  float beta, two_over_w, inv_i0_beta, phase;
+};
+
+template <int W>
+__global__ void __launch_bounds__(256) k_prepare3(Prepare3Args a) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= a.samples) return;
+  const float kz = __ldg(a.traj + 3 * static_cast<size_t>(idx));
+  const float ky = __ldg(a.traj + 3 * static_cast<size_t>(idx) + 1);
+  const float kx = __ldg(a.traj + 3 * static_cast<size_t>(idx) + 2);
+  bool ok = isfinite(kz) && isfinite(ky) && isfinite(kx) && fabsf(kz) < 1.0e4f && fabsf(ky) < 1.0e4f &&
+            fabsf(kx) < 1.0e4f;
+  float w = 1.0f;
+  if (a.dcf_mode == KSJ_GPU_DCF_ANALYTIC_RAMP) {
+    w = fmaf(kz, kz, fmaf(ky, ky, kx * kx));  // 3-D radial density ~ 1 / |k|^2
+  } else if (a.dcf_mode == KSJ_GPU_DCF_EXTERNAL) {
+    w = __ldg(a.dcf + idx);
+    if (!(isfinite(w) && w >= 0.0f)) {
+      atomicOr(a.flags, KSJ_GPU_FLAG_BAD_DCF);
+      w = 0.0f;
+    }
+  }
+  SampleRecord3<W> rec;
+  rec.pad = 0;
+  if (!ok) {
+    atomicOr(a.flags, KSJ_GPU_FLAG_BAD_TRAJECTORY);
+    rec.z0 = rec.r0 = rec.c0 = 0;
+    rec.scale = make_float2(0.0f, 0.0f);
+#pragma unroll
+    for (int j = 0; j < W; ++j) rec.wz[j] = rec.wr[j] = rec.wc[j] = 0.0f;
+  } else {
+    const float gf = static_cast<float>(a.grid);
+    const dfloat uz = grid_coordinate(kz, gf), uy = grid_coordinate(ky, gf), ux = grid_coordinate(kx, gf);
+    float f;
+    const int sz = dfloor(uz, &f) - W / 2 + 1;
+    const int sy = dfloor(uy, &f) - W / 2 + 1;
+    const int sx = dfloor(ux, &f) - W / 2 + 1;
+    rec.z0 = wrap_index(sz, a.grid);
+    rec.r0 = wrap_index(sy, a.grid);
+    rec.c0 = wrap_index(sx, a.grid);
+#pragma unroll
+    for (int j = 0; j < W; ++j) {
+      rec.wz[j] = kb_weight(__fsub_rn(__fsub_rn(static_cast<float>(sz + j), uz.hi), uz.lo), a.two_over_w, a.beta,
+                            a.inv_i0_beta);
+      rec.wr[j] = kb_weight(__fsub_rn(__fsub_rn(static_cast<float>(sy + j), uy.hi), uy.lo), a.two_over_w, a.beta,
+                            a.inv_i0_beta);
+      rec.wc[j] = kb_weight(__fsub_rn(__fsub_rn(static_cast<float>(sx + j), ux.hi), ux.lo), a.two_over_w, a.beta,
+                            a.inv_i0_beta);
+    }
+    rec.scale = cscale(exp_i_dot3(kz, a.phase, ky, a.phase, kx, a.phase), w);
+  }
+  reinterpret_cast<SampleRecord3<W>*>(a.records)[idx] = rec;
+  int k0, k1;
+  list_chunks<W>(rec.c0, a.grid, &k0, &k1);
+#pragma unroll
+  for (int i = 0; i < W; ++i) {
+    int plane = rec.z0 + i;
+    if (plane >= a.grid) plane -= a.grid;
+    uint32_t* counts = a.counts + static_cast<size_t>(plane) * a.lists_per_plane;
+#pragma unroll
+    for (int j = 0; j < W; ++j) {
+      int row = rec.r0 + j;
+      if (row >= a.grid) row -= a.grid;
+      atomicAdd(counts + row * a.nchunks + k0, 1u);
+      if (k1 != k0) atomicAdd(counts + row * a.nchunks + k1, 1u);
+    }
+  }
+}
+
+// The per-plane scans leave offsets[p][lists] = the plane's total; turn them
+// into absolute positions in one entry array (one block: planes <= 512).
+__global__ void __launch_bounds__(512) k_plane_bases(uint32_t* offsets, int planes, int lists, uint32_t* bases) {
+  __shared__ uint32_t tot[512];
+  const int t = threadIdx.x;
+  tot[t] = t < planes ? offsets[static_cast<size_t>(t) * (lists + 1) + lists] : 0u;
+  __syncthreads();
+  if (t == 0) {
+    uint32_t run = 0;
+    for (int p = 0; p < planes; ++p) {
+      const uint32_t v = tot[p];
+      tot[p] = run;
+      run += v;
+    }
+  }
+  __syncthreads();
+  if (t < planes) bases[t] = tot[t];
+}
+
+__global__ void __launch_bounds__(256) k_offsets_add(uint32_t* offsets, int planes, int lists, const uint32_t* bases) {
+  const size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= static_cast<size_t>(planes) * (lists + 1)) return;
+  offsets[i] += bases[i / (lists + 1)];
+}
+
+template <int W>
+__global__ void __launch_bounds__(256) k_scatter3(const unsigned char* records, const uint32_t* offsets,
+                                                  uint32_t* cursor, uint32_t* entries, int samples, int grid,
+                                                  int nchunks, int lists_per_plane) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= samples) return;
+  const SampleRecord3<W>& rec = reinterpret_cast<const SampleRecord3<W>*>(records)[idx];
+  int k0, k1;
+  list_chunks<W>(rec.c0, grid, &k0, &k1);
+  for (int i = 0; i < W; ++i) {
+    int plane = rec.z0 + i;
+    if (plane >= grid) plane -= grid;
+    const uint32_t* off = offsets + static_cast<size_t>(plane) * (lists_per_plane + 1);
+    uint32_t* cur = cursor + static_cast<size_t>(plane) * lists_per_plane;
+    for (int j = 0; j < W; ++j) {
+      int row = rec.r0 + j;
+      if (row >= grid) row -= grid;
+      const int l0 = row * nchunks + k0;
+      entries[off[l0] + atomicAdd(cur + l0, 1u)] = static_cast<uint32_t>(idx);
+      if (k1 != k0) {
+        const int l1 = row * nchunks + k1;
+        entries[off[l1] + atomicAdd(cur + l1, 1u)] = static_cast<uint32_t>(idx);
+      }
+    }
+  }
+}
+
+struct Layout3 {
+  size_t flags, records, counts, cursor, offsets, bases, entries, expanded, samples_t, inter, inter2, tables, total;
+  size_t entries_total;
+};
+
+size_t record3_bytes(int width) {
+  switch (width) {
+    case 2: return sizeof(SampleRecord3<2>);
+    case 4: return sizeof(SampleRecord3<4>);
+    case 6: return sizeof(SampleRecord3<6>);
+    default: return sizeof(SampleRecord3<8>);
+  }
+}
+
+// s: the 2-D shape of one plane with frames = planes (see make_shape3).
+Layout3 make_layout3(const Shape& s, uint32_t sample_format) {
+  Layout3 l{};
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    const size_t at = off;
+    off = align_up(off + bytes, 256);
+    return at;
+  };
+  const size_t g = static_cast<size_t>(s.grid_rows), n = static_cast<size_t>(s.rows);
+  const size_t nl = g * s.lists_per_frame;
+  l.entries_total = static_cast<size_t>(s.samples) * s.width * s.width * 2;
+  l.flags = take(kFlagBytes);
+  l.records = take(static_cast<size_t>(s.samples) * record3_bytes(s.width));
+  l.counts = take(nl * 4);
+  l.cursor = take(nl * 4);
+  l.offsets = take((nl + g) * 4);
+  l.bases = take(g * 4);
+  l.entries = take(l.entries_total * 4);
+  l.expanded = take(l.entries_total * meta_vecs(s.width) * 16);
+  l.samples_t = take(static_cast<size_t>(s.samples) * s.channels * sample_bytes(sample_format));
+  l.inter = take(g * g * n * s.cpitch * sizeof(float2));
+  l.inter2 = take(g * n * n * s.cpitch * sizeof(float2));
+  // twiddles (rows, cols), deapodisation (rows, cols), DIF positions (rows, cols), ones for the pixel axis
+  l.tables = take(2 * g * sizeof(float2) + 2 * n * sizeof(float) + 2 * n * sizeof(int) + n * n * sizeof(float));
+  l.total = off;
+  return l;
+}
+
+ksj_gpu_status make_shape3(const ksj_gpu_gridding3_desc* d, const ksj_gpu_gridding_tuning* t, Shape* s) {
+  if (d == nullptr || d->struct_size < sizeof(ksj_gpu_gridding3_desc)) return KSJ_GPU_ERROR_INVALID_ARGUMENT;
+  if (d->output != KSJ_GPU_OUTPUT_RSS && d->output != KSJ_GPU_OUTPUT_COIL_LAST) return KSJ_GPU_ERROR_UNSUPPORTED;
+  if (d->image == 0 || d->grid == 0 || static_cast<uint64_t>(d->image) * d->image > (1u << 24))
+    return KSJ_GPU_ERROR_INVALID_ARGUMENT;
+  ksj_gpu_gridding_desc d2{};
+  d2.struct_size = sizeof(d2);
+  d2.kernel = KSJ_GPU_KERNEL_KAISER_BESSEL;
+  d2.image_rows = d2.image_cols = d->image;
+  d2.grid_rows = d2.grid_cols = d->grid;
+  d2.kernel_width = d->kernel_width;
+  d2.kb_beta = d->kb_beta;
+  d2.row_origin = d2.col_origin = (static_cast<double>(d->image) - 1.0) / 2.0;
+  d2.channels = d->channels;
+  d2.samples = d->samples;
+  d2.frames = d->grid;  // one frame per z-plane
+  d2.dcf_mode = d->dcf_mode;
+  d2.output = KSJ_GPU_OUTPUT_COIL_LAST;
+  d2.sample_format = d->sample_format;
+  const ksj_gpu_status st = make_shape(&d2, t, s);
+  if (st != KSJ_GPU_OK) return st;
+  s->entries_per_frame = 0;  // absolute offsets into one entry array
+  return KSJ_GPU_OK;
+}
+
+template <int W, uint32_t kFormat>
+ksj_gpu_status launch_all3(const Shape& s, const Layout3& l, const ksj_gpu_gridding3_desc* d, const void* d_kspace,
+                           const float* d_traj, const float* d_dcf, void* d_out, unsigned char* ws,
+                           cudaStream_t stream) {
+  const int g = s.grid_rows, n = s.rows;
+  uint32_t* flags = reinterpret_cast<uint32_t*>(ws + l.flags);
+  uint32_t* counts = reinterpret_cast<uint32_t*>(ws + l.counts);
+  uint32_t* cursor = reinterpret_cast<uint32_t*>(ws + l.cursor);
+  uint32_t* offsets = reinterpret_cast<uint32_t*>(ws + l.offsets);
+  uint32_t* entries = reinterpret_cast<uint32_t*>(ws + l.entries);
+  float2* inter = reinterpret_cast<float2*>(ws + l.inter);
+  float2* inter2 = reinterpret_cast<float2*>(ws + l.inter2);
+  float2* tw_rows = reinterpret_cast<float2*>(ws + l.tables);
+  float2* tw_cols = tw_rows + g;
+  float* inv_dr = reinterpret_cast<float*>(tw_cols + g);
+  float* inv_dc = inv_dr + n;
+  int* pos_rows = reinterpret_cast<int*>(inv_dc + n);
+  int* pos_cols = pos_rows + n;
+  float* ones = reinterpret_cast<float*>(pos_cols + n);
+  const size_t nl = static_cast<size_t>(g) * s.lists_per_frame;
+
+  if (cudaMemsetAsync(flags, 0, kFlagBytes, stream) != cudaSuccess) return KSJ_GPU_ERROR_CUDA;
+  if (cudaMemsetAsync(counts, 0, nl * 4, stream) != cudaSuccess) return KSJ_GPU_ERROR_CUDA;
+  if (cudaMemsetAsync(cursor, 0, nl * 4, stream) != cudaSuccess) return KSJ_GPU_ERROR_CUDA;
+  {
+    const int nt = std::max(g, n);
+    LaunchScope scope("k_tables", stream);
+    k_tables<<<(nt + 255) / 256, 256, 0, stream>>>(tw_rows, g, tw_cols, g, inv_dr, n, inv_dc, n, pos_rows, pos_cols,
+                                                   s.plan_rows, s.plan_cols, 1, s.width, s.beta,
+                                                   std::cyl_bessel_i(0.0, static_cast<double>(s.beta)));
+  }
+  {
+    LaunchScope scope("k_fill_ones", stream);
+    k_fill<<<(n * n + 255) / 256, 256, 0, stream>>>(ones, n * n, 1.0f);
+  }
+  {
+    Prepare3Args p{};
+    p.traj = d_traj;
+    p.dcf = d_dcf;
+    p.dcf_mode = d->dcf_mode;
+    p.records = ws + l.records;
+    p.counts = counts;
+    p.flags = flags;
+    p.samples = s.samples;
+    p.grid = g;
+    p.nchunks = s.nchunks;
+    p.lists_per_plane = s.lists_per_frame;
+    p.beta = s.beta;
+    p.two_over_w = 2.0f / static_cast<float>(s.width);
+    p.inv_i0_beta = s.inv_i0_beta;
+    p.phase = s.phase_row;
+    LaunchScope scope("k_prepare3", stream);
+    k_prepare3<W><<<(s.samples + 255) / 256, 256, 0, stream>>>(p);
+  }
+  {
+    LaunchScope scope("k_scan", stream);
+    k_scan<<<g, 1024, 0, stream>>>(counts, offsets, s.lists_per_frame);
+  }
+  {
+    uint32_t* bases = reinterpret_cast<uint32_t*>(ws + l.bases);
+    LaunchScope scope("k_plane_offsets", stream);
+    k_plane_bases<<<1, 512, 0, stream>>>(offsets, g, s.lists_per_frame, bases);
+    const size_t total = static_cast<size_t>(g) * (s.lists_per_frame + 1);
+    k_offsets_add<<<static_cast<unsigned>((total + 255) / 256), 256, 0, stream>>>(offsets, g, s.lists_per_frame,
+                                                                                bases);
+  }
+  {
+    LaunchScope scope("k_scatter3", stream);
+    k_scatter3<W><<<(s.samples + 255) / 256, 256, 0, stream>>>(ws + l.records, offsets, cursor, entries, s.samples, g,
+                                                               s.nchunks, s.lists_per_frame);
+  }
+  {
+    const size_t smem = static_cast<size_t>(8) * s.list_capacity * 4;
+    if (cudaFuncSetAttribute(k_sort<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)) !=
+        cudaSuccess)
+      return KSJ_GPU_ERROR_CUDA;
+    SortArgs sa{};
+    sa.offsets = offsets;
+    sa.entries = entries;
+    sa.records = ws + l.records;
+    sa.expanded = reinterpret_cast<float4*>(ws + l.expanded);
+    sa.frames = g;
+    sa.samples = s.samples;
+    sa.lists_per_frame = s.lists_per_frame;
+    sa.nchunks = s.nchunks;
+    sa.grid_rows = g;
+    sa.grid_cols = g;
+    sa.capacity = s.list_capacity;
+    sa.entries_per_frame = 0;
+    sa.dim3 = 1;
+    LaunchScope scope("k_sort", stream);
+    k_sort<W><<<static_cast<unsigned>((nl + 7) / 8), 256, smem, stream>>>(sa);
+  }
+  {
+    const dim3 tg((s.samples + 31) / 32, (s.channels + 31) / 32, 1);
+    LaunchScope scope("k_samples_coil_last", stream);
+    k_samples_coil_last<kFormat><<<tg, dim3(32, 8), 0, stream>>>(d_kspace, ws + l.samples_t, s.channels, s.samples,
+                                                                 flags);
+  }
+  // rows of every plane (x transformed, kept columns, coil-last)
+  RowsArgs r{};
+  r.samples_t = ws + l.samples_t;
+  r.sample_frame_stride = 0;
+  r.offsets = offsets;
+  r.expanded = reinterpret_cast<const float4*>(ws + l.expanded);
+  r.tw_cols = tw_cols;
+  r.pos_cols = pos_cols;
+  r.inter = inter;
+  r.flags = flags;
+  r.frames = g;
+  r.channels = s.channels;
+  r.samples = s.samples;
+  r.grid_rows = g;
+  r.grid_cols = g;
+  r.nchunks = s.nchunks;
+  r.lists_per_frame = s.lists_per_frame;
+  r.entries_per_frame = 0;
+  r.coil_group = s.coil_group;
+  r.coil_parts = s.coil_parts;
+  r.out_cols = n;
+  r.cpitch = s.cpitch;
+  r.plan = s.plan_cols;
+  const size_t rows_smem = rows_smem_bytes(s);
+  const int rows_threads = rows_threads_for(g);
+  const bool whole32 = s.coil_group == 32 && s.coil_parts == 1;
+  auto rows_kernel = (rows_threads <= 384 && s.rows_blocks == 2)
+                         ? (whole32 ? k_rows<W, kFormat, 384, 2, 32> : k_rows<W, kFormat, 384, 2, 0>)
+                         : (whole32 ? k_rows<W, kFormat, kMaxThreads, 1, 32> : k_rows<W, kFormat, kMaxThreads, 1, 0>);
+  if (cudaFuncSetAttribute(rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(rows_smem)) !=
+          cudaSuccess ||
+      cudaFuncSetAttribute(rows_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100) != cudaSuccess)
+    return KSJ_GPU_ERROR_CUDA;
+  const size_t cols_smem = cols_smem_bytes(s);
+  if (cudaFuncSetAttribute(k_cols, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(cols_smem)) !=
+          cudaSuccess ||
+      cudaFuncSetAttribute(k_cols, cudaFuncAttributePreferredSharedMemoryCarveout, 100) != cudaSuccess)
+    return KSJ_GPU_ERROR_CUDA;
+  // columns of every plane (y transformed, cropped, y/x deapodised): [plane][pixel][cpitch]
+  ColsArgs c{};
+  c.tw_rows = tw_rows;
+  c.inv_dr = inv_dr;
+  c.inv_dc = inv_dc;
+  c.pos_rows = pos_rows;
+  c.flags = flags;
+  c.frames = g;
+  c.channels = s.channels;
+  c.grid_rows = g;
+  c.out_rows = n;
+  c.out_cols = n;
+  c.kb = 1;
+  c.column_block = s.column_block;
+  c.col_group = s.col_group;
+  c.groups = s.cpitch / s.col_group;
+  c.plan = s.plan_rows;
+  c.output = KSJ_GPU_OUTPUT_COIL_LAST;
+  c.out = inter2;
+  c.out_pitch = s.cpitch;
+  CUtensorMap map;
+  if (!make_inter_map(s, inter, &map, &c.box_rows, &c.boxes)) return KSJ_GPU_ERROR_CUDA;
+  for (int f0 = 0; f0 < g; f0 += s.frames_per_pass) {
+    const int nf = std::min(s.frames_per_pass, g - f0);
+    r.frame0 = f0;
+    c.frame0 = f0;
+    {
+      LaunchScope scope("k_rows", stream);
+      rows_kernel<<<dim3(g, (s.channels + s.coil_group - 1) / s.coil_group, nf), rows_threads, rows_smem, stream>>>(r);
+    }
+    {
+      LaunchScope scope("k_cols", stream);
+      k_cols<<<dim3((n + s.column_block - 1) / s.column_block, nf), kColsThreads, cols_smem, stream>>>(map, c);
+    }
+  }
+  // z: the column pass over [plane][pixel][cpitch] with planes as rows and pixels as columns
+  Shape z = s;
+  z.frames = 1;
+  z.out_cols = n * n;
+  CUtensorMap zmap;
+  ColsArgs cz = c;
+  if (!make_inter_map(z, inter2, &zmap, &cz.box_rows, &cz.boxes)) return KSJ_GPU_ERROR_CUDA;
+  cz.frame0 = 0;
+  cz.frames = 1;
+  cz.out_cols = n * n;
+  cz.inv_dc = ones;
+  cz.output = d->output;
+  cz.out = d_out;
+  cz.out_pitch = s.channels;
+  {
+    LaunchScope scope("k_cols_z", stream);
+    k_cols<<<dim3((n * n + s.column_block - 1) / s.column_block, 1), kColsThreads, cols_smem, stream>>>(zmap, cz);
+  }
+  return check_launch();
+}
+
 template <int W>
 ksj_gpu_status dispatch_format(const Shape& s, const Layout& l, const ksj_gpu_gridding_desc* d, const void* k,
                                const float* t, const float* w, void* o, unsigned char* ws, cudaStream_t st) {
@@ -1655,6 +2123,42 @@ extern "C" ksj_gpu_status ksj_gpu_pipe_menon_dcf(const ksj_gpu_gridding_desc* de
     case 4: return launch_pipe_menon<4>(s, l, desc, iterations, d_traj, d_dcf, ws, cs);
     case 6: return launch_pipe_menon<6>(s, l, desc, iterations, d_traj, d_dcf, ws, cs);
     case 8: return launch_pipe_menon<8>(s, l, desc, iterations, d_traj, d_dcf, ws, cs);
+    default: return KSJ_GPU_ERROR_UNSUPPORTED;
+  }
+}
+
+extern "C" size_t ksj_gpu_gridding3_workspace_bytes(const ksj_gpu_gridding3_desc* desc) {
+  Shape s{};
+  if (make_shape3(desc, nullptr, &s) != KSJ_GPU_OK) return 0;
+  return make_layout3(s, desc->sample_format).total;
+}
+
+extern "C" ksj_gpu_status ksj_gpu_gridding3_adjoint(const ksj_gpu_gridding3_desc* desc,
+                                                    const ksj_gpu_gridding_tuning* tuning, const void* d_kspace,
+                                                    const float* d_traj, const float* d_dcf, void* d_out,
+                                                    void* d_workspace, size_t workspace_bytes, void* stream) {
+  Shape s{};
+  const ksj_gpu_status st = make_shape3(desc, tuning, &s);
+  if (st != KSJ_GPU_OK) return st;
+  if (d_kspace == nullptr || d_traj == nullptr || d_out == nullptr) return KSJ_GPU_ERROR_INVALID_ARGUMENT;
+  if (desc->dcf_mode == KSJ_GPU_DCF_EXTERNAL && d_dcf == nullptr) return KSJ_GPU_ERROR_INVALID_ARGUMENT;
+  const Layout3 l = make_layout3(s, desc->sample_format);
+  if (l.entries_total > 0xffffffffull) return KSJ_GPU_ERROR_UNSUPPORTED;
+  if (d_workspace == nullptr || (reinterpret_cast<uintptr_t>(d_workspace) & 255u) != 0 || workspace_bytes < l.total)
+    return KSJ_GPU_ERROR_WORKSPACE;
+  if ((reinterpret_cast<uintptr_t>(d_kspace) & (sample_bytes(desc->sample_format) - 1)) != 0 ||
+      (reinterpret_cast<uintptr_t>(d_traj) & 3u) != 0 || (reinterpret_cast<uintptr_t>(d_out) & 7u) != 0)
+    return KSJ_GPU_ERROR_INVALID_ARGUMENT;
+  unsigned char* ws = static_cast<unsigned char*>(d_workspace);
+  cudaStream_t cs = static_cast<cudaStream_t>(stream);
+  const bool bf16 = desc->sample_format == KSJ_GPU_SAMPLES_BF16;
+  switch (s.width) {
+#define KSJ_G3_CASE(W)                                                                                       \
+  case W:                                                                                                    \
+    return bf16 ? launch_all3<W, KSJ_GPU_SAMPLES_BF16>(s, l, desc, d_kspace, d_traj, d_dcf, d_out, ws, cs)     \
+                : launch_all3<W, KSJ_GPU_SAMPLES_CF32>(s, l, desc, d_kspace, d_traj, d_dcf, d_out, ws, cs);
+    KSJ_G3_CASE(2) KSJ_G3_CASE(4) KSJ_G3_CASE(6) KSJ_G3_CASE(8)
+#undef KSJ_G3_CASE
     default: return KSJ_GPU_ERROR_UNSUPPORTED;
   }
 }

@@ -138,6 +138,27 @@ __device__ __forceinline__ float2 exp_i_dot(float a1, float b1, float a2, float 
   return make_float2(cs, sn);
 }
 
+// exp(i (a1 b1 + a2 b2 + a3 b3)): the three-term form of exp_i_dot (sign +1).
+__device__ __forceinline__ float2 exp_i_dot3(float a1, float b1, float a2, float b2, float a3, float b3) {
+  const float p1 = __fmul_rn(a1, b1);
+  const float e1 = __fmaf_rn(a1, b1, -p1);
+  const float p2 = __fmul_rn(a2, b2);
+  const float e2 = __fmaf_rn(a2, b2, -p2);
+  const float p3 = __fmul_rn(a3, b3);
+  const float e3 = __fmaf_rn(a3, b3, -p3);
+  const dfloat s = two_sum(p1, p2);
+  const dfloat t = two_sum(s.hi, p3);
+  const float lo = __fadd_rn(__fadd_rn(s.lo, t.lo), __fadd_rn(__fadd_rn(e1, e2), e3));
+  const float n = rintf(__fmul_rn(t.hi, kInvTwoPi));
+  float r = __fmaf_rn(-n, kCw1, t.hi);
+  r = __fmaf_rn(-n, kCw2, r);
+  r = __fmaf_rn(-n, kCw3, r);
+  r = __fadd_rn(r, lo);
+  float sn, cs;
+  sincosf(r, &sn, &cs);
+  return make_float2(cs, sn);
+}
+
 // Kaiser-Bessel tap weight at offset d (grid cells), normalised to 1 at d = 0:
 // I0(beta sqrt(1 - (2d/W)^2)) / I0(beta).
 __device__ __forceinline__ float kb_weight(float d, float two_over_w, float beta, float inv_i0_beta) {

@@ -88,6 +88,11 @@ def lib() -> ctypes.CDLL:
         L.ksj_coil_compression_basis.argtypes = [u32, u32, vp, vp, vp]
         L.ksj_gpu_coil_compress.restype = ctypes.c_int32
         L.ksj_gpu_coil_compress.argtypes = [u32, u32, u32, vp, vp, vp, vp]
+        L.ksj_gpu_gridding3_workspace_bytes.restype = sz
+        L.ksj_gpu_gridding3_workspace_bytes.argtypes = [ctypes.POINTER(Gridding3Desc)]
+        L.ksj_gpu_gridding3_adjoint.restype = ctypes.c_int32
+        L.ksj_gpu_gridding3_adjoint.argtypes = [ctypes.POINTER(Gridding3Desc), ctypes.POINTER(GriddingTuning), vp, vp,
+                                                vp, vp, vp, sz, vp]
         L.ksj_gpu_rss_coil_last.restype = ctypes.c_int32
         L.ksj_gpu_rss_coil_last.argtypes = [u64, u32, vp, vp, vp]
         L.ksj_gpu_launch_count.restype = u64
@@ -228,6 +233,59 @@ class Gridding:
                                            workspace.data_ptr(), workspace.numel(), _stream(stream),
                                            ctypes.byref(t)), "gridding_tune")
         return t
+
+
+class Gridding3Desc(ctypes.Structure):
+    _fields_ = [("struct_size", ctypes.c_uint32), ("image", ctypes.c_uint32), ("grid", ctypes.c_uint32),
+                ("kernel_width", ctypes.c_uint32), ("kb_beta", ctypes.c_double), ("channels", ctypes.c_uint32),
+                ("samples", ctypes.c_uint32), ("dcf_mode", ctypes.c_uint32), ("output", ctypes.c_uint32),
+                ("sample_format", ctypes.c_uint32), ("reserved0", ctypes.c_uint32)]
+
+
+@dataclass
+class Gridding3:
+    """3-D Kaiser-Bessel adjoint gridding (see ``ksj_gpu_gridding3_desc``)."""
+
+    image: int
+    grid: int
+    channels: int
+    samples: int
+    width: int = 4
+    beta: float = 0.0
+    dcf: int = DCF_NONE
+    output: int = OUTPUT_RSS
+    sample_format: int = SAMPLES_CF32
+
+    def desc(self) -> Gridding3Desc:
+        return Gridding3Desc(ctypes.sizeof(Gridding3Desc), self.image, self.grid, self.width, self.beta,
+                             self.channels, self.samples, self.dcf, self.output, self.sample_format, 0)
+
+    def workspace_bytes(self) -> int:
+        d = self.desc()
+        n = lib().ksj_gpu_gridding3_workspace_bytes(ctypes.byref(d))
+        if n == 0:
+            raise GpuError(1, "gridding3_workspace_bytes")
+        return int(n)
+
+    def output_shape(self) -> tuple[int, ...]:
+        n = self.image
+        return (n, n, n) if self.output == OUTPUT_RSS else (n, n, n, self.channels)
+
+    def new_output(self, device="cuda") -> torch.Tensor:
+        dt = torch.float32 if self.output == OUTPUT_RSS else torch.complex64
+        return torch.empty(self.output_shape(), dtype=dt, device=device)
+
+    def new_workspace(self, device="cuda") -> torch.Tensor:
+        return torch.empty(self.workspace_bytes(), dtype=torch.uint8, device=device)
+
+    def run(self, kspace: torch.Tensor, traj: torch.Tensor, out: torch.Tensor, workspace: torch.Tensor,
+            dcf: torch.Tensor | None = None, tuning: GriddingTuning | None = None, stream=None) -> None:
+        d = self.desc()
+        st = lib().ksj_gpu_gridding3_adjoint(ctypes.byref(d), ctypes.byref(tuning) if tuning else None,
+                                             kspace.data_ptr(), traj.data_ptr(),
+                                             dcf.data_ptr() if dcf is not None else None, out.data_ptr(),
+                                             workspace.data_ptr(), workspace.numel(), _stream(stream))
+        _check(st, "gridding3_adjoint")
 
 
 def kb_gridding(image: int, grid: int, channels: int, samples: int, frames: int = 1, width: int = 4,

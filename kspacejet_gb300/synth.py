@@ -139,3 +139,16 @@ def dynamic_radial(frames: int, spokes: int, readout: int, channels: int, seed: 
         trajs.append(t)
         ksps.append(multicoil_kspace(t, image, channels, seed, snr_db, shift=shift, ellipses=ell))
     return np.stack(trajs), np.stack(ksps)
+
+
+def kooshball(readout: int, spokes: int) -> np.ndarray:
+    """[spokes * readout, 3] float32 (k_z, k_y, k_x) in radians per pixel: 3-D
+    radial spokes through the centre along Fibonacci-sphere directions
+    (z_i = 1 - (2i + 1) / spokes, azimuth i * pi (3 - sqrt 5))."""
+    i = np.arange(spokes, dtype=np.float64)
+    z = 1.0 - (2.0 * i + 1.0) / spokes
+    r = np.sqrt(np.maximum(0.0, 1.0 - z * z))
+    phi = i * math.pi * (3.0 - math.sqrt(5.0))
+    d = np.stack([z, r * np.sin(phi), r * np.cos(phi)], axis=-1)
+    k = (np.arange(readout, dtype=np.float64) - readout / 2.0) * (2.0 * math.pi / readout)
+    return (d[:, None, :] * k[None, :, None]).reshape(-1, 3).astype(np.float32)

@@ -213,6 +213,30 @@ class Oracle(_Base):
         return out
 
 
+    def kb_gridding3(self, grid: int, n: int, samples: np.ndarray, traj: np.ndarray, dcf: np.ndarray | None,
+                     width: int = 4, sigma: float | None = None, beta: float | None = None) -> np.ndarray:
+        """3-D Kaiser-Bessel gridding adjoint in double precision (one coil), origin (n-1)/2."""
+        samples = np.ascontiguousarray(samples, dtype=np.complex128)
+        traj = np.ascontiguousarray(traj, dtype=np.float64).reshape(-1, 3)
+        if beta is None:
+            beta = self.kb_beta(width, sigma if sigma is not None else grid / n)
+        d = None if dcf is None else np.ascontiguousarray(dcf, dtype=np.float64)
+        out = np.zeros((n, n, n), dtype=np.complex128)
+        fn = self._fn("kb_gridding3_adjoint_f64", ctypes.c_int,
+                      [_i64, _i64, ctypes.c_int, _dbl, _dbl, _ptr, _ptr, _ptr, _i64, _ptr])
+        if fn(grid, n, width, beta, (n - 1) / 2.0, _p(samples), _p(traj), None if d is None else _p(d),
+              samples.shape[0], _p(out)) != 0:
+            raise OracleError("3-D KB gridding rejected its configuration")
+        return out
+
+    def direct_adjoint3(self, n: int, samples: np.ndarray, traj: np.ndarray) -> np.ndarray:
+        samples = np.ascontiguousarray(samples, dtype=np.complex128)
+        traj = np.ascontiguousarray(traj, dtype=np.float64).reshape(-1, 3)
+        out = np.zeros((n, n, n), dtype=np.complex128)
+        self._fn("direct_nudft3_adjoint_f64", None, [_i64, _dbl, _ptr, _ptr, _i64, _ptr])(
+            n, (n - 1) / 2.0, _p(samples), _p(traj), samples.shape[0], _p(out))
+        return out
+
     def coil_covariance(self, x: np.ndarray, double: bool = False) -> np.ndarray:
         """Coil covariance of channel-major k-space x complex64 [C, M]: the
         reference's float arithmetic, or double precision."""

@@ -680,3 +680,103 @@ KSJO_EXPORT void ksjo_coil_covariance_f64(int64_t c, int64_t m, const float* x_i
       out[col * c + r] = (cf64){out[r * c + col].re, -out[r * c + col].im};
     }
 }
+
+/* ------------------------------------------------------- 3-D Kaiser-Bessel */
+
+/* The 2-D Kaiser-Bessel adjoint above extended to a cube (the CUDA 3-D path):
+ * grid g^3, image n^3, coordinates u = k g / 2 pi per axis (z, y, x order in
+ * the trajectory), taps floor(u) - W/2 + 1 ... floor(u) + W/2 mod g, weight
+ * phi_z phi_y phi_x, sample weight y * dcf * exp(i k . delta) with
+ * delta = n/2 - origin per axis, exact separable inverse DFT along x, y, z,
+ * crop q = p - n/2 and deapodisation 1 / (psi(q_z) psi(q_y) psi(q_x)).
+ * samples complex128 [m]; traj double [m][3]; image complex128 [n][n][n]. */
+KSJO_EXPORT int ksjo_kb_gridding3_adjoint_f64(int64_t g, int64_t n, int width, double beta, double origin,
+                                              const double* samples_in, const double* traj, const double* dcf,
+                                              int64_t m, double* image_out) {
+  if (g < n || g < width || (width % 2) != 0) return -1;
+  const cf64* samples = (const cf64*)samples_in;
+  cf64* image = (cf64*)image_out;
+  cf64* grid = (cf64*)calloc((size_t)(g * g * g), sizeof(cf64));
+  cf64* src = (cf64*)malloc((size_t)g * sizeof(cf64));
+  cf64* dst = (cf64*)malloc((size_t)g * sizeof(cf64));
+  if (!grid || !src || !dst) return -2;
+  const double delta = (double)(n / 2) - origin;
+  for (int64_t s = 0; s < m; ++s) {
+    double u[3], w[3][16];
+    int64_t t0[3];
+    double ph = 0.0;
+    for (int d = 0; d < 3; ++d) {
+      const double k = traj[3 * s + d];
+      u[d] = k * (double)g / (2.0 * kPiD);
+      ph += k * delta;
+      t0[d] = (int64_t)floor(u[d]) - width / 2 + 1;
+      for (int j = 0; j < width; ++j) w[d][j] = ksjo_kb_kernel((double)(t0[d] + j) - u[d], width, beta);
+    }
+    const cf64 e = {cos(ph), sin(ph)};
+    const cf64 v = cmul_d(cscale_d(samples[s], dcf ? dcf[s] : 1.0), e);
+    for (int a = 0; a < width; ++a) {
+      const int64_t zz = (((t0[0] + a) % g) + g) % g;
+      for (int b = 0; b < width; ++b) {
+        const int64_t yy = (((t0[1] + b) % g) + g) % g;
+        const double wzy = w[0][a] * w[1][b];
+        for (int c = 0; c < width; ++c) {
+          const int64_t xx = (((t0[2] + c) % g) + g) % g;
+          const int64_t at = (zz * g + yy) * g + xx;
+          grid[at] = cadd_d(grid[at], cscale_d(v, wzy * w[2][c]));
+        }
+      }
+    }
+  }
+  /* separable exact inverse DFT: x lines, then y lines, then z lines */
+  for (int axis = 0; axis < 3; ++axis) {
+    const int64_t stride = axis == 0 ? 1 : (axis == 1 ? g : g * g);
+    for (int64_t a = 0; a < g; ++a)
+      for (int64_t b = 0; b < g; ++b) {
+        int64_t base;
+        if (axis == 0) base = (a * g + b) * g;
+        else if (axis == 1) base = a * g * g + b;
+        else base = a * g + b;
+        for (int64_t i = 0; i < g; ++i) src[i] = grid[base + i * stride];
+        ksjo_exact_idft_f64((const double*)src, (double*)dst, g);
+        for (int64_t i = 0; i < g; ++i) grid[base + i * stride] = dst[i];
+      }
+  }
+  for (int64_t pz = 0; pz < n; ++pz) {
+    const int64_t qz = pz - n / 2;
+    const double az = ksjo_kb_deapod((double)qz, width, beta, g);
+    for (int64_t py = 0; py < n; ++py) {
+      const int64_t qy = py - n / 2;
+      const double ay = ksjo_kb_deapod((double)qy, width, beta, g);
+      for (int64_t px = 0; px < n; ++px) {
+        const int64_t qx = px - n / 2;
+        const double ax = ksjo_kb_deapod((double)qx, width, beta, g);
+        const cf64 x = grid[((((qz % g) + g) % g) * g + (((qy % g) + g) % g)) * g + (((qx % g) + g) % g)];
+        image[(pz * n + py) * n + px] = cscale_d(x, 1.0 / (az * ay * ax));
+      }
+    }
+  }
+  free(grid);
+  free(src);
+  free(dst);
+  return 0;
+}
+
+/* Exact 3-D adjoint NUDFT: img(z, y, x) = sum_s y_s exp(i k_s . (p - origin)),
+ * the 3-D extension of direct_nudft2_adjoint (eigen_nufft_direct_nudft.cpp:77-97);
+ * samples complex128 [m], traj double [m][3] (z, y, x), image complex128 [n][n][n]. */
+KSJO_EXPORT void ksjo_direct_nudft3_adjoint_f64(int64_t n, double origin, const double* samples_in,
+                                                const double* traj, int64_t m, double* image_out) {
+  const cf64* samples = (const cf64*)samples_in;
+  cf64* image = (cf64*)image_out;
+  for (int64_t p = 0; p < n * n * n; ++p) {
+    const double z = (double)(p / (n * n)) - origin, y = (double)((p / n) % n) - origin, x = (double)(p % n) - origin;
+    double re = 0.0, im = 0.0;
+    for (int64_t s = 0; s < m; ++s) {
+      const double ph = traj[3 * s] * z + traj[3 * s + 1] * y + traj[3 * s + 2] * x;
+      const double c = cos(ph), sn = sin(ph);
+      re += samples[s].re * c - samples[s].im * sn;
+      im += samples[s].re * sn + samples[s].im * c;
+    }
+    image[p] = (cf64){re, im};
+  }
+}
