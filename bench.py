@@ -622,6 +622,33 @@ def run_rows(args) -> list[dict]:
                   "roofline": {"bound": "hbm", "achieved": round(byts / (ms / 1e3) / 1e9, 1), "peak": hbm,
                                "unit": "GB/s", "frac": round(byts / (ms / 1e3) / 1e9 / hbm, 4)}})
 
+    # 3-D kooshball: 256 readout x `spokes3` Fibonacci spokes, 20 coils, grid 384^3 (sigma 1.5), KB W=4,
+    # |k|^2 density weights, RSS; complex64 and bf16 sample storage
+    if args.spokes3 > 0:
+        tr3 = torch.from_numpy(synth.kooshball(256, args.spokes3)).to(dev)
+        m3 = tr3.shape[0]
+        gen = torch.Generator(device=dev).manual_seed(5)
+        k3 = torch.randn((20, m3), dtype=torch.complex64, device=dev, generator=gen)
+        for fmt, name in ((gpu.SAMPLES_CF32, "complex64"), (gpu.SAMPLES_BF16, "bf16")):
+            g3 = gpu.Gridding3(image=256, grid=384, channels=20, samples=m3, width=4, dcf=gpu.DCF_ANALYTIC_RAMP,
+                               output=gpu.OUTPUT_RSS, sample_format=fmt)
+            kin = k3 if fmt == gpu.SAMPLES_CF32 else torch.stack([k3.real.to(torch.bfloat16),
+                                                                  k3.imag.to(torch.bfloat16)], dim=-1).contiguous()
+            ws3 = g3.new_workspace(dev)
+            o3 = g3.new_output(dev)
+            gpu.timing_reset()
+            gpu.timing_enable(True)
+            ms = _time_gpu(lambda: g3.run(kin, tr3, o3, ws3), 1, max(1, min(s, 3)))
+            kern = {n_: round(t_ / c_, 3) for n_, c_, t_ in gpu.timing_read()}
+            gpu.timing_enable(False)
+            lines.append({"metric": "3-D kooshball gridded samples/s", "value": 20 * m3 / (ms / 1e3),
+                          "unit": "samples/s", "ms_per_call": ms, "dtype": f"f32 ({name} sample storage)",
+                          "config": {"workload": f"256 x {args.spokes3} spokes kooshball, 20 coils, grid 384^3, "
+                                                 "KB W=4, sigma 1.5, |k|^2 DCF, RSS", "gridded_samples": 20 * m3,
+                                     "workspace_bytes": ws3.numel()},
+                          "kernels_ms": kern})
+            del ws3, o3
+
     # Walsh 7x7 on the compressed 8-coil image (256 x 256), and RSS of 32 coils
     img = torch.from_numpy((rng.standard_normal((256, 256, 8)) + 1j * rng.standard_normal((256, 256, 8))).astype(np.complex64)).to(dev)
     ms = _time_gpu(lambda: gpu.walsh_combine(img, window=7, iterations=24), w, s)
@@ -648,6 +675,7 @@ def main() -> int:
                     help="frames per call (default: the 96-frame workload; fewer only for small profiling cases)")
     ap.add_argument("--serve", action="store_true", help="served-stream benchmark (separate JSON line)")
     ap.add_argument("--rows", action="store_true", help="the other hot-path rows (one JSON line each)")
+    ap.add_argument("--spokes3", type=int, default=40000, help="--rows: spokes of the 3-D kooshball (0 skips it)")
     ap.add_argument("--serve-requests", type=int, default=160)
     ap.add_argument("--serve-slots", type=int, default=4)
     ap.add_argument("--serve-cap-gib", type=int, default=24)

@@ -118,7 +118,8 @@ struct Shape {
 };
 
 struct Layout {
-  size_t flags, records, counts, cursor, offsets, entries, expanded, samples_t, inter, coil_last, tables, total;
+  size_t flags, records, counts, cursor, offsets, entries, expanded, long_lists, samples_t, inter, coil_last, tables,
+      total;
 };
 
 size_t record_bytes(int width) {
@@ -281,6 +282,7 @@ Layout make_layout(const Shape& s, const ksj_gpu_gridding_desc* d) {
   l.offsets = take((nl + s.frames) * 4);
   l.entries = take(static_cast<size_t>(s.frames) * s.entries_per_frame * 4);
   l.expanded = take(static_cast<size_t>(s.frames) * s.entries_per_frame * meta_vecs(s.width) * 16);
+  l.long_lists = take((2 + static_cast<size_t>(s.frames) * s.entries_per_frame / (s.list_capacity + 1)) * 4);
   l.samples_t = take(fm * s.channels * sample_bytes(d->sample_format));
   l.inter = take(static_cast<size_t>(s.frames) * s.grid_rows * s.out_cols * s.cpitch * sizeof(float2));
   l.coil_last = d->output == KSJ_GPU_OUTPUT_COIL_MAJOR
@@ -534,8 +536,6 @@ __device__ __forceinline__ void warp_sort(uint32_t* buf, int n, int lane) {
   }
 }
 
-// One warp per list: sort its sample indices ascending, in shared memory
-// when the list fits the per-warp buffer, in place in global memory otherwise.
 // One list entry as k_rows consumes it (meta_vecs(W) 16-byte vectors):
 //   v0 = {tap word, sample index, scale.re, scale.im}, v1.. = the W column
 //   weights times this row's weight (zero padded).
@@ -626,18 +626,48 @@ struct SortArgs {
   uint32_t* entries;
   const unsigned char* records;
   float4* expanded;
+  uint32_t* long_lists;  // lists longer than `capacity`, left to k_sort_long
+  uint32_t* long_count;
   int frames, samples, lists_per_frame, nchunks, grid_rows, grid_cols, capacity;
   size_t entries_per_frame;  // 0 when the offsets are absolute (3-D: one entry array for all planes)
   int dim3;                  // 3-D: frames are grid planes and the records are per sample (SampleRecord3)
 };
 
-// Per list (one warp): sort the sample indices, then write every entry in
-// its expanded form (the dependent record loads happen here, across many
-// lists in flight, not in the row pass).
+// Expanded entries of list l of frame f, entries i = first, first + step, ...
+template <int W>
+__device__ __forceinline__ void expand_list(const SortArgs& a, int f, int l, uint32_t begin, int n,
+                                            const uint32_t* sorted, int first, int step) {
+  constexpr int kMV = meta_vecs(W);
+  const int row = l / a.nchunks;
+  const int col_lo = (l - row * a.nchunks) * kChunk;
+  const int col_hi = min(col_lo + kChunk, a.grid_cols);
+  float4* out = a.expanded + (static_cast<size_t>(f) * a.entries_per_frame + begin) * kMV;
+  if (a.dim3) {
+    const SampleRecord3<W>* recs = reinterpret_cast<const SampleRecord3<W>*>(a.records);
+    for (int i = first; i < n; i += step) {
+      float4 e[kMV];
+      expand_entry3<W>(recs, sorted[i], f, row, col_lo, col_hi, a.grid_cols, e);
+#pragma unroll
+      for (int v = 0; v < kMV; ++v) out[static_cast<size_t>(i) * kMV + v] = e[v];
+    }
+    return;
+  }
+  const SampleRecord<W>* recs = reinterpret_cast<const SampleRecord<W>*>(a.records) + static_cast<size_t>(f) * a.samples;
+  for (int i = first; i < n; i += step) {
+    float4 e[kMV];
+    expand_entry<W>(recs, sorted[i], row, col_lo, col_hi, a.grid_rows, a.grid_cols, e);
+#pragma unroll
+    for (int v = 0; v < kMV; ++v) out[static_cast<size_t>(i) * kMV + v] = e[v];
+  }
+}
+
+// Per list (one warp): sort the sample indices ascending in the warp's
+// shared buffer, then write every entry in its expanded form (the dependent
+// record loads happen here, across many lists in flight, not in the row
+// pass).  Lists longer than the buffer are queued for k_sort_long.
 template <int W>
 __global__ void __launch_bounds__(256) k_sort(SortArgs a) {
   extern __shared__ uint32_t sort_buf[];
-  constexpr int kMV = meta_vecs(W);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const size_t gl = static_cast<size_t>(blockIdx.x) * (blockDim.x >> 5) + warp;
   if (gl >= static_cast<size_t>(a.frames) * a.lists_per_frame) return;
@@ -647,43 +677,102 @@ __global__ void __launch_bounds__(256) k_sort(SortArgs a) {
   const uint32_t begin = off[l];
   const int n = static_cast<int>(off[l + 1] - begin);
   if (n == 0) return;
+  if (n > a.capacity) {
+    if (lane == 0) a.long_lists[atomicAdd(a.long_count, 1u)] = static_cast<uint32_t>(gl);
+    return;
+  }
   uint32_t* ent = a.entries + static_cast<size_t>(f) * a.entries_per_frame + begin;
   const uint32_t* sorted = ent;
   if (n >= 2) {
-    if (n <= a.capacity) {
-      uint32_t* buf = sort_buf + static_cast<size_t>(warp) * a.capacity;
-      for (int i = lane; i < n; i += 32) buf[i] = ent[i];
-      __syncwarp();
-      warp_sort(buf, n, lane);
-      for (int i = lane; i < n; i += 32) ent[i] = buf[i];
-      sorted = buf;
-    } else {
-      warp_sort(ent, n, lane);
-    }
+    uint32_t* buf = sort_buf + static_cast<size_t>(warp) * a.capacity;
+    for (int i = lane; i < n; i += 32) buf[i] = ent[i];
+    __syncwarp();
+    warp_sort(buf, n, lane);
+    for (int i = lane; i < n; i += 32) ent[i] = buf[i];
+    sorted = buf;
     __syncwarp();
   }
   if (a.expanded == nullptr) return;  // lists only (density compensation)
-  const int row = l / a.nchunks;
-  const int col_lo = (l - row * a.nchunks) * kChunk;
-  const int col_hi = min(col_lo + kChunk, a.grid_cols);
-  float4* out = a.expanded + (static_cast<size_t>(f) * a.entries_per_frame + begin) * kMV;
-  if (a.dim3) {
-    const SampleRecord3<W>* recs = reinterpret_cast<const SampleRecord3<W>*>(a.records);
-    for (int i = lane; i < n; i += 32) {
-      float4 e[kMV];
-      expand_entry3<W>(recs, sorted[i], f, row, col_lo, col_hi, a.grid_cols, e);
-#pragma unroll
-      for (int v = 0; v < kMV; ++v) out[static_cast<size_t>(i) * kMV + v] = e[v];
+  expand_list<W>(a, f, l, begin, n, sorted, lane, 32);
+}
+
+constexpr int kLongSortThreads = 1024;
+constexpr int kLongSortSmem = 16384;  // entries sorted in shared memory; longer lists in place in L2/HBM
+
+// The same bitonic network over a whole block.
+__device__ __forceinline__ void block_sort(uint32_t* buf, int n) {
+  int p = 1;
+  while (p < n) p <<= 1;
+  for (int k = 2; k <= p; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int i = threadIdx.x; i < p; i += blockDim.x) {
+        const int partner = (j == (k >> 1)) ? (i ^ (k - 1)) : (i ^ j);
+        if (partner > i && partner < n) {
+          const uint32_t x = buf[i], y = buf[partner];
+          if (x > y) {
+            buf[i] = y;
+            buf[partner] = x;
+          }
+        }
+      }
+      __syncthreads();
     }
-    return;
   }
-  const SampleRecord<W>* recs = reinterpret_cast<const SampleRecord<W>*>(a.records) + static_cast<size_t>(f) * a.samples;
-  for (int i = lane; i < n; i += 32) {
-    float4 e[kMV];
-    expand_entry<W>(recs, sorted[i], row, col_lo, col_hi, a.grid_rows, a.grid_cols, e);
-#pragma unroll
-    for (int v = 0; v < kMV; ++v) out[static_cast<size_t>(i) * kMV + v] = e[v];
+}
+
+template <int W>
+__device__ __forceinline__ void sort_long_list(const SortArgs& a, size_t gl, uint32_t* long_buf) {
+  const int f = static_cast<int>(gl / a.lists_per_frame);
+  const int l = static_cast<int>(gl - static_cast<size_t>(f) * a.lists_per_frame);
+  const uint32_t* off = a.offsets + static_cast<size_t>(f) * (a.lists_per_frame + 1);
+  const uint32_t begin = off[l];
+  const int n = static_cast<int>(off[l + 1] - begin);
+  uint32_t* ent = a.entries + static_cast<size_t>(f) * a.entries_per_frame + begin;
+  const uint32_t* sorted = ent;
+  if (n <= kLongSortSmem) {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) long_buf[i] = ent[i];
+    __syncthreads();
+    block_sort(long_buf, n);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) ent[i] = long_buf[i];
+    sorted = long_buf;
+  } else {
+    block_sort(ent, n);
   }
+  __syncthreads();
+  if (a.expanded != nullptr) expand_list<W>(a, f, l, begin, n, sorted, threadIdx.x, blockDim.x);
+}
+
+// Blocks take the queued long lists in turn: sort (in shared memory up to
+// kLongSortSmem entries, else in place) and expand.
+template <int W>
+__global__ void __launch_bounds__(kLongSortThreads) k_sort_long(SortArgs a) {
+  extern __shared__ uint32_t long_buf[];
+  const uint32_t queued = *a.long_count;
+  for (uint32_t q = blockIdx.x; q < queued; q += gridDim.x) {
+    sort_long_list<W>(a, a.long_lists[q], long_buf);
+    __syncthreads();
+  }
+}
+
+// Launch k_sort and then k_sort_long for the lists it queued.
+template <int W>
+ksj_gpu_status launch_sort(SortArgs sa, size_t lists, size_t entries_total, int capacity, cudaStream_t stream) {
+  if (cudaMemsetAsync(sa.long_count, 0, sizeof(uint32_t), stream) != cudaSuccess) return KSJ_GPU_ERROR_CUDA;
+  const size_t smem = static_cast<size_t>(8) * capacity * 4;
+  if (cudaFuncSetAttribute(k_sort<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)) !=
+          cudaSuccess ||
+      cudaFuncSetAttribute(k_sort_long<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, kLongSortSmem * 4) !=
+          cudaSuccess)
+    return KSJ_GPU_ERROR_CUDA;
+  {
+    LaunchScope scope("k_sort", stream);
+    k_sort<W><<<static_cast<unsigned>((lists + 7) / 8), 256, smem, stream>>>(sa);
+  }
+  const size_t most = std::max<size_t>(1, entries_total / (static_cast<size_t>(capacity) + 1));
+  LaunchScope scope("k_sort_long", stream);
+  k_sort_long<W><<<static_cast<unsigned>(std::min<size_t>(std::min<size_t>(most, lists), 1024)), kLongSortThreads,
+                   kLongSortSmem * 4, stream>>>(sa);
+  return KSJ_GPU_OK;
 }
 
 // [frame][channel][sample] -> [frame][sample][channel] through a 32x33
@@ -1143,7 +1232,8 @@ bool make_inter_map(const Shape& s, void* inter, CUtensorMap* map, int* box_rows
 template <int W>
 ksj_gpu_status build_lists(const Shape& s, const ksj_gpu_gridding_desc* d, const float* d_traj, const float* d_dcf,
                            uint32_t* flags, unsigned char* records, uint32_t* counts, uint32_t* cursor,
-                           uint32_t* offsets, uint32_t* entries, float4* expanded, cudaStream_t stream) {
+                           uint32_t* offsets, uint32_t* entries, float4* expanded, uint32_t* long_lists,
+                           cudaStream_t stream) {
   const size_t nl = static_cast<size_t>(s.frames) * s.lists_per_frame;
   if (cudaMemsetAsync(counts, 0, nl * 4, stream) != cudaSuccess) return KSJ_GPU_ERROR_CUDA;
   if (cudaMemsetAsync(cursor, 0, nl * 4, stream) != cudaSuccess) return KSJ_GPU_ERROR_CUDA;
@@ -1184,15 +1274,13 @@ ksj_gpu_status build_lists(const Shape& s, const ksj_gpu_gridding_desc* d, const
         s.entries_per_frame);
   }
   {
-    const size_t smem = static_cast<size_t>(8) * s.list_capacity * 4;
-    if (cudaFuncSetAttribute(k_sort<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)) !=
-        cudaSuccess)
-      return KSJ_GPU_ERROR_CUDA;
     SortArgs sa{};
     sa.offsets = offsets;
     sa.entries = entries;
     sa.records = records;
     sa.expanded = expanded;
+    sa.long_count = long_lists;
+    sa.long_lists = long_lists + 1;
     sa.frames = s.frames;
     sa.samples = s.samples;
     sa.lists_per_frame = s.lists_per_frame;
@@ -1202,8 +1290,9 @@ ksj_gpu_status build_lists(const Shape& s, const ksj_gpu_gridding_desc* d, const
     sa.capacity = s.list_capacity;
     sa.entries_per_frame = s.entries_per_frame;
     sa.dim3 = 0;
-    LaunchScope scope("k_sort", stream);
-    k_sort<W><<<static_cast<unsigned>((nl + 7) / 8), 256, smem, stream>>>(sa);
+    const ksj_gpu_status st = launch_sort<W>(sa, nl, static_cast<size_t>(s.frames) * s.entries_per_frame,
+                                             s.list_capacity, stream);
+    if (st != KSJ_GPU_OK) return st;
   }
   return KSJ_GPU_OK;
 }
@@ -1238,7 +1327,8 @@ ksj_gpu_status launch_all(const Shape& s, const Layout& l, const ksj_gpu_griddin
   }
   {
     const ksj_gpu_status st = build_lists<W>(s, d, d_traj, d_dcf, flags, records, counts, cursor, offsets, entries,
-                                             reinterpret_cast<float4*>(ws + l.expanded), stream);
+                                             reinterpret_cast<float4*>(ws + l.expanded),
+                                             reinterpret_cast<uint32_t*>(ws + l.long_lists), stream);
     if (st != KSJ_GPU_OK) return st;
   }
   {
@@ -1458,7 +1548,7 @@ __global__ void __launch_bounds__(256) k_pm_update(const PmRecord<W>* pm, const 
 }
 
 struct PmLayout {
-  size_t flags, records, counts, cursor, offsets, entries, pm, w, grid, total;
+  size_t flags, records, counts, cursor, offsets, entries, long_lists, pm, w, grid, total;
 };
 
 PmLayout make_pm_layout(const Shape& s) {
@@ -1477,6 +1567,7 @@ PmLayout make_pm_layout(const Shape& s) {
   l.cursor = take(nl * 4);
   l.offsets = take((nl + s.frames) * 4);
   l.entries = take(static_cast<size_t>(s.frames) * s.entries_per_frame * 4);
+  l.long_lists = take((2 + static_cast<size_t>(s.frames) * s.entries_per_frame / (s.list_capacity + 1)) * 4);
   l.pm = take(fm * (8 + 16 * static_cast<size_t>(s.width)));
   l.w = take(fm * sizeof(double));
   l.grid = take(static_cast<size_t>(s.frames) * s.grid_rows * s.grid_cols * sizeof(double));
@@ -1496,7 +1587,8 @@ ksj_gpu_status launch_pipe_menon(const Shape& s, const PmLayout& l, const ksj_gp
   const ksj_gpu_status st =
       build_lists<W>(s, &dd, d_traj, nullptr, flags, ws + l.records, reinterpret_cast<uint32_t*>(ws + l.counts),
                      reinterpret_cast<uint32_t*>(ws + l.cursor), reinterpret_cast<uint32_t*>(ws + l.offsets),
-                     reinterpret_cast<uint32_t*>(ws + l.entries), nullptr, stream);
+                     reinterpret_cast<uint32_t*>(ws + l.entries), nullptr,
+                     reinterpret_cast<uint32_t*>(ws + l.long_lists), stream);
   if (st != KSJ_GPU_OK) return st;
   const size_t fm = static_cast<size_t>(s.frames) * s.samples;
   PmRecord<W>* pm = reinterpret_cast<PmRecord<W>*>(ws + l.pm);
@@ -1664,7 +1756,8 @@ __global__ void __launch_bounds__(256) k_scatter3(const unsigned char* records, 
 }
 
 struct Layout3 {
-  size_t flags, records, counts, cursor, offsets, bases, entries, expanded, samples_t, inter, inter2, tables, total;
+  size_t flags, records, counts, cursor, offsets, bases, entries, expanded, long_lists, samples_t, inter, inter2,
+      tables, total;
   size_t entries_total;
 };
 
@@ -1697,6 +1790,7 @@ Layout3 make_layout3(const Shape& s, uint32_t sample_format) {
   l.bases = take(g * 4);
   l.entries = take(l.entries_total * 4);
   l.expanded = take(l.entries_total * meta_vecs(s.width) * 16);
+  l.long_lists = take((2 + l.entries_total / (s.list_capacity + 1)) * 4);
   l.samples_t = take(static_cast<size_t>(s.samples) * s.channels * sample_bytes(sample_format));
   l.inter = take(g * g * n * s.cpitch * sizeof(float2));
   l.inter2 = take(g * n * n * s.cpitch * sizeof(float2));
@@ -1803,15 +1897,13 @@ ksj_gpu_status launch_all3(const Shape& s, const Layout3& l, const ksj_gpu_gridd
                                                                s.nchunks, s.lists_per_frame);
   }
   {
-    const size_t smem = static_cast<size_t>(8) * s.list_capacity * 4;
-    if (cudaFuncSetAttribute(k_sort<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)) !=
-        cudaSuccess)
-      return KSJ_GPU_ERROR_CUDA;
     SortArgs sa{};
     sa.offsets = offsets;
     sa.entries = entries;
     sa.records = ws + l.records;
     sa.expanded = reinterpret_cast<float4*>(ws + l.expanded);
+    sa.long_count = reinterpret_cast<uint32_t*>(ws + l.long_lists);
+    sa.long_lists = sa.long_count + 1;
     sa.frames = g;
     sa.samples = s.samples;
     sa.lists_per_frame = s.lists_per_frame;
@@ -1821,8 +1913,8 @@ ksj_gpu_status launch_all3(const Shape& s, const Layout3& l, const ksj_gpu_gridd
     sa.capacity = s.list_capacity;
     sa.entries_per_frame = 0;
     sa.dim3 = 1;
-    LaunchScope scope("k_sort", stream);
-    k_sort<W><<<static_cast<unsigned>((nl + 7) / 8), 256, smem, stream>>>(sa);
+    const ksj_gpu_status st = launch_sort<W>(sa, nl, l.entries_total, s.list_capacity, stream);
+    if (st != KSJ_GPU_OK) return st;
   }
   {
     const dim3 tg((s.samples + 31) / 32, (s.channels + 31) / 32, 1);
