@@ -199,6 +199,14 @@ KSJ_GPU_API ksj_gpu_status ksj_gpu_pipe_menon_dcf(const ksj_gpu_gridding_desc* d
                                                   const float* d_traj, float* d_dcf, void* d_workspace,
                                                   size_t workspace_bytes, void* stream);
 
+/* The same iteration in 3-D, for the kernel and grid of a 3-D gridding
+ * descriptor (its channels and output are not used): d_traj [sample][3],
+ * d_dcf [sample] float32 out. */
+KSJ_GPU_API size_t ksj_gpu_pipe_menon3_workspace_bytes(const ksj_gpu_gridding3_desc* desc);
+KSJ_GPU_API ksj_gpu_status ksj_gpu_pipe_menon_dcf3(const ksj_gpu_gridding3_desc* desc, uint32_t iterations,
+                                                   const float* d_traj, float* d_dcf, void* d_workspace,
+                                                   size_t workspace_bytes, void* stream);
+
 /* ----------------------------------------------------------- direct NUDFT */
 
 /* Exact direct adjoint NUDFT, no DCF:

@@ -1825,6 +1825,76 @@ ksj_gpu_status make_shape3(const ksj_gpu_gridding3_desc* d, const ksj_gpu_griddi
   return KSJ_GPU_OK;
 }
 
+// The 3-D binning lists: per-sample records, (plane, row, chunk) counts, per-plane
+// scans made absolute, the scattered entries, their sort and (when `expanded`
+// is given) the expanded entries.  `flags` must already be cleared.
+template <int W>
+ksj_gpu_status build_lists3(const Shape& s, uint32_t dcf_mode, const float* d_traj, const float* d_dcf,
+                            uint32_t* flags, unsigned char* records, uint32_t* counts, uint32_t* cursor,
+                            uint32_t* offsets, uint32_t* bases, uint32_t* entries, float4* expanded,
+                            uint32_t* long_lists, size_t entries_total, cudaStream_t stream) {
+  const int g = s.grid_rows;
+  const size_t nl = static_cast<size_t>(g) * s.lists_per_frame;
+  if (cudaMemsetAsync(counts, 0, nl * 4, stream) != cudaSuccess) return KSJ_GPU_ERROR_CUDA;
+  if (cudaMemsetAsync(cursor, 0, nl * 4, stream) != cudaSuccess) return KSJ_GPU_ERROR_CUDA;
+  {
+    Prepare3Args p{};
+    p.traj = d_traj;
+    p.dcf = d_dcf;
+    p.dcf_mode = dcf_mode;
+    p.records = records;
+    p.counts = counts;
+    p.flags = flags;
+    p.samples = s.samples;
+    p.grid = g;
+    p.nchunks = s.nchunks;
+    p.lists_per_plane = s.lists_per_frame;
+    p.beta = s.beta;
+    p.two_over_w = 2.0f / static_cast<float>(s.width);
+    p.inv_i0_beta = s.inv_i0_beta;
+    p.phase = s.phase_row;
+    LaunchScope scope("k_prepare3", stream);
+    k_prepare3<W><<<(s.samples + 255) / 256, 256, 0, stream>>>(p);
+  }
+  {
+    LaunchScope scope("k_scan", stream);
+    k_scan<<<g, 1024, 0, stream>>>(counts, offsets, s.lists_per_frame);
+  }
+  {
+        LaunchScope scope("k_plane_offsets", stream);
+    k_plane_bases<<<1, 512, 0, stream>>>(offsets, g, s.lists_per_frame, bases);
+    const size_t total = static_cast<size_t>(g) * (s.lists_per_frame + 1);
+    k_offsets_add<<<static_cast<unsigned>((total + 255) / 256), 256, 0, stream>>>(offsets, g, s.lists_per_frame,
+                                                                                bases);
+  }
+  {
+    LaunchScope scope("k_scatter3", stream);
+    k_scatter3<W><<<(s.samples + 255) / 256, 256, 0, stream>>>(records, offsets, cursor, entries, s.samples, g,
+                                                               s.nchunks, s.lists_per_frame);
+  }
+  {
+    SortArgs sa{};
+    sa.offsets = offsets;
+    sa.entries = entries;
+    sa.records = records;
+    sa.expanded = expanded;
+    sa.long_count = long_lists;
+    sa.long_lists = sa.long_count + 1;
+    sa.frames = g;
+    sa.samples = s.samples;
+    sa.lists_per_frame = s.lists_per_frame;
+    sa.nchunks = s.nchunks;
+    sa.grid_rows = g;
+    sa.grid_cols = g;
+    sa.capacity = s.list_capacity;
+    sa.entries_per_frame = 0;
+    sa.dim3 = 1;
+    const ksj_gpu_status st = launch_sort<W>(sa, nl, entries_total, s.list_capacity, stream);
+    if (st != KSJ_GPU_OK) return st;
+  }
+  return KSJ_GPU_OK;
+}
+
 template <int W, uint32_t kFormat>
 ksj_gpu_status launch_all3(const Shape& s, const Layout3& l, const ksj_gpu_gridding3_desc* d, const void* d_kspace,
                            const float* d_traj, const float* d_dcf, void* d_out, unsigned char* ws,
@@ -1844,11 +1914,8 @@ ksj_gpu_status launch_all3(const Shape& s, const Layout3& l, const ksj_gpu_gridd
   int* pos_rows = reinterpret_cast<int*>(inv_dc + n);
   int* pos_cols = pos_rows + n;
   float* ones = reinterpret_cast<float*>(pos_cols + n);
-  const size_t nl = static_cast<size_t>(g) * s.lists_per_frame;
 
   if (cudaMemsetAsync(flags, 0, kFlagBytes, stream) != cudaSuccess) return KSJ_GPU_ERROR_CUDA;
-  if (cudaMemsetAsync(counts, 0, nl * 4, stream) != cudaSuccess) return KSJ_GPU_ERROR_CUDA;
-  if (cudaMemsetAsync(cursor, 0, nl * 4, stream) != cudaSuccess) return KSJ_GPU_ERROR_CUDA;
   {
     const int nt = std::max(g, n);
     LaunchScope scope("k_tables", stream);
@@ -1861,59 +1928,11 @@ ksj_gpu_status launch_all3(const Shape& s, const Layout3& l, const ksj_gpu_gridd
     k_fill<<<(n * n + 255) / 256, 256, 0, stream>>>(ones, n * n, 1.0f);
   }
   {
-    Prepare3Args p{};
-    p.traj = d_traj;
-    p.dcf = d_dcf;
-    p.dcf_mode = d->dcf_mode;
-    p.records = ws + l.records;
-    p.counts = counts;
-    p.flags = flags;
-    p.samples = s.samples;
-    p.grid = g;
-    p.nchunks = s.nchunks;
-    p.lists_per_plane = s.lists_per_frame;
-    p.beta = s.beta;
-    p.two_over_w = 2.0f / static_cast<float>(s.width);
-    p.inv_i0_beta = s.inv_i0_beta;
-    p.phase = s.phase_row;
-    LaunchScope scope("k_prepare3", stream);
-    k_prepare3<W><<<(s.samples + 255) / 256, 256, 0, stream>>>(p);
-  }
-  {
-    LaunchScope scope("k_scan", stream);
-    k_scan<<<g, 1024, 0, stream>>>(counts, offsets, s.lists_per_frame);
-  }
-  {
-    uint32_t* bases = reinterpret_cast<uint32_t*>(ws + l.bases);
-    LaunchScope scope("k_plane_offsets", stream);
-    k_plane_bases<<<1, 512, 0, stream>>>(offsets, g, s.lists_per_frame, bases);
-    const size_t total = static_cast<size_t>(g) * (s.lists_per_frame + 1);
-    k_offsets_add<<<static_cast<unsigned>((total + 255) / 256), 256, 0, stream>>>(offsets, g, s.lists_per_frame,
-                                                                                bases);
-  }
-  {
-    LaunchScope scope("k_scatter3", stream);
-    k_scatter3<W><<<(s.samples + 255) / 256, 256, 0, stream>>>(ws + l.records, offsets, cursor, entries, s.samples, g,
-                                                               s.nchunks, s.lists_per_frame);
-  }
-  {
-    SortArgs sa{};
-    sa.offsets = offsets;
-    sa.entries = entries;
-    sa.records = ws + l.records;
-    sa.expanded = reinterpret_cast<float4*>(ws + l.expanded);
-    sa.long_count = reinterpret_cast<uint32_t*>(ws + l.long_lists);
-    sa.long_lists = sa.long_count + 1;
-    sa.frames = g;
-    sa.samples = s.samples;
-    sa.lists_per_frame = s.lists_per_frame;
-    sa.nchunks = s.nchunks;
-    sa.grid_rows = g;
-    sa.grid_cols = g;
-    sa.capacity = s.list_capacity;
-    sa.entries_per_frame = 0;
-    sa.dim3 = 1;
-    const ksj_gpu_status st = launch_sort<W>(sa, nl, l.entries_total, s.list_capacity, stream);
+    const ksj_gpu_status st = build_lists3<W>(s, d->dcf_mode, d_traj, d_dcf, flags, ws + l.records, counts, cursor,
+                                              offsets, reinterpret_cast<uint32_t*>(ws + l.bases), entries,
+                                              reinterpret_cast<float4*>(ws + l.expanded),
+                                              reinterpret_cast<uint32_t*>(ws + l.long_lists), l.entries_total,
+                                              stream);
     if (st != KSJ_GPU_OK) return st;
   }
   {
@@ -2012,6 +2031,171 @@ ksj_gpu_status launch_all3(const Shape& s, const Layout3& l, const ksj_gpu_gridd
   {
     LaunchScope scope("k_cols_z", stream);
     k_cols<<<dim3((n * n + s.column_block - 1) / s.column_block, 1), kColsThreads, cols_smem, stream>>>(zmap, cz);
+  }
+  return check_launch();
+}
+
+// ------------------------------------------- 3-D Pipe-Menon density weights
+
+template <int W>
+struct PmRecord3 {
+  int z0, r0, c0, pad;
+  double wz[W];
+  double wr[W];
+  double wc[W];
+};
+
+template <int W>
+__global__ void __launch_bounds__(256) k_pm_prepare3(const float* traj, PmRecord3<W>* pm, double* w, int samples,
+                                                     int grid, double beta, double inv_i0_beta) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= samples) return;
+  float k[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) k[d] = __ldg(traj + 3 * static_cast<size_t>(idx) + d);
+  const bool ok = isfinite(k[0]) && isfinite(k[1]) && isfinite(k[2]) && fabsf(k[0]) < 1.0e4f &&
+                  fabsf(k[1]) < 1.0e4f && fabsf(k[2]) < 1.0e4f;
+  PmRecord3<W> r;
+  r.pad = 0;
+  constexpr double kTwoPiD = 6.283185307179586476925286766559;
+  int t0[3] = {0, 0, 0};
+  double u[3] = {0.0, 0.0, 0.0};
+  if (ok)
+    for (int d = 0; d < 3; ++d) {
+      u[d] = static_cast<double>(k[d]) * grid / kTwoPiD;
+      t0[d] = static_cast<int>(floor(u[d])) - W / 2 + 1;
+    }
+  r.z0 = wrap_index(t0[0], grid);
+  r.r0 = wrap_index(t0[1], grid);
+  r.c0 = wrap_index(t0[2], grid);
+#pragma unroll
+  for (int j = 0; j < W; ++j) {
+    r.wz[j] = ok ? kb_weight64(static_cast<double>(t0[0] + j) - u[0], W, beta, inv_i0_beta) : 0.0;
+    r.wr[j] = ok ? kb_weight64(static_cast<double>(t0[1] + j) - u[1], W, beta, inv_i0_beta) : 0.0;
+    r.wc[j] = ok ? kb_weight64(static_cast<double>(t0[2] + j) - u[2], W, beta, inv_i0_beta) : 0.0;
+  }
+  pm[idx] = r;
+  w[idx] = ok ? 1.0 : 0.0;
+}
+
+// One half-warp per (plane, row, chunk) list; lane l % 16 is a column.
+template <int W>
+__global__ void __launch_bounds__(256) k_pm_grid3(const uint32_t* offsets, const uint32_t* entries,
+                                                  const PmRecord3<W>* pm, const double* w, double* grid, int g,
+                                                  int nchunks, int lists_per_plane) {
+  const size_t hw = (static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 4;
+  const int sub = threadIdx.x & 15;
+  if (hw >= static_cast<size_t>(g) * lists_per_plane) return;
+  const int plane = static_cast<int>(hw / lists_per_plane);
+  const int l = static_cast<int>(hw - static_cast<size_t>(plane) * lists_per_plane);
+  const int row = l / nchunks;
+  const int col = (l - row * nchunks) * kChunk + sub;
+  const uint32_t* off = offsets + static_cast<size_t>(plane) * (lists_per_plane + 1);
+  double acc = 0.0;
+  for (uint32_t e = off[l]; e < off[l + 1]; ++e) {
+    const uint32_t sidx = __ldg(entries + e);
+    const PmRecord3<W>& r = pm[sidx];
+    int dz = plane - r.z0;
+    if (dz < 0) dz += g;
+    int dr = row - r.r0;
+    if (dr < 0) dr += g;
+    int dc = col - r.c0;
+    if (dc < 0) dc += g;
+    if (dz < W && dr < W && dc < W) acc += w[sidx] * ((r.wz[dz] * r.wr[dr]) * r.wc[dc]);
+  }
+  if (col < g) grid[(static_cast<size_t>(plane) * g + row) * g + col] = acc;
+}
+
+template <int W>
+__global__ void __launch_bounds__(256) k_pm_update3(const PmRecord3<W>* pm, const double* grid, double* w, float* out,
+                                                    int samples, int g) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= samples) return;
+  const PmRecord3<W> r = pm[idx];
+  double d = 0.0;
+  for (int a = 0; a < W; ++a) {
+    int zz = r.z0 + a;
+    if (zz >= g) zz -= g;
+    for (int b = 0; b < W; ++b) {
+      int yy = r.r0 + b;
+      if (yy >= g) yy -= g;
+      const double wzy = r.wz[a] * r.wr[b];
+      const double* line = grid + (static_cast<size_t>(zz) * g + yy) * g;
+#pragma unroll
+      for (int c = 0; c < W; ++c) {
+        int xx = r.c0 + c;
+        if (xx >= g) xx -= g;
+        d += line[xx] * (wzy * r.wc[c]);
+      }
+    }
+  }
+  const double nw = d > 0.0 ? w[idx] / d : 0.0;
+  w[idx] = nw;
+  if (out != nullptr) out[idx] = static_cast<float>(nw);
+}
+
+struct PmLayout3 {
+  size_t flags, records, counts, cursor, offsets, bases, entries, long_lists, pm, w, grid, total, entries_total;
+};
+
+PmLayout3 make_pm_layout3(const Shape& s) {
+  PmLayout3 l{};
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    const size_t at = off;
+    off = align_up(off + bytes, 256);
+    return at;
+  };
+  const size_t g = static_cast<size_t>(s.grid_rows);
+  const size_t nl = g * s.lists_per_frame;
+  l.entries_total = static_cast<size_t>(s.samples) * s.width * s.width * 2;
+  l.flags = take(kFlagBytes);
+  l.records = take(static_cast<size_t>(s.samples) * record3_bytes(s.width));
+  l.counts = take(nl * 4);
+  l.cursor = take(nl * 4);
+  l.offsets = take((nl + g) * 4);
+  l.bases = take(g * 4);
+  l.entries = take(l.entries_total * 4);
+  l.long_lists = take((2 + l.entries_total / (s.list_capacity + 1)) * 4);
+  l.pm = take(static_cast<size_t>(s.samples) * (16 + 24 * static_cast<size_t>(s.width)));
+  l.w = take(static_cast<size_t>(s.samples) * sizeof(double));
+  l.grid = take(g * g * g * sizeof(double));
+  l.total = off;
+  return l;
+}
+
+template <int W>
+ksj_gpu_status launch_pipe_menon3(const Shape& s, const PmLayout3& l, uint32_t iterations, const float* d_traj,
+                                  float* d_dcf, unsigned char* ws, cudaStream_t stream) {
+  static_assert(sizeof(PmRecord3<W>) == 16 + 24 * W, "PmRecord3 layout");
+  const int g = s.grid_rows;
+  uint32_t* flags = reinterpret_cast<uint32_t*>(ws + l.flags);
+  if (cudaMemsetAsync(flags, 0, kFlagBytes, stream) != cudaSuccess) return KSJ_GPU_ERROR_CUDA;
+  const ksj_gpu_status st = build_lists3<W>(
+      s, KSJ_GPU_DCF_NONE, d_traj, nullptr, flags, ws + l.records, reinterpret_cast<uint32_t*>(ws + l.counts),
+      reinterpret_cast<uint32_t*>(ws + l.cursor), reinterpret_cast<uint32_t*>(ws + l.offsets),
+      reinterpret_cast<uint32_t*>(ws + l.bases), reinterpret_cast<uint32_t*>(ws + l.entries), nullptr,
+      reinterpret_cast<uint32_t*>(ws + l.long_lists), l.entries_total, stream);
+  if (st != KSJ_GPU_OK) return st;
+  PmRecord3<W>* pm = reinterpret_cast<PmRecord3<W>*>(ws + l.pm);
+  double* w = reinterpret_cast<double*>(ws + l.w);
+  double* grid = reinterpret_cast<double*>(ws + l.grid);
+  {
+    LaunchScope scope("k_pm_prepare3", stream);
+    k_pm_prepare3<W><<<(s.samples + 255) / 256, 256, 0, stream>>>(d_traj, pm, w, s.samples, g, s.beta,
+                                                                 1.0 / std::cyl_bessel_i(0.0, static_cast<double>(s.beta)));
+  }
+  const size_t half_warps = static_cast<size_t>(g) * s.lists_per_frame;
+  for (uint32_t it = 0; it < iterations; ++it) {
+    {
+      LaunchScope scope("k_pm_grid3", stream);
+      k_pm_grid3<W><<<static_cast<unsigned>((half_warps * 16 + 255) / 256), 256, 0, stream>>>(
+          reinterpret_cast<const uint32_t*>(ws + l.offsets), reinterpret_cast<const uint32_t*>(ws + l.entries), pm, w,
+          grid, g, s.nchunks, s.lists_per_frame);
+    }
+    LaunchScope scope("k_pm_update3", stream);
+    k_pm_update3<W><<<(s.samples + 255) / 256, 256, 0, stream>>>(pm, grid, w, it + 1 == iterations ? d_dcf : nullptr,
+                                                                s.samples, g);
   }
   return check_launch();
 }
@@ -2251,6 +2435,37 @@ extern "C" ksj_gpu_status ksj_gpu_gridding3_adjoint(const ksj_gpu_gridding3_desc
                 : launch_all3<W, KSJ_GPU_SAMPLES_CF32>(s, l, desc, d_kspace, d_traj, d_dcf, d_out, ws, cs);
     KSJ_G3_CASE(2) KSJ_G3_CASE(4) KSJ_G3_CASE(6) KSJ_G3_CASE(8)
 #undef KSJ_G3_CASE
+    default: return KSJ_GPU_ERROR_UNSUPPORTED;
+  }
+}
+
+extern "C" size_t ksj_gpu_pipe_menon3_workspace_bytes(const ksj_gpu_gridding3_desc* desc) {
+  Shape s{};
+  if (make_shape3(desc, nullptr, &s) != KSJ_GPU_OK) return 0;
+  return make_pm_layout3(s).total;
+}
+
+extern "C" ksj_gpu_status ksj_gpu_pipe_menon_dcf3(const ksj_gpu_gridding3_desc* desc, uint32_t iterations,
+                                                  const float* d_traj, float* d_dcf, void* d_workspace,
+                                                  size_t workspace_bytes, void* stream) {
+  if (iterations == 0 || iterations > 1000) return KSJ_GPU_ERROR_INVALID_ARGUMENT;
+  Shape s{};
+  const ksj_gpu_status st = make_shape3(desc, nullptr, &s);
+  if (st != KSJ_GPU_OK) return st;
+  if (d_traj == nullptr || d_dcf == nullptr || (reinterpret_cast<uintptr_t>(d_traj) & 3u) != 0 ||
+      (reinterpret_cast<uintptr_t>(d_dcf) & 3u) != 0)
+    return KSJ_GPU_ERROR_INVALID_ARGUMENT;
+  const PmLayout3 l = make_pm_layout3(s);
+  if (l.entries_total > 0xffffffffull) return KSJ_GPU_ERROR_UNSUPPORTED;
+  if (d_workspace == nullptr || (reinterpret_cast<uintptr_t>(d_workspace) & 255u) != 0 || workspace_bytes < l.total)
+    return KSJ_GPU_ERROR_WORKSPACE;
+  unsigned char* ws = static_cast<unsigned char*>(d_workspace);
+  cudaStream_t cs = static_cast<cudaStream_t>(stream);
+  switch (s.width) {
+    case 2: return launch_pipe_menon3<2>(s, l, iterations, d_traj, d_dcf, ws, cs);
+    case 4: return launch_pipe_menon3<4>(s, l, iterations, d_traj, d_dcf, ws, cs);
+    case 6: return launch_pipe_menon3<6>(s, l, iterations, d_traj, d_dcf, ws, cs);
+    case 8: return launch_pipe_menon3<8>(s, l, iterations, d_traj, d_dcf, ws, cs);
     default: return KSJ_GPU_ERROR_UNSUPPORTED;
   }
 }

@@ -93,6 +93,10 @@ def lib() -> ctypes.CDLL:
         L.ksj_gpu_gridding3_adjoint.restype = ctypes.c_int32
         L.ksj_gpu_gridding3_adjoint.argtypes = [ctypes.POINTER(Gridding3Desc), ctypes.POINTER(GriddingTuning), vp, vp,
                                                 vp, vp, vp, sz, vp]
+        L.ksj_gpu_pipe_menon3_workspace_bytes.restype = sz
+        L.ksj_gpu_pipe_menon3_workspace_bytes.argtypes = [ctypes.POINTER(Gridding3Desc)]
+        L.ksj_gpu_pipe_menon_dcf3.restype = ctypes.c_int32
+        L.ksj_gpu_pipe_menon_dcf3.argtypes = [ctypes.POINTER(Gridding3Desc), u32, vp, vp, vp, sz, vp]
         L.ksj_gpu_rss_coil_last.restype = ctypes.c_int32
         L.ksj_gpu_rss_coil_last.argtypes = [u64, u32, vp, vp, vp]
         L.ksj_gpu_launch_count.restype = u64
@@ -313,6 +317,22 @@ def pipe_menon_dcf(traj: torch.Tensor, image: int, grid: int, width: int = 4, it
     _check(L.ksj_gpu_pipe_menon_dcf(ctypes.byref(d), iterations, t.contiguous().data_ptr(), out.data_ptr(),
                                     ws.data_ptr(), ws.numel(), _stream(stream)), "pipe_menon_dcf")
     return out if traj.dim() == 3 else out[0]
+
+
+def pipe_menon_dcf3(traj: torch.Tensor, image: int, grid: int, width: int = 4, iterations: int = 10,
+                    stream=None) -> torch.Tensor:
+    """3-D Pipe-Menon weights: traj [M, 3] float32 on the GPU -> float32 [M]."""
+    m = traj.shape[0]
+    d = Gridding3(image=image, grid=grid, channels=1, samples=m, width=width).desc()
+    L = lib()
+    n = int(L.ksj_gpu_pipe_menon3_workspace_bytes(ctypes.byref(d)))
+    if n == 0:
+        raise GpuError(1, "pipe_menon3_workspace_bytes")
+    ws = torch.empty(n, dtype=torch.uint8, device=traj.device)
+    out = torch.empty(m, dtype=torch.float32, device=traj.device)
+    _check(L.ksj_gpu_pipe_menon_dcf3(ctypes.byref(d), iterations, traj.contiguous().data_ptr(), out.data_ptr(),
+                                     ws.data_ptr(), ws.numel(), _stream(stream)), "pipe_menon_dcf3")
+    return out
 
 
 def direct_adjoint(kspace: torch.Tensor, traj: torch.Tensor, rows: int, cols: int,

@@ -237,6 +237,18 @@ class Oracle(_Base):
             n, (n - 1) / 2.0, _p(samples), _p(traj), samples.shape[0], _p(out))
         return out
 
+    def pipe_menon_dcf3(self, traj: np.ndarray, grid: int, width: int = 4, beta: float | None = None,
+                        sigma: float = 1.5, iterations: int = 10) -> np.ndarray:
+        """3-D Pipe-Menon density compensation, grid-based, double precision."""
+        traj = np.ascontiguousarray(traj, dtype=np.float32).reshape(-1, 3)
+        if beta is None:
+            beta = self.kb_beta(width, sigma)
+        out = np.zeros(traj.shape[0], dtype=np.float64)
+        fn = self._fn("pipe_menon_dcf3_f64", ctypes.c_int, [_i64, ctypes.c_int, _dbl, _ptr, _i64, ctypes.c_int, _ptr])
+        if fn(grid, width, beta, _p(traj), traj.shape[0], iterations, _p(out)) != 0:
+            raise OracleError("3-D Pipe-Menon rejected its configuration")
+        return out
+
     def coil_covariance(self, x: np.ndarray, double: bool = False) -> np.ndarray:
         """Coil covariance of channel-major k-space x complex64 [C, M]: the
         reference's float arithmetic, or double precision."""

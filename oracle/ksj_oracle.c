@@ -780,3 +780,52 @@ KSJO_EXPORT void ksjo_direct_nudft3_adjoint_f64(int64_t n, double origin, const 
     image[p] = (cf64){re, im};
   }
 }
+
+/* The Pipe-Menon iteration of ksjo_pipe_menon_dcf2_f64 on a g^3 grid (taps
+ * per axis as the 3-D gridding; tap product (phi_z phi_y) phi_x, taps in
+ * z, y, x order).  traj float32 [m][3]; out double [m]. */
+KSJO_EXPORT int ksjo_pipe_menon_dcf3_f64(int64_t g, int width, double beta, const float* traj, int64_t m,
+                                         int iterations, double* out) {
+  if (width < 2 || width > 16 || g < width) return -1;
+  double* grid = (double*)malloc((size_t)(g * g * g) * sizeof(double));
+  int64_t* t0 = (int64_t*)malloc((size_t)(3 * m) * sizeof(int64_t));
+  double* wt = (double*)malloc((size_t)(3 * m * width) * sizeof(double));
+  if (!grid || !t0 || !wt) return -2;
+  for (int64_t s = 0; s < m; ++s) {
+    for (int d = 0; d < 3; ++d) {
+      const double u = (double)traj[3 * s + d] * (double)g / (2.0 * kPiD);
+      const int64_t t = (int64_t)floor(u) - width / 2 + 1;
+      t0[3 * s + d] = ((t % g) + g) % g;
+      for (int j = 0; j < width; ++j) wt[(3 * s + d) * width + j] = ksjo_kb_kernel((double)(t + j) - u, width, beta);
+    }
+    out[s] = 1.0;
+  }
+  for (int it = 0; it < iterations; ++it) {
+    memset(grid, 0, (size_t)(g * g * g) * sizeof(double));
+    for (int pass = 0; pass < 2; ++pass)
+      for (int64_t s = 0; s < m; ++s) {
+        const double* wz = wt + (3 * s) * width;
+        const double* wy = wt + (3 * s + 1) * width;
+        const double* wx = wt + (3 * s + 2) * width;
+        double d = 0.0;
+        for (int a = 0; a < width; ++a) {
+          const int64_t zz = (t0[3 * s] + a) % g;
+          for (int b = 0; b < width; ++b) {
+            const int64_t yy = (t0[3 * s + 1] + b) % g;
+            const double wzy = wz[a] * wy[b];
+            for (int c = 0; c < width; ++c) {
+              const int64_t xx = (t0[3 * s + 2] + c) % g;
+              double* cell = grid + (zz * g + yy) * g + xx;
+              if (pass == 0) *cell += out[s] * (wzy * wx[c]);
+              else d += *cell * (wzy * wx[c]);
+            }
+          }
+        }
+        if (pass == 1) out[s] = d > 0.0 ? out[s] / d : 0.0;
+      }
+  }
+  free(grid);
+  free(t0);
+  free(wt);
+  return 0;
+}

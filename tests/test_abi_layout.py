@@ -47,8 +47,9 @@ def _declared(header: Path, prefix: str) -> list[str]:
 
 def test_gpu_library_exports_every_declared_symbol(native):
     lib = ctypes.CDLL(str(native.GPU_LIB))
-    names = _declared(ROOT / "include/ksj_gpu.h", "ksj_gpu_")
-    assert len(names) >= 15
+    names = _declared(ROOT / "include/ksj_gpu.h", "ksj_gpu_") + _declared(ROOT / "include/ksj_gpu.h", "ksj_coil_")
+    names += _declared(ROOT / "include/ksj_serve.h", "ksj_serve_")
+    assert len(names) >= 30
     for n in names:
         assert hasattr(lib, n), n
 

@@ -53,3 +53,21 @@ def test_pipe_menon_is_deterministic_and_converges(native, cuda, orc):
     late = np.linalg.norm(steps[3] - steps[2]) / np.linalg.norm(steps[2])
     print(f"relative change: iteration 2->3 {early:.2e}, 9->10 {late:.2e}")
     assert late < early
+
+
+@pytest.mark.parametrize("n,g,width", [(16, 24, 4), (16, 32, 6)])
+def test_pipe_menon3_matches_fp64_oracle(native, cuda, orc, n, g, width):
+    """3-D Pipe-Menon (the kooshball configuration's density weights) against
+    the double-precision restatement, 10 iterations.  The oracle gets the
+    float32 kernel shape the GPU path uses."""
+    import torch
+    from kspacejet_gb300 import gpu, synth
+
+    tr = synth.kooshball(g, 300)
+    got = gpu.pipe_menon_dcf3(torch.from_numpy(tr).to(cuda), n, g, width=width).cpu().numpy()
+    beta = float(np.float32(orc.kb_beta(width, g / n)))
+    want = orc.pipe_menon_dcf3(tr, g, width, beta=beta)
+    err = oracle.rel_l2(got.astype(np.float64), want)
+    print(f"3-D Pipe-Menon {g}^3 W={width}: rel L2 {err:.2e}")
+    assert err <= TOL
+    assert np.all(got > 0)

@@ -88,3 +88,31 @@ def test_gridding3_tunings_agree(native, cuda):
         t = gpu.GriddingTuning(ctypes.sizeof(gpu.GriddingTuning), cg, 0, 0, fpp, rb, parts)
         got = _run(cuda, 16, 24, 4, tr, ks, gpu.OUTPUT_RSS, tuning=t)
         assert got.tobytes() == base.tobytes(), (cg, parts, rb, fpp)
+
+
+def test_gridding3_64_cube_subproblem(native, cuda, orc):
+    """The kooshball configuration's accuracy check on a 64^3 sub-problem
+    (sigma 1.5, W=4, 96 readout x 2000 spokes): against the FP64 Kaiser-Bessel
+    restatement on every voxel, and against the exact NUDFT (in double,
+    numpy) on 256 seeded voxels."""
+    from kspacejet_gb300 import gpu
+
+    n, g = 64, 96
+    tr, ks = _case(n, 96, 2000, 2, seed=64)
+    got = _run(cuda, n, g, 4, tr, ks, gpu.OUTPUT_COIL_LAST)[..., 0]
+    tr64 = tr.astype(np.float64)
+    dcf = np.sum(tr64 ** 2, axis=1)
+    ref = orc.kb_gridding3(g, n, ks[0].astype(np.complex128), tr64, dcf, width=4, sigma=g / n)
+    e_ref = oracle.rel_l2(got, ref)
+    rng = np.random.default_rng(3)
+    vox = rng.integers(0, n, size=(256, 3))
+    y = ks[0].astype(np.complex128) * dcf
+    exact = np.empty(256, dtype=np.complex128)
+    for i0 in range(0, 256, 32):
+        pos = vox[i0:i0 + 32].astype(np.float64) - (n - 1) / 2.0
+        exact[i0:i0 + 32] = np.exp(1j * (tr64 @ pos.T)).T @ y
+    approx = got[vox[:, 0], vox[:, 1], vox[:, 2]]
+    e_exact = np.linalg.norm(approx - exact) / np.linalg.norm(exact)
+    print(f"3-D 64^3 sub-problem: vs FP64 KB {e_ref:.2e}, vs exact NUDFT (256 voxels) {e_exact:.2e}")
+    assert e_ref <= TOL_FP64
+    assert e_exact <= TOL_EXACT[4]
