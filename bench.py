@@ -648,6 +648,12 @@ def run_rows(args) -> list[dict]:
                                      "workspace_bytes": ws3.numel()},
                           "kernels_ms": kern})
             del ws3, o3
+        # 3-D Pipe-Menon weights for the same trajectory (FP64, 10 iterations)
+        ms = _time_gpu(lambda: gpu.pipe_menon_dcf3(tr3, 256, 384, width=4, iterations=10), 1, max(1, min(s, 3)))
+        lines.append({"metric": "3-D Pipe-Menon weights: sample-iterations/s", "value": m3 * 10 / (ms / 1e3),
+                      "unit": "sample-iterations/s", "ms_per_call": ms, "dtype": "f64",
+                      "config": {"workload": f"256 x {args.spokes3} spokes kooshball, grid 384^3, KB W=4, "
+                                             "10 iterations", "samples": m3}})
 
     # Walsh 7x7 on the compressed 8-coil image (256 x 256), and RSS of 32 coils
     img = torch.from_numpy((rng.standard_normal((256, 256, 8)) + 1j * rng.standard_normal((256, 256, 8))).astype(np.complex64)).to(dev)
