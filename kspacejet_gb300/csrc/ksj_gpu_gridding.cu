@@ -60,6 +60,7 @@ constexpr int kMaxGrid = 512;
 constexpr int kMaxThreads = 512;
 constexpr int kColsThreads = 256;  // k_cols block size
 constexpr int kAhead = 8;         // coil loads in flight per warp in k_rows
+constexpr int kAheadRegs = 4;     // the same for the register-cell form (a shorter unrolled body)
 constexpr uint32_t kFlagBytes = 256;
 
 // Per (frame, sample) record written by k_prepare, read by k_rows.
@@ -828,6 +829,7 @@ struct RowsArgs {
   size_t entries_per_frame;
   int coil_group, coil_parts;
   int out_cols, cpitch;
+  int col_shift;  // kept column of frequency k: (k + col_shift) mod grid_cols, when below out_cols
   DifPlan plan;
 };
 
@@ -838,6 +840,143 @@ struct AccAddr {
   int cg;
   __device__ __forceinline__ int operator()(int coil, int col) const { return col * cg + coil; }
 };
+
+// Register form of one column chunk (lane = coil): r[t] is the cell of column
+// col_lo + t.  A straight entry's taps are the columns cbase + j, so with the
+// warp-uniform d = cbase - col_lo every tap is a compile-time register index
+// (one switch case per d).  Taps at t < 0 or t >= kChunk belong to other
+// lists' chunks and are dropped; taps at width <= t < kChunk (a partial last
+// chunk) land in registers that are never stored.
+template <int W, int D, int J = 0>
+__device__ __forceinline__ void chunk_taps_at(float2 (&r)[kChunk], float2 v, const float* wt) {
+  if constexpr (J < W) {
+    if constexpr (D + J >= 0 && D + J < kChunk) {
+      r[D + J].x = fmaf(v.x, wt[J], r[D + J].x);
+      r[D + J].y = fmaf(v.y, wt[J], r[D + J].y);
+    }
+    chunk_taps_at<W, D, J + 1>(r, v, wt);
+  }
+}
+
+template <int W>
+__device__ __forceinline__ void chunk_taps(float2 (&r)[kChunk], int d, float2 v, const float* wt) {
+  static_assert(W <= 8 && kChunk == 16, "cases cover d in [-7, 15]");
+  switch (d) {
+#define KSJ_TAPS_CASE(D) \
+  case D:                \
+    chunk_taps_at<W, D>(r, v, wt); \
+    break;
+    KSJ_TAPS_CASE(-7) KSJ_TAPS_CASE(-6) KSJ_TAPS_CASE(-5) KSJ_TAPS_CASE(-4) KSJ_TAPS_CASE(-3) KSJ_TAPS_CASE(-2)
+    KSJ_TAPS_CASE(-1) KSJ_TAPS_CASE(0) KSJ_TAPS_CASE(1) KSJ_TAPS_CASE(2) KSJ_TAPS_CASE(3) KSJ_TAPS_CASE(4)
+    KSJ_TAPS_CASE(5) KSJ_TAPS_CASE(6) KSJ_TAPS_CASE(7) KSJ_TAPS_CASE(8) KSJ_TAPS_CASE(9) KSJ_TAPS_CASE(10)
+    KSJ_TAPS_CASE(11) KSJ_TAPS_CASE(12) KSJ_TAPS_CASE(13) KSJ_TAPS_CASE(14) KSJ_TAPS_CASE(15)
+#undef KSJ_TAPS_CASE
+    default:
+      break;
+  }
+}
+
+// Entries whose taps wrap around the grid inside one chunk (grids of at most
+// one chunk): the in-chunk taps of the mask, each at its wrapped column.
+template <int W>
+__device__ __forceinline__ void chunk_taps_wrapped(float2 (&r)[kChunk], int c0, uint32_t mask, int col_lo,
+                                                   int grid_cols, float2 v, const float* wt) {
+#pragma unroll
+  for (int j = 0; j < W; ++j) {
+    if (!((mask >> j) & 1u)) continue;
+    int col = c0 + j;
+    if (col >= grid_cols) col -= grid_cols;
+    const int t = col - col_lo;
+#pragma unroll
+    for (int u = 0; u < kChunk; ++u) {
+      if (u == t) {
+        r[u].x = fmaf(v.x, wt[j], r[u].x);
+        r[u].y = fmaf(v.y, wt[j], r[u].y);
+      }
+    }
+  }
+}
+
+// Gridding of one row by whole 32-coil warps (lane = coil).  A task is one
+// column chunk: its cells stay in registers for the whole list, in the same
+// per-cell order (sample order, starting from zero) as the shared-memory form
+// in k_rows, and are stored once at its end.  Every chunk is a task, so every
+// cell of the row is stored (an empty list stores zeros).  kWrap admits
+// entries whose taps wrap around the grid inside the chunk.
+template <int W, uint32_t kFormat, bool kWrap>
+__device__ __forceinline__ void rows_grid_regs(const RowsArgs& a, int f, int cgi, int lane, float2* acc,
+                                               const uint32_t* offs, const int* task_chunk, int* task_next,
+                                               float4* meta) {
+  constexpr int kMV = meta_vecs(W);
+  constexpr int kBatch = meta_batch(W);
+  const int coil_global = cgi * 32 + lane;
+  const bool coil_ok = coil_global < a.channels;
+  const size_t sample_base = static_cast<size_t>(f) * a.sample_frame_stride + (coil_ok ? coil_global : 0);
+  const void* ks = a.samples_t;
+  for (;;) {
+    int task = 0;
+    if (lane == 0) task = atomicAdd(task_next, 1);
+    task = __shfl_sync(0xffffffffu, task, 0);
+    if (task >= a.nchunks) break;
+    const int chunk = task_chunk[task];
+    const uint32_t begin = offs[chunk];
+    const int n = static_cast<int>(offs[chunk + 1] - begin);
+    const float4* xent = a.expanded + (static_cast<size_t>(f) * a.entries_per_frame + begin) * kMV;
+    const int col_lo = chunk * kChunk;
+    float2 r[kChunk];
+#pragma unroll
+    for (int t = 0; t < kChunk; ++t) r[t] = make_float2(0.0f, 0.0f);
+    for (int base = 0; base < n; base += kBatch) {
+      const int cnt = min(kBatch, n - base);
+      __syncwarp();  // the previous batch is read by every lane before it is replaced
+      if (lane < cnt) {
+        const float4* src = xent + static_cast<size_t>(base + lane) * kMV;
+        float4* m = meta + lane * kMV;
+#pragma unroll
+        for (int v = 0; v < kMV; ++v) m[v] = __ldg(src + v);
+      }
+      __syncwarp();
+      auto fetch = [&](int i) {
+        const uint32_t sk = __float_as_uint(meta[i * kMV].y);
+        return load_sample<kFormat>(ks, sample_base + static_cast<size_t>(sk) * a.channels);
+      };
+      float2 yv[kAheadRegs];
+#pragma unroll
+      for (int k = 0; k < kAheadRegs; ++k) yv[k] = (coil_ok && k < cnt) ? fetch(k) : make_float2(0.0f, 0.0f);
+      for (int i0 = 0; i0 < cnt; i0 += kAheadRegs) {
+#pragma unroll
+        for (int k = 0; k < kAheadRegs; ++k) {
+          const int i = i0 + k;
+          if (i >= cnt) break;
+          const float2 y = yv[k];
+          yv[k] = (coil_ok && i + kAheadRegs < cnt) ? fetch(i + kAheadRegs) : make_float2(0.0f, 0.0f);
+          const float4 m0 = meta[i * kMV];
+          float wt[4 * (kMV - 1)];
+#pragma unroll
+          for (int v = 1; v < kMV; ++v) {
+            const float4 mv = meta[i * kMV + v];
+            wt[4 * (v - 1)] = mv.x;
+            wt[4 * (v - 1) + 1] = mv.y;
+            wt[4 * (v - 1) + 2] = mv.z;
+            wt[4 * (v - 1) + 3] = mv.w;
+          }
+          const int word0 = __float_as_int(m0.x);
+          const int cbase = word0 >> 9;  // arithmetic shift: may be negative
+          const float2 v = cmul(y, make_float2(m0.z, m0.w));
+          if (kWrap && (word0 & 256))
+            chunk_taps_wrapped<W>(r, cbase, static_cast<uint32_t>(word0) & 255u, col_lo, a.grid_cols, v, wt);
+          else
+            chunk_taps<W>(r, cbase - col_lo, v, wt);
+        }
+      }
+    }
+    const int width = min(kChunk, a.grid_cols - col_lo);
+    float2* dst = acc + static_cast<size_t>(col_lo) * 32 + lane;
+#pragma unroll
+    for (int t = 0; t < kChunk; ++t)
+      if (t < width) dst[t * 32] = r[t];
+  }
+}
 
 // kBlocks CTAs per SM: 2 for rows of up to 384 columns (384 threads), 1
 // above; two resident CTAs let one block's FFT overlap another's gridding.
@@ -891,10 +1030,20 @@ __global__ void __launch_bounds__(kThreads, kBlocks) k_rows(RowsArgs a) {
     if (lane < a.nchunks) task_chunk[lane] = key & 255;
     if (lane == 0) task_next = 0;
   }
-  for (int i = tid; i < a.grid_cols * cg; i += nthreads) acc[i] = make_float2(0.0f, 0.0f);
+  // (the 32-coil path stores every cell of the row from registers)
+  if (kCG != 32)
+    for (int i = tid; i < a.grid_cols * cg; i += nthreads) acc[i] = make_float2(0.0f, 0.0f);
   for (int i = tid; i < a.grid_cols; i += nthreads) tw[i] = a.tw_cols[i];
   __syncthreads();
 
+  if constexpr (kCG == 32) {
+    // taps wrap around the grid inside one chunk only on grids narrower than
+    // kChunk + W - 1 columns; the loop for those keeps a per-tap form
+    if (a.grid_cols < kChunk + W - 1)
+      rows_grid_regs<W, kFormat, true>(a, f, cgi, lane, acc, offs, task_chunk, &task_next, meta);
+    else
+      rows_grid_regs<W, kFormat, false>(a, f, cgi, lane, acc, offs, task_chunk, &task_next, meta);
+  } else {
   // ---- gridding.  A task is (column chunk, coil part): the chunk's sorted
   // list applied to a subset of the coil group.  Cells of different coils are
   // independent, so parts of one list may run on different warps with every
@@ -1006,19 +1155,28 @@ __global__ void __launch_bounds__(kThreads, kBlocks) k_rows(RowsArgs a) {
       }
     }
   }
+  }
   __syncthreads();
 
-  // ---- row inverse FFT of every coil line, in place (output digit-reversed)
+  // ---- row inverse FFT of every coil line; the kept columns are written
+  // coil-last: [frame][grid_row][out_col][channel]
   const int lg_cg = ilog2(cg);
-  dif_lines(acc, lg_cg, a.plan, tw, tid, nthreads);
+  float2* dst_row = a.inter + (static_cast<size_t>(f) * a.grid_rows + row) * a.out_cols * a.cpitch + cgi * cg;
+  const int live_lines = min(cg, a.channels - cgi * cg);
+  auto emit = [&](int k, int line, float2 v) {
+    int pc = k + a.col_shift;
+    if (pc >= a.grid_cols) pc -= a.grid_cols;
+    if (pc < a.out_cols && line < live_lines) dst_row[static_cast<size_t>(pc) * a.cpitch + line] = v;
+  };
+  // (blocks of kThreads threads take rows of up to kThreads columns)
+  if (fft_two_step_rows<kThreads>(a.grid_cols, acc, lg_cg, tw, tid, nthreads, emit)) return;
 
-  // ---- write the kept columns, coil-last: [frame][grid_row][out_col][channel]
+  // other lengths: in place (output digit-reversed), then the kept columns
+  dif_lines(acc, lg_cg, a.plan, tw, tid, nthreads);
   const int coil = tid & (cg - 1);
-  const int gc = cgi * cg + coil;
-  if (gc < a.channels) {
-    float2* dst = a.inter + (static_cast<size_t>(f) * a.grid_rows + row) * a.out_cols * a.cpitch + gc;
+  if (coil < live_lines) {
     for (int pc = tid >> lg_cg; pc < a.out_cols; pc += nthreads >> lg_cg)
-      dst[static_cast<size_t>(pc) * a.cpitch] = acc[(__ldg(a.pos_cols + pc) << lg_cg) + coil];
+      dst_row[static_cast<size_t>(pc) * a.cpitch + coil] = acc[(__ldg(a.pos_cols + pc) << lg_cg) + coil];
   }
 }
 
@@ -1359,6 +1517,7 @@ ksj_gpu_status launch_all(const Shape& s, const Layout& l, const ksj_gpu_griddin
   r.out_cols = s.out_cols;
   r.cpitch = s.cpitch;
   r.plan = s.plan_cols;
+  r.col_shift = s.kb ? s.out_cols / 2 : 0;
   const size_t rows_smem = rows_smem_bytes(s);
   const int rows_threads = rows_threads_for(s.grid_cols);
   const bool whole32 = s.coil_group == 32 && s.coil_parts == 1;
@@ -1964,6 +2123,7 @@ ksj_gpu_status launch_all3(const Shape& s, const Layout3& l, const ksj_gpu_gridd
   r.out_cols = n;
   r.cpitch = s.cpitch;
   r.plan = s.plan_cols;
+  r.col_shift = n / 2;
   const size_t rows_smem = rows_smem_bytes(s);
   const int rows_threads = rows_threads_for(g);
   const bool whole32 = s.coil_group == 32 && s.coil_parts == 1;

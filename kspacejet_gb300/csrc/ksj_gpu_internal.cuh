@@ -261,6 +261,159 @@ __device__ __forceinline__ void dft_inverse<6>(float2* v) {
   v[5] = o[2];
 }
 
+// cos(2 pi r / 96) for r in [0, 24] (a quarter turn), as double literals.
+__host__ __device__ constexpr double cos96(int r) {
+  switch (r) {
+    case 0: return 1.0;
+    case 1: return 0.9978589232386035;
+    case 2: return 0.9914448613738104;
+    case 3: return 0.9807852804032304;
+    case 4: return 0.9659258262890683;
+    case 5: return 0.9469301294951057;
+    case 6: return 0.9238795325112867;
+    case 7: return 0.8968727415326884;
+    case 8: return 0.8660254037844387;
+    case 9: return 0.8314696123025452;
+    case 10: return 0.7933533402912352;
+    case 11: return 0.7518398074789774;
+    case 12: return 0.7071067811865476;
+    case 13: return 0.6593458151000688;
+    case 14: return 0.6087614290087207;
+    case 15: return 0.5555702330196024;
+    case 16: return 0.5;
+    case 17: return 0.44228869021900125;
+    case 18: return 0.38268343236508984;
+    case 19: return 0.3214394653031617;
+    case 20: return 0.25881904510252074;
+    case 21: return 0.19509032201612833;
+    case 22: return 0.1305261922200517;
+    case 23: return 0.06540312923014327;
+    default: return 0.0;
+  }
+}
+
+// exp(2 pi i m / 96) for m in [0, 96): a whole number of quarter turns times
+// the first-quadrant value.  Called with m known at compile time (unrolled
+// loops), it folds to two float constants.
+__device__ __forceinline__ float2 omega96(int m) {
+  const int q = m / 24, r = m - 24 * (m / 24);
+  const float c = static_cast<float>(cos96(r)), s = static_cast<float>(cos96(24 - r));
+  switch (q & 3) {
+    case 0: return make_float2(c, s);
+    case 1: return make_float2(-s, c);
+    case 2: return make_float2(-c, -s);
+    default: return make_float2(s, -c);
+  }
+}
+
+// Two-factor split L = P * Q of the in-register DFT lengths above 8.
+template <int L>
+struct DftSplit;
+template <>
+struct DftSplit<12> { static constexpr int P = 3, Q = 4; };
+template <>
+struct DftSplit<16> { static constexpr int P = 4, Q = 4; };
+template <>
+struct DftSplit<24> { static constexpr int P = 3, Q = 8; };
+template <>
+struct DftSplit<32> { static constexpr int P = 4, Q = 8; };
+
+// In-place L-point inverse DFT on registers, natural order in and out.  For
+// L = P * Q > 8 (Cooley-Tukey, n = Q p + q, k = k1 + P k2): the P-point DFTs
+// over p of x[Q p + q], times exp(2 pi i q k1 / L), then the Q-point DFTs over
+// q give X[k1 + P k2].
+template <int L>
+__device__ __forceinline__ void dft_reg(float2* v) {
+  if constexpr (L == 2 || L == 3 || L == 4 || L == 6 || L == 8) {
+    dft_inverse<L>(v);
+  } else {
+    constexpr int P = DftSplit<L>::P, Q = DftSplit<L>::Q;
+    static_assert(96 % L == 0, "twiddles are multiples of 2 pi / 96");
+    float2 t[Q][P];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+#pragma unroll
+      for (int p = 0; p < P; ++p) t[q][p] = v[Q * p + q];
+      dft_inverse<P>(t[q]);
+    }
+#pragma unroll
+    for (int q = 1; q < Q; ++q) {
+#pragma unroll
+      for (int k1 = 1; k1 < P; ++k1) t[q][k1] = cmul(t[q][k1], omega96(q * k1 * (96 / L)));
+    }
+#pragma unroll
+    for (int k1 = 0; k1 < P; ++k1) {
+      float2 u[Q];
+#pragma unroll
+      for (int q = 0; q < Q; ++q) u[q] = t[q][k1];
+      dft_inverse<Q>(u);
+#pragma unroll
+      for (int k2 = 0; k2 < Q; ++k2) v[k1 + P * k2] = u[k2];
+    }
+  }
+}
+
+// Unnormalised inverse DFT (exp(+2 pi i n k / N)) of every line of a block
+// held in shared memory as [column][line] (lines = 1 << lg_lines), in two
+// steps for N = N1 * N2 (n = N2 n1 + n2, k = k1 + N1 k2):
+//   A  for each (n2, line): the N1-point DFT over n1 of x[N2 n1 + n2], times
+//      exp(2 pi i n2 k1 / N), written back in place at column N2 k1 + n2;
+//   B  for each (k1, line): the N2-point DFT over n2 of those N2 contiguous
+//      columns gives X[k1 + N1 k2], handed to emit(k, line, value) instead of
+//      being stored back.
+// tw[t] = exp(2 pi i t / N).  Synchronises the block between the steps; the
+// caller synchronises before (the block is complete) as needed after.
+template <int N1, int N2, typename Emit>
+__device__ __forceinline__ void fft_two_step(float2* smem, int lg_lines, const float2* __restrict__ tw, int tid,
+                                             int nthreads, Emit&& emit) {
+  const int lines = 1 << lg_lines;
+  for (int u = tid; u < N2 * lines; u += nthreads) {
+    const int line = u & (lines - 1), n2 = u >> lg_lines;
+    float2* e = smem + (n2 << lg_lines) + line;
+    float2 v[N1];
+#pragma unroll
+    for (int n1 = 0; n1 < N1; ++n1) v[n1] = e[(N2 * n1) << lg_lines];
+    dft_reg<N1>(v);
+#pragma unroll
+    for (int k1 = 1; k1 < N1; ++k1) v[k1] = cmul(v[k1], tw[n2 * k1]);
+#pragma unroll
+    for (int k1 = 0; k1 < N1; ++k1) e[(N2 * k1) << lg_lines] = v[k1];
+  }
+  __syncthreads();
+  for (int u = tid; u < N1 * lines; u += nthreads) {
+    const int line = u & (lines - 1), k1 = u >> lg_lines;
+    const float2* e = smem + ((N2 * k1) << lg_lines) + line;
+    float2 v[N2];
+#pragma unroll
+    for (int n2 = 0; n2 < N2; ++n2) v[n2] = e[n2 << lg_lines];
+    dft_reg<N2>(v);
+#pragma unroll
+    for (int k2 = 0; k2 < N2; ++k2) emit(k1 + N1 * k2, line, v[k2]);
+  }
+}
+
+// Row lengths up to kMaxN with a two-step form (N1 = 16): false for any other n.
+template <int kMaxN, typename Emit>
+__device__ __forceinline__ bool fft_two_step_rows(int n, float2* smem, int lg_lines, const float2* tw, int tid,
+                                                  int nthreads, Emit&& emit) {
+  switch (n) {
+    case 128: fft_two_step<16, 8>(smem, lg_lines, tw, tid, nthreads, emit); return true;
+    case 192: fft_two_step<16, 12>(smem, lg_lines, tw, tid, nthreads, emit); return true;
+    case 256: fft_two_step<16, 16>(smem, lg_lines, tw, tid, nthreads, emit); return true;
+    case 384: fft_two_step<16, 24>(smem, lg_lines, tw, tid, nthreads, emit); return true;
+    case 512:
+      if constexpr (kMaxN >= 512) {
+        fft_two_step<16, 32>(smem, lg_lines, tw, tid, nthreads, emit);
+        return true;
+      }
+      return false;
+    default: return false;
+  }
+}
+__host__ __device__ constexpr bool has_two_step_rows(int n) {
+  return n == 128 || n == 192 || n == 256 || n == 384 || n == 512;
+}
+
 // In-place mixed-radix decimation-in-frequency plan for n = 2^a 3^b (b <= 1):
 // a factor 3 first (as radix 6 when n is even), then radix-8 stages, then a
 // final 4 or 2, so every block length after the first stage is a power of
