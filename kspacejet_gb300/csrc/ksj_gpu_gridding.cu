@@ -313,7 +313,10 @@ __global__ void k_tables(float2* tw_rows, int grid_rows, float2* tw_cols, int gr
                          DifPlan plan_cols, int kb, int width, double beta, double i0_beta) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   auto source = [&](int p, int n, int g) { return kb ? (p - n / 2 + g) % g : p; };
-  if (i < out_rows) pos_rows[i] = dif_position(plan_rows, source(i, out_rows, grid_rows));
+  if (i < out_rows) {
+    const int k = source(i, out_rows, grid_rows);
+    pos_rows[i] = has_two_step_rows(grid_rows) ? two_step_slot(k, grid_rows) : dif_position(plan_rows, k);
+  }
   if (i < out_cols) pos_cols[i] = dif_position(plan_cols, source(i, out_cols, grid_cols));
   if (i < grid_rows) tw_rows[i] = twiddle(i, grid_rows);
   if (i < grid_cols) tw_cols[i] = twiddle(i, grid_cols);
@@ -1193,6 +1196,7 @@ struct ColsArgs {
   int box_rows, boxes;                  // TMA boxes of box_rows rows cover one tile
   uint32_t output;                      // RSS or COIL_LAST (COIL_MAJOR goes through COIL_LAST + transpose)
   int out_pitch;                        // COIL_LAST: elements between pixels of the output (>= channels)
+  int row_shift;                        // kept row of frequency k: (k + row_shift) mod grid_rows, when below out_rows
   DifPlan plan;
 };
 
@@ -1270,16 +1274,12 @@ __global__ void __launch_bounds__(kColsThreads) k_cols(const __grid_constant__ C
       break;
     }
     float2* tile = tiles + b * tile_elems;
-    dif_lines(tile, lg_lines, a.plan, tw, tid, nthreads);
     // crop and deapodise; coil-last images are written from here, RSS
-    // inputs are squared in place
-    const int gc = g * cgc + lcoil;
-    for (int pr = tid >> lg_lines; pr < a.out_rows; pr += nthreads >> lg_lines) {
-      if (!col_ok || gc >= a.channels) continue;
-      float2* e = tile + (static_cast<size_t>(__ldg(a.pos_rows + pr)) << lg_lines) + line;
-      float2 x = *e;
+    // inputs are squared in place at pos_rows[pr]
+    auto emit_pixel = [&](int pr, int ln, float2* e, float2 x) {
+      const int lc = ln >> lg_cgc;
       if (a.kb) {
-        const float sc = a.inv_dr[pr] * a.inv_dc[col0 + lcol];
+        const float sc = a.inv_dr[pr] * a.inv_dc[col0 + lc];
         x.x *= sc;
         x.y *= sc;
       }
@@ -1287,7 +1287,24 @@ __global__ void __launch_bounds__(kColsThreads) k_cols(const __grid_constant__ C
         e->x = __fadd_rn(__fmul_rn(x.x, x.x), __fmul_rn(x.y, x.y));
       } else {
         float2* o = static_cast<float2*>(a.out);
-        o[((static_cast<size_t>(fg) * a.out_rows + pr) * a.out_cols + col0 + lcol) * a.out_pitch + gc] = x;
+        o[((static_cast<size_t>(fg) * a.out_rows + pr) * a.out_cols + col0 + lc) * a.out_pitch + g * cgc +
+          (ln & (cgc - 1))] = x;
+      }
+    };
+    const int live_coils_g = min(cgc, a.channels - g * cgc);
+    auto emit = [&](int k, int ln, float2 v) {
+      int pr = k + a.row_shift;
+      if (pr >= a.grid_rows) pr -= a.grid_rows;
+      if (pr >= a.out_rows || col0 + (ln >> lg_cgc) >= a.out_cols || (ln & (cgc - 1)) >= live_coils_g) return;
+      emit_pixel(pr, ln, tile + (two_step_slot(k, a.grid_rows) << lg_lines) + ln, v);
+    };
+    if (!fft_two_step_rows<512>(a.grid_rows, tile, lg_lines, tw, tid, nthreads, emit)) {
+      dif_lines(tile, lg_lines, a.plan, tw, tid, nthreads);
+      if (col_ok && lcoil < live_coils_g) {
+        for (int pr = tid >> lg_lines; pr < a.out_rows; pr += nthreads >> lg_lines) {
+          float2* e = tile + (static_cast<size_t>(__ldg(a.pos_rows + pr)) << lg_lines) + line;
+          emit_pixel(pr, line, e, *e);
+        }
       }
     }
     if (a.output == KSJ_GPU_OUTPUT_RSS) {
@@ -1541,6 +1558,7 @@ ksj_gpu_status launch_all(const Shape& s, const Layout& l, const ksj_gpu_griddin
   c.out_rows = s.out_rows;
   c.out_cols = s.out_cols;
   c.kb = s.kb ? 1 : 0;
+  c.row_shift = s.kb ? s.out_rows / 2 : 0;
   c.column_block = s.column_block;
   c.col_group = s.col_group;
   c.groups = s.cpitch / s.col_group;
@@ -2152,6 +2170,7 @@ ksj_gpu_status launch_all3(const Shape& s, const Layout3& l, const ksj_gpu_gridd
   c.out_rows = n;
   c.out_cols = n;
   c.kb = 1;
+  c.row_shift = n / 2;
   c.column_block = s.column_block;
   c.col_group = s.col_group;
   c.groups = s.cpitch / s.col_group;

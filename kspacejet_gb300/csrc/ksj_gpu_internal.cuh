@@ -413,6 +413,9 @@ __device__ __forceinline__ bool fft_two_step_rows(int n, float2* smem, int lg_li
 __host__ __device__ constexpr bool has_two_step_rows(int n) {
   return n == 128 || n == 192 || n == 256 || n == 384 || n == 512;
 }
+// Column of X[k] when step B stores its outputs in place (over the N2
+// columns it read): N2 * (k mod 16) + k / 16.
+__host__ __device__ constexpr int two_step_slot(int k, int n) { return (k & 15) * (n >> 4) + (k >> 4); }
 
 // In-place mixed-radix decimation-in-frequency plan for n = 2^a 3^b (b <= 1):
 // a factor 3 first (as radix 6 when n is even), then radix-8 stages, then a
