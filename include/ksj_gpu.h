@@ -127,7 +127,8 @@ KSJ_GPU_API ksj_gpu_status ksj_gpu_gridding_adjoint(const ksj_gpu_gridding_desc*
 
 /* The sorted binning lists of the last call that used `d_workspace`, copied to
  * host memory: for every frame, list (grid_row, column_chunk) in row-major
- * order, the sample indices that touch it in increasing order.  out_offsets
+ * order, the sample indices that touch it in increasing order (read from the
+ * expanded entries the row pass consumes).  out_offsets
  * receives frames * lists + 1 entries (lists = grid_rows * chunks), out_samples
  * the concatenated indices.  Pass NULL arrays to query the sizes. */
 KSJ_GPU_API ksj_gpu_status ksj_gpu_gridding_binning(const ksj_gpu_gridding_desc* desc,

@@ -637,38 +637,40 @@ struct SortArgs {
   int dim3;                  // 3-D: frames are grid planes and the records are per sample (SampleRecord3)
 };
 
-// Expanded entries of list l of frame f, entries i = first, first + step, ...
+// Expanded entry i of list l of frame f (sample index sidx).
 template <int W>
-__device__ __forceinline__ void expand_list(const SortArgs& a, int f, int l, uint32_t begin, int n,
-                                            const uint32_t* sorted, int first, int step) {
+__device__ __forceinline__ void expand_at(const SortArgs& a, int f, int l, uint32_t begin, int i, uint32_t sidx) {
   constexpr int kMV = meta_vecs(W);
   const int row = l / a.nchunks;
   const int col_lo = (l - row * a.nchunks) * kChunk;
   const int col_hi = min(col_lo + kChunk, a.grid_cols);
-  float4* out = a.expanded + (static_cast<size_t>(f) * a.entries_per_frame + begin) * kMV;
-  if (a.dim3) {
-    const SampleRecord3<W>* recs = reinterpret_cast<const SampleRecord3<W>*>(a.records);
-    for (int i = first; i < n; i += step) {
-      float4 e[kMV];
-      expand_entry3<W>(recs, sorted[i], f, row, col_lo, col_hi, a.grid_cols, e);
+  float4* out = a.expanded + (static_cast<size_t>(f) * a.entries_per_frame + begin + i) * kMV;
+  float4 e[kMV];
+  if (a.dim3)
+    expand_entry3<W>(reinterpret_cast<const SampleRecord3<W>*>(a.records), sidx, f, row, col_lo, col_hi, a.grid_cols,
+                     e);
+  else
+    expand_entry<W>(reinterpret_cast<const SampleRecord<W>*>(a.records) + static_cast<size_t>(f) * a.samples, sidx, row,
+                    col_lo, col_hi, a.grid_rows, a.grid_cols, e);
 #pragma unroll
-      for (int v = 0; v < kMV; ++v) out[static_cast<size_t>(i) * kMV + v] = e[v];
-    }
-    return;
-  }
-  const SampleRecord<W>* recs = reinterpret_cast<const SampleRecord<W>*>(a.records) + static_cast<size_t>(f) * a.samples;
-  for (int i = first; i < n; i += step) {
-    float4 e[kMV];
-    expand_entry<W>(recs, sorted[i], row, col_lo, col_hi, a.grid_rows, a.grid_cols, e);
-#pragma unroll
-    for (int v = 0; v < kMV; ++v) out[static_cast<size_t>(i) * kMV + v] = e[v];
-  }
+  for (int v = 0; v < kMV; ++v) out[v] = e[v];
 }
 
-// Per list (one warp): sort the sample indices ascending in the warp's
-// shared buffer, then write every entry in its expanded form (the dependent
-// record loads happen here, across many lists in flight, not in the row
-// pass).  Lists longer than the buffer are queued for k_sort_long.
+// Expanded entries of list l of frame f, entries i = first, first + step, ...
+template <int W>
+__device__ __forceinline__ void expand_list(const SortArgs& a, int f, int l, uint32_t begin, int n,
+                                            const uint32_t* sorted, int first, int step) {
+  for (int i = first; i < n; i += step) expand_at<W>(a, f, l, begin, i, sorted[i]);
+}
+
+// Per list (one warp): sort the sample indices ascending, then write every
+// entry in its expanded form (the dependent record loads happen here, across
+// many lists in flight, not in the row pass).  A list of at most 32 entries
+// is ranked on registers: its sample indices are distinct, so the number of
+// smaller indices is each entry's sorted position.  Longer lists are sorted
+// in the warp's shared buffer; lists longer than the buffer are queued for
+// k_sort_long.  The sorted indices themselves are written back only for the
+// density-weight path (no expansion), the one reader of them.
 template <int W>
 __global__ void __launch_bounds__(256) k_sort(SortArgs a) {
   extern __shared__ uint32_t sort_buf[];
@@ -686,18 +688,27 @@ __global__ void __launch_bounds__(256) k_sort(SortArgs a) {
     return;
   }
   uint32_t* ent = a.entries + static_cast<size_t>(f) * a.entries_per_frame + begin;
-  const uint32_t* sorted = ent;
-  if (n >= 2) {
-    uint32_t* buf = sort_buf + static_cast<size_t>(warp) * a.capacity;
-    for (int i = lane; i < n; i += 32) buf[i] = ent[i];
-    __syncwarp();
-    warp_sort(buf, n, lane);
-    for (int i = lane; i < n; i += 32) ent[i] = buf[i];
-    sorted = buf;
-    __syncwarp();
+  if (n <= 32) {
+    const uint32_t key = lane < n ? ent[lane] : 0xffffffffu;
+    int rank = 0;
+    for (int j = 0; j < n; ++j) rank += __shfl_sync(0xffffffffu, key, j) < key ? 1 : 0;
+    if (lane < n) {
+      if (a.expanded == nullptr)
+        ent[rank] = key;  // every lane read its key before the shuffles
+      else
+        expand_at<W>(a, f, l, begin, rank, key);
+    }
+    return;
   }
-  if (a.expanded == nullptr) return;  // lists only (density compensation)
-  expand_list<W>(a, f, l, begin, n, sorted, lane, 32);
+  uint32_t* buf = sort_buf + static_cast<size_t>(warp) * a.capacity;
+  for (int i = lane; i < n; i += 32) buf[i] = ent[i];
+  __syncwarp();
+  warp_sort(buf, n, lane);
+  if (a.expanded == nullptr) {
+    for (int i = lane; i < n; i += 32) ent[i] = buf[i];
+    return;
+  }
+  expand_list<W>(a, f, l, begin, n, buf, lane, 32);
 }
 
 constexpr int kLongSortThreads = 1024;
@@ -737,7 +748,8 @@ __device__ __forceinline__ void sort_long_list(const SortArgs& a, size_t gl, uin
     for (int i = threadIdx.x; i < n; i += blockDim.x) long_buf[i] = ent[i];
     __syncthreads();
     block_sort(long_buf, n);
-    for (int i = threadIdx.x; i < n; i += blockDim.x) ent[i] = long_buf[i];
+    if (a.expanded == nullptr)
+      for (int i = threadIdx.x; i < n; i += blockDim.x) ent[i] = long_buf[i];
     sorted = long_buf;
   } else {
     block_sort(ent, n);
@@ -2450,9 +2462,11 @@ extern "C" ksj_gpu_status ksj_gpu_gridding_binning(const ksj_gpu_gridding_desc* 
     const uint32_t* fo = off.data() + static_cast<size_t>(f) * (s.lists_per_frame + 1);
     for (int i = 0; i < s.lists_per_frame; ++i)
       out_offsets[static_cast<size_t>(f) * s.lists_per_frame + i] = base + fo[i];
+    // the sample index of every expanded entry (second word of its first vector)
     const uint32_t n = fo[s.lists_per_frame];
-    if (n && cudaMemcpy(out_samples + base, ws + l.entries + static_cast<size_t>(f) * s.entries_per_frame * 4,
-                        static_cast<size_t>(n) * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
+    const size_t entry_bytes = static_cast<size_t>(meta_vecs(s.width)) * 16;
+    if (n && cudaMemcpy2D(out_samples + base, 4, ws + l.expanded + static_cast<size_t>(f) * s.entries_per_frame * entry_bytes + 4,
+                          entry_bytes, 4, n, cudaMemcpyDeviceToHost) != cudaSuccess)
       return KSJ_GPU_ERROR_CUDA;
     base += n;
   }
