@@ -663,7 +663,9 @@ __device__ __forceinline__ void expand_list(const SortArgs& a, int f, int l, uin
   for (int i = first; i < n; i += step) expand_at<W>(a, f, l, begin, i, sorted[i]);
 }
 
-// Per list (one warp): sort the sample indices ascending, then write every
+constexpr int kSortGroup = 4;  // consecutive lists per warp in k_sort
+
+// One list (one warp): sort the sample indices ascending, then write every
 // entry in its expanded form (the dependent record loads happen here, across
 // many lists in flight, not in the row pass).  A list of at most 32 entries
 // is ranked on registers: its sample indices are distinct, so the number of
@@ -672,19 +674,12 @@ __device__ __forceinline__ void expand_list(const SortArgs& a, int f, int l, uin
 // k_sort_long.  The sorted indices themselves are written back only for the
 // density-weight path (no expansion), the one reader of them.
 template <int W>
-__global__ void __launch_bounds__(256) k_sort(SortArgs a) {
-  extern __shared__ uint32_t sort_buf[];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const size_t gl = static_cast<size_t>(blockIdx.x) * (blockDim.x >> 5) + warp;
-  if (gl >= static_cast<size_t>(a.frames) * a.lists_per_frame) return;
-  const int f = static_cast<int>(gl / a.lists_per_frame);
-  const int l = static_cast<int>(gl - static_cast<size_t>(f) * a.lists_per_frame);
-  const uint32_t* off = a.offsets + static_cast<size_t>(f) * (a.lists_per_frame + 1);
-  const uint32_t begin = off[l];
-  const int n = static_cast<int>(off[l + 1] - begin);
+__device__ __forceinline__ void sort_list(const SortArgs& a, int f, int l, uint32_t begin, int n, int lane,
+                                          uint32_t* buf) {
   if (n == 0) return;
   if (n > a.capacity) {
-    if (lane == 0) a.long_lists[atomicAdd(a.long_count, 1u)] = static_cast<uint32_t>(gl);
+    if (lane == 0)
+      a.long_lists[atomicAdd(a.long_count, 1u)] = static_cast<uint32_t>(static_cast<size_t>(f) * a.lists_per_frame + l);
     return;
   }
   uint32_t* ent = a.entries + static_cast<size_t>(f) * a.entries_per_frame + begin;
@@ -700,7 +695,6 @@ __global__ void __launch_bounds__(256) k_sort(SortArgs a) {
     }
     return;
   }
-  uint32_t* buf = sort_buf + static_cast<size_t>(warp) * a.capacity;
   for (int i = lane; i < n; i += 32) buf[i] = ent[i];
   __syncwarp();
   warp_sort(buf, n, lane);
@@ -709,6 +703,59 @@ __global__ void __launch_bounds__(256) k_sort(SortArgs a) {
     return;
   }
   expand_list<W>(a, f, l, begin, n, buf, lane, 32);
+}
+
+// kSortGroup consecutive lists of one frame per warp.  Their entries are
+// contiguous; when there are at most 32 of them, lane i takes entry i of the
+// group, finds its list from the list starts and ranks it among that list's
+// entries (same order as sort_list), so tiny and empty lists share one warp.
+template <int W>
+__global__ void __launch_bounds__(256) k_sort(SortArgs a) {
+  extern __shared__ uint32_t sort_buf[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int groups = (a.lists_per_frame + kSortGroup - 1) / kSortGroup;
+  const size_t gg = static_cast<size_t>(blockIdx.x) * (blockDim.x >> 5) + warp;
+  if (gg >= static_cast<size_t>(a.frames) * groups) return;
+  const int f = static_cast<int>(gg / groups);
+  const int l0 = static_cast<int>(gg - static_cast<size_t>(f) * groups) * kSortGroup;
+  const int ng = min(kSortGroup, a.lists_per_frame - l0);
+  const uint32_t* off = a.offsets + static_cast<size_t>(f) * (a.lists_per_frame + 1) + l0;
+  const uint32_t my_off = lane <= ng ? off[lane] : 0u;  // lane s: start of list l0 + s
+  const uint32_t begin = __shfl_sync(0xffffffffu, my_off, 0);
+  const int total = static_cast<int>(__shfl_sync(0xffffffffu, my_off, ng) - begin);
+  if (total == 0) return;
+  if (total > 32) {
+    uint32_t* buf = sort_buf + static_cast<size_t>(warp) * a.capacity;
+    for (int s = 0; s < ng; ++s) {
+      const uint32_t b = __shfl_sync(0xffffffffu, my_off, s);
+      const uint32_t e = __shfl_sync(0xffffffffu, my_off, s + 1);
+      sort_list<W>(a, f, l0 + s, b, static_cast<int>(e - b), lane, buf);
+      __syncwarp();
+    }
+    return;
+  }
+  uint32_t* ent = a.entries + static_cast<size_t>(f) * a.entries_per_frame + begin;
+  const bool live = lane < total;
+  const uint32_t key = live ? ent[lane] : 0xffffffffu;
+  int seg = 0;  // list of entry `lane` within the group (empty lists are skipped over)
+#pragma unroll
+  for (int s = 1; s < kSortGroup; ++s) {
+    const uint32_t st = __shfl_sync(0xffffffffu, my_off, s);
+    if (s < ng && begin + lane >= st) seg = s;
+  }
+  int rank = 0;
+  for (int j = 0; j < total; ++j) {
+    const uint32_t kj = __shfl_sync(0xffffffffu, key, j);
+    const int sj = __shfl_sync(0xffffffffu, seg, j);
+    rank += (sj == seg && kj < key) ? 1 : 0;
+  }
+  const uint32_t lbegin = __shfl_sync(0xffffffffu, my_off, seg);
+  if (live) {
+    if (a.expanded == nullptr)
+      ent[lbegin - begin + rank] = key;  // every lane read its key before the shuffles
+    else
+      expand_at<W>(a, f, l0 + seg, lbegin, rank, key);
+  }
 }
 
 constexpr int kLongSortThreads = 1024;
@@ -782,7 +829,8 @@ ksj_gpu_status launch_sort(SortArgs sa, size_t lists, size_t entries_total, int 
     return KSJ_GPU_ERROR_CUDA;
   {
     LaunchScope scope("k_sort", stream);
-    k_sort<W><<<static_cast<unsigned>((lists + 7) / 8), 256, smem, stream>>>(sa);
+    const size_t warps = static_cast<size_t>(sa.frames) * ((sa.lists_per_frame + kSortGroup - 1) / kSortGroup);
+    k_sort<W><<<static_cast<unsigned>((warps + 7) / 8), 256, smem, stream>>>(sa);
   }
   const size_t most = std::max<size_t>(1, entries_total / (static_cast<size_t>(capacity) + 1));
   LaunchScope scope("k_sort_long", stream);
