@@ -1274,6 +1274,11 @@ constexpr uint32_t kWaitLimit = 1u << 22;  // mbarrier polls before a tile wait 
 // different coils (distinct banks) while each pixel still adds its coils
 // 0, 1, 2, ... in order: the result is bit-identical to the RSS of the coil
 // images.
+//
+// kN is the column length for the two-step transform (128 .. 512, see
+// has_two_step_rows), or 0 for the in-place mixed-radix form of any other
+// length; one instance per length keeps each kernel's code small.
+template <int kN>
 __global__ void __launch_bounds__(kColsThreads) k_cols(const __grid_constant__ CUtensorMap inter_map, ColsArgs a) {
   extern __shared__ __align__(16) unsigned char smem_cols[];
   unsigned char* smem_raw = smem_cols;
@@ -1297,6 +1302,7 @@ __global__ void __launch_bounds__(kColsThreads) k_cols(const __grid_constant__ C
   float* rss = reinterpret_cast<float*>(tw + a.grid_rows);
   const int npix = a.out_rows * cb;
   uint64_t* bars = reinterpret_cast<uint64_t*>(rss + ((npix + 1) & ~1));
+  float* inv_dr = reinterpret_cast<float*>(bars + 2);  // row deapodisation, out_rows values
   const uint32_t tile_bytes = static_cast<uint32_t>(static_cast<size_t>(a.grid_rows) * lines * sizeof(float2));
   if (tid == 0) {
     mbar_init(&bars[0], 1);
@@ -1305,6 +1311,8 @@ __global__ void __launch_bounds__(kColsThreads) k_cols(const __grid_constant__ C
   }
   for (int i = tid; i < a.grid_rows; i += nthreads) tw[i] = a.tw_rows[i];
   for (int i = tid; i < npix; i += nthreads) rss[i] = 0.0f;
+  if (a.kb)
+    for (int i = tid; i < a.out_rows; i += nthreads) inv_dr[i] = __ldg(a.inv_dr + i);
   __syncthreads();
   auto issue = [&](int g, int b) {
     float2* dst = tiles + b * tile_elems;
@@ -1339,7 +1347,7 @@ __global__ void __launch_bounds__(kColsThreads) k_cols(const __grid_constant__ C
     auto emit_pixel = [&](int pr, int ln, float2* e, float2 x) {
       const int lc = ln >> lg_cgc;
       if (a.kb) {
-        const float sc = a.inv_dr[pr] * a.inv_dc[col0 + lc];
+        const float sc = inv_dr[pr] * __ldg(a.inv_dc + col0 + lc);
         x.x *= sc;
         x.y *= sc;
       }
@@ -1358,7 +1366,9 @@ __global__ void __launch_bounds__(kColsThreads) k_cols(const __grid_constant__ C
       if (pr >= a.out_rows || col0 + (ln >> lg_cgc) >= a.out_cols || (ln & (cgc - 1)) >= live_coils_g) return;
       emit_pixel(pr, ln, tile + (two_step_slot(k, a.grid_rows) << lg_lines) + ln, v);
     };
-    if (!fft_two_step_rows<512>(a.grid_rows, tile, lg_lines, tw, tid, nthreads, emit)) {
+    if constexpr (kN != 0) {
+      fft_two_step<16, kN / 16>(tile, lg_lines, tw, tid, nthreads, emit);
+    } else {
       dif_lines(tile, lg_lines, a.plan, tw, tid, nthreads);
       if (col_ok && lcoil < live_coils_g) {
         for (int pr = tid >> lg_lines; pr < a.out_rows; pr += nthreads >> lg_lines) {
@@ -1421,7 +1431,27 @@ size_t cols_smem_bytes(const Shape& s) {
   const int nbuf = s.cpitch / s.col_group > 1 ? 2 : 1;
   const size_t npix = static_cast<size_t>(s.out_rows) * s.column_block;
   return 128 + nbuf * tile * sizeof(float2) + s.grid_rows * sizeof(float2) + ((npix + 1) & ~size_t{1}) * sizeof(float) +
-         2 * sizeof(uint64_t);
+         2 * sizeof(uint64_t) + static_cast<size_t>(s.out_rows) * sizeof(float);
+}
+
+using ColsKernel = void (*)(const __grid_constant__ CUtensorMap, ColsArgs);
+
+// The k_cols instance for columns of n grid rows.
+ColsKernel cols_kernel_for(int n) {
+  switch (n) {
+    case 128: return k_cols<128>;
+    case 192: return k_cols<192>;
+    case 256: return k_cols<256>;
+    case 384: return k_cols<384>;
+    case 512: return k_cols<512>;
+    default: return k_cols<0>;
+  }
+}
+
+// Opt a k_cols instance into its dynamic shared memory.
+bool cols_kernel_setup(ColsKernel k, size_t smem) {
+  return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)) == cudaSuccess &&
+         cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100) == cudaSuccess;
 }
 
 using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
@@ -1630,10 +1660,8 @@ ksj_gpu_status launch_all(const Shape& s, const Layout& l, const ksj_gpu_griddin
   CUtensorMap map;
   if (!make_inter_map(s, inter, &map, &c.box_rows, &c.boxes)) return KSJ_GPU_ERROR_CUDA;
   const size_t cols_smem = cols_smem_bytes(s);
-  if (cudaFuncSetAttribute(k_cols, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(cols_smem)) !=
-          cudaSuccess ||
-      cudaFuncSetAttribute(k_cols, cudaFuncAttributePreferredSharedMemoryCarveout, 100) != cudaSuccess)
-    return KSJ_GPU_ERROR_CUDA;
+  const ColsKernel cols_kernel = cols_kernel_for(s.grid_rows);
+  if (!cols_kernel_setup(cols_kernel, cols_smem)) return KSJ_GPU_ERROR_CUDA;
 
   // frames in passes sized so one pass's row-transformed grid stays in L2
   for (int f0 = 0; f0 < s.frames; f0 += s.frames_per_pass) {
@@ -1648,7 +1676,7 @@ ksj_gpu_status launch_all(const Shape& s, const Layout& l, const ksj_gpu_griddin
     {
       LaunchScope scope("k_cols", stream);
       const dim3 grid((s.out_cols + s.column_block - 1) / s.column_block, nf);
-      k_cols<<<grid, kColsThreads, cols_smem, stream>>>(map, c);
+      cols_kernel<<<grid, kColsThreads, cols_smem, stream>>>(map, c);
     }
   }
   if (coil_major) {
@@ -2213,10 +2241,8 @@ ksj_gpu_status launch_all3(const Shape& s, const Layout3& l, const ksj_gpu_gridd
       cudaFuncSetAttribute(rows_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100) != cudaSuccess)
     return KSJ_GPU_ERROR_CUDA;
   const size_t cols_smem = cols_smem_bytes(s);
-  if (cudaFuncSetAttribute(k_cols, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(cols_smem)) !=
-          cudaSuccess ||
-      cudaFuncSetAttribute(k_cols, cudaFuncAttributePreferredSharedMemoryCarveout, 100) != cudaSuccess)
-    return KSJ_GPU_ERROR_CUDA;
+  const ColsKernel cols_kernel = cols_kernel_for(s.grid_rows);
+  if (!cols_kernel_setup(cols_kernel, cols_smem)) return KSJ_GPU_ERROR_CUDA;
   // columns of every plane (y transformed, cropped, y/x deapodised): [plane][pixel][cpitch]
   ColsArgs c{};
   c.tw_rows = tw_rows;
@@ -2250,7 +2276,7 @@ ksj_gpu_status launch_all3(const Shape& s, const Layout3& l, const ksj_gpu_gridd
     }
     {
       LaunchScope scope("k_cols", stream);
-      k_cols<<<dim3((n + s.column_block - 1) / s.column_block, nf), kColsThreads, cols_smem, stream>>>(map, c);
+      cols_kernel<<<dim3((n + s.column_block - 1) / s.column_block, nf), kColsThreads, cols_smem, stream>>>(map, c);
     }
   }
   // z: the column pass over [plane][pixel][cpitch] with planes as rows and pixels as columns
@@ -2269,7 +2295,7 @@ ksj_gpu_status launch_all3(const Shape& s, const Layout3& l, const ksj_gpu_gridd
   cz.out_pitch = s.channels;
   {
     LaunchScope scope("k_cols_z", stream);
-    k_cols<<<dim3((n * n + s.column_block - 1) / s.column_block, 1), kColsThreads, cols_smem, stream>>>(zmap, cz);
+    cols_kernel<<<dim3((n * n + s.column_block - 1) / s.column_block, 1), kColsThreads, cols_smem, stream>>>(zmap, cz);
   }
   return check_launch();
 }
