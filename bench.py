@@ -622,6 +622,29 @@ def run_rows(args) -> list[dict]:
                   "roofline": {"bound": "hbm", "achieved": round(byts / (ms / 1e3) / 1e9, 1), "peak": hbm,
                                "unit": "GB/s", "frac": round(byts / (ms / 1e3) / 1e9 / hbm, 4)}})
 
+    # noise model from 32 x 65536 noise samples (covariance on the tensor cores, eigensolve on the
+    # host) and prewhitening Y = W X of the same 32 x 412 160 k-space
+    mn = 65536
+    noise = torch.from_numpy((rng.standard_normal((32, mn)) + 1j * rng.standard_normal((32, mn))).astype(np.complex64)).to(dev)
+    ms = _time_gpu(lambda: gpu.noise_model(noise), w, s)
+    lines.append({"metric": "noise model estimate: noise samples/s", "value": mn / (ms / 1e3), "unit": "samples/s",
+                  "ms_per_call": ms, "dtype": "bf16 x3 split covariance, f64 host eigensolve",
+                  "config": {"workload": "32 coils x 65536 noise samples, whitening matrix to the device"}})
+    wd = gpu.noise_model(noise)
+    yw = torch.empty((32, mm), dtype=torch.complex64, device=dev)
+
+    def prewhiten():
+        gpu._check(L.ksj_gpu_noise_prewhiten(32, mm, wd.data_ptr(), x.data_ptr(), yw.data_ptr(),
+                                             torch.cuda.current_stream().cuda_stream), "noise_prewhiten")
+
+    ms = _time_gpu(prewhiten, w, s)
+    byts = 2 * 32 * mm * 8
+    lines.append({"metric": "noise prewhitening 32x32: samples/s", "value": mm / (ms / 1e3), "unit": "samples/s",
+                  "ms_per_call": ms, "dtype": "f32",
+                  "config": {"workload": "32 coils x 512 x 805 samples (complex64)"},
+                  "roofline": {"bound": "hbm", "achieved": round(byts / (ms / 1e3) / 1e9, 1), "peak": hbm,
+                               "unit": "GB/s", "frac": round(byts / (ms / 1e3) / 1e9 / hbm, 4)}})
+
     # 3-D kooshball: 256 readout x `spokes3` Fibonacci spokes, 20 coils, grid 384^3 (sigma 1.5), KB W=4,
     # |k|^2 density weights, RSS; complex64 and bf16 sample storage
     if args.spokes3 > 0:

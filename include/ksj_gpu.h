@@ -289,6 +289,32 @@ KSJ_GPU_API ksj_gpu_status ksj_gpu_coil_covariance(uint32_t channels, uint32_t s
 KSJ_GPU_API ksj_gpu_status ksj_coil_compression_basis(uint32_t channels, uint32_t virtual_channels,
                                                       const void* covariance, void* basis, float* eigenvalues);
 
+/* Noise covariance of noise_model_estimate.cpp:161-162 (population
+ * normalisation, channel means removed, the reference's convention
+ * C(r, c) = (1/M) sum_s conj(x_r - mu_r) (x_c - mu_c), moments.hpp:99-140)
+ * of channel-major noise samples complex64 [channels][samples] -> d_cov
+ * complex64 [channels][channels], Hermitian.  The product sums run on the
+ * tensor cores as in ksj_gpu_coil_covariance (split BF16, FP32 accumulate);
+ * the means are removed afterwards as mu_r conj(mu_c).  channels <= 32.
+ * Workspace: ksj_gpu_coil_covariance_workspace_bytes. */
+KSJ_GPU_API ksj_gpu_status ksj_gpu_noise_covariance(uint32_t channels, uint32_t samples, const void* d_noise,
+                                                    void* d_cov, void* d_workspace, size_t workspace_bytes,
+                                                    void* stream);
+
+/* Host: the whitening matrix of a noise covariance (host complex64 [C][C],
+ * lower triangle read and mirrored), noise_model_estimate.cpp:163-167 and
+ * whitening.hpp:27-51: W = V diag(1 / sqrt(max(lambda, floor))) V^H by
+ * double-precision cyclic Jacobi; the reference's floor is 1e-6.  whitening:
+ * host complex64 [channels][channels].  channels <= 64. */
+KSJ_GPU_API ksj_gpu_status ksj_whitening_matrix(uint32_t channels, const void* covariance, float eigenvalue_floor,
+                                                void* whitening);
+
+/* Y = W X (noncartesian_noise_prewhiten.cpp:140-146): d_whitening complex64
+ * [channels][channels], d_kspace complex64 [channels][samples] -> d_out
+ * complex64 [channels][samples].  channels <= 32. */
+KSJ_GPU_API ksj_gpu_status ksj_gpu_noise_prewhiten(uint32_t channels, uint32_t samples, const void* d_whitening,
+                                                   const void* d_kspace, void* d_out, void* stream);
+
 /* Y = B X (noncartesian_coil_compress.cpp:143-148): d_basis complex64
  * [virtual][channels], d_kspace complex64 [channels][samples] ->
  * d_out complex64 [virtual][samples].  channels <= 32, virtual <= 16. */

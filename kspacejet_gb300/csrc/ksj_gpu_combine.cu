@@ -397,6 +397,55 @@ __global__ void __launch_bounds__(256) k_cov_form(const float* d, int channels, 
   cov[idx] = make_float2(re * inv_m, (i >= j ? im : -im) * inv_m);
 }
 
+// Per-channel mean of channel-major X [channels][samples] (one block per
+// channel, a fixed-order tree over the block: deterministic), as
+// covariance_channel_major_with_workspace forms it (moments.hpp:117-123).
+__global__ void __launch_bounds__(256) k_channel_means(const float2* __restrict__ x, int samples, float2* means) {
+  __shared__ float2 part[256];
+  const float2* row = x + static_cast<size_t>(blockIdx.x) * samples;
+  float2 acc = make_float2(0.0f, 0.0f);
+  for (int s = threadIdx.x; s < samples; s += blockDim.x) {
+    const float2 v = __ldg(row + s);
+    acc.x += v.x;
+    acc.y += v.y;
+  }
+  part[threadIdx.x] = acc;
+  __syncthreads();
+  for (int h = blockDim.x >> 1; h > 0; h >>= 1) {
+    if (threadIdx.x < h) {
+      part[threadIdx.x].x += part[threadIdx.x + h].x;
+      part[threadIdx.x].y += part[threadIdx.x + h].y;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const float inv = 1.0f / static_cast<float>(samples);
+    means[blockIdx.x] = make_float2(part[0].x * inv, part[0].y * inv);
+  }
+}
+
+// The noise covariance of noise_model_estimate.cpp:161-162
+// (covariance_channel_major_with_workspace, population normalisation,
+// moments.hpp:99-140): C(r, c) = (1/M) sum_s conj(x_r - mu_r) (x_c - mu_c)
+// = conj(R(r, c) - mu_r conj(mu_c)) with R = (1/M) X X^H as k_cov_form
+// forms it.  The lower triangle is computed and the upper mirrored, so C is
+// Hermitian bit for bit.
+__global__ void __launch_bounds__(256) k_noise_form(const float* d, int channels, float inv_m,
+                                                    const float2* __restrict__ means, float2* cov) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= channels * channels) return;
+  const int i = idx / channels, j = idx - (idx / channels) * channels;
+  auto g = [&](int r, int c) { return d[r * 64 + c] + d[(64 + r) * 64 + c] + d[(64 + c) * 64 + r]; };
+  const int r = i >= j ? i : j, c = i >= j ? j : i;
+  const float rre = (g(r, c) + g(32 + r, 32 + c)) * inv_m;
+  const float rim = r == c ? 0.0f : (g(32 + r, c) - g(r, 32 + c)) * inv_m;
+  const float2 mr = means[r], mc = means[c];
+  // d = R(r, c) - mu_r conj(mu_c)
+  const float dre = rre - (mr.x * mc.x + mr.y * mc.y);
+  const float dim = r == c ? 0.0f : rim - (mr.y * mc.x - mr.x * mc.y);
+  cov[idx] = make_float2(dre, i >= j ? -dim : dim);  // C(r, c) = conj(d); C(c, r) = d
+}
+
 using EncodeTiled2Fn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                     const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                                     CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
@@ -414,7 +463,7 @@ EncodeTiled2Fn cov_encode() {
 }
 
 struct CovLayout {
-  size_t flags, operand, partials, sum, total;
+  size_t flags, operand, partials, sum, means, total;
   int kpad, ktiles, blocks;
 };
 
@@ -433,6 +482,7 @@ CovLayout cov_layout(uint32_t samples) {
   l.operand = take(static_cast<size_t>(kCovRows) * l.kpad * 2);
   l.partials = take(static_cast<size_t>(l.blocks) * kCovRows * 64 * sizeof(float));
   l.sum = take(static_cast<size_t>(kCovRows) * 64 * sizeof(float));
+  l.means = take(32 * sizeof(float2));
   l.total = off;
   return l;
 }
@@ -445,10 +495,14 @@ extern "C" size_t ksj_gpu_coil_covariance_workspace_bytes(uint32_t channels, uin
   return ksj_gpu::cov_layout(samples).total;
 }
 
-extern "C" ksj_gpu_status ksj_gpu_coil_covariance(uint32_t channels, uint32_t samples, const void* d_kspace,
-                                                  void* d_cov, void* d_workspace, size_t workspace_bytes,
-                                                  void* stream) {
-  using namespace ksj_gpu;
+namespace ksj_gpu {
+namespace {
+
+// X [channels][samples] -> the summed split-BF16 products (tensor cores), then
+// either R = (1/M) X X^H (noise = false) or the mean-removed noise covariance
+// in the reference's convention (noise = true) into d_cov.
+ksj_gpu_status covariance_run(uint32_t channels, uint32_t samples, const void* d_kspace, void* d_cov,
+                              void* d_workspace, size_t workspace_bytes, void* stream, bool noise) {
   if (channels == 0 || channels > 32 || samples == 0 || samples > (1u << 28) || d_kspace == nullptr ||
       d_cov == nullptr || (reinterpret_cast<uintptr_t>(d_kspace) & 7u) != 0 ||
       (reinterpret_cast<uintptr_t>(d_cov) & 7u) != 0)
@@ -494,13 +548,38 @@ extern "C" ksj_gpu_status ksj_gpu_coil_covariance(uint32_t channels, uint32_t sa
     LaunchScope scope("k_cov_sum", cs);
     k_cov_sum<<<kCovRows * 64 / 256, 256, 0, cs>>>(partials, l.blocks, sum);
   }
-  {
-    const int n = static_cast<int>(channels * channels);
+  const int n = static_cast<int>(channels * channels);
+  const float inv_m = 1.0f / static_cast<float>(samples);
+  if (noise) {
+    float2* means = reinterpret_cast<float2*>(ws + l.means);
+    {
+      LaunchScope scope("k_channel_means", cs);
+      k_channel_means<<<channels, 256, 0, cs>>>(static_cast<const float2*>(d_kspace), static_cast<int>(samples),
+                                                means);
+    }
+    LaunchScope scope("k_noise_form", cs);
+    k_noise_form<<<(n + 255) / 256, 256, 0, cs>>>(sum, static_cast<int>(channels), inv_m, means,
+                                                  static_cast<float2*>(d_cov));
+  } else {
     LaunchScope scope("k_cov_form", cs);
-    k_cov_form<<<(n + 255) / 256, 256, 0, cs>>>(sum, static_cast<int>(channels), 1.0f / static_cast<float>(samples),
-                                                static_cast<float2*>(d_cov));
+    k_cov_form<<<(n + 255) / 256, 256, 0, cs>>>(sum, static_cast<int>(channels), inv_m, static_cast<float2*>(d_cov));
   }
   return check_launch();
+}
+
+}  // namespace
+}  // namespace ksj_gpu
+
+extern "C" ksj_gpu_status ksj_gpu_coil_covariance(uint32_t channels, uint32_t samples, const void* d_kspace,
+                                                  void* d_cov, void* d_workspace, size_t workspace_bytes,
+                                                  void* stream) {
+  return ksj_gpu::covariance_run(channels, samples, d_kspace, d_cov, d_workspace, workspace_bytes, stream, false);
+}
+
+extern "C" ksj_gpu_status ksj_gpu_noise_covariance(uint32_t channels, uint32_t samples, const void* d_noise,
+                                                   void* d_cov, void* d_workspace, size_t workspace_bytes,
+                                                   void* stream) {
+  return ksj_gpu::covariance_run(channels, samples, d_noise, d_cov, d_workspace, workspace_bytes, stream, true);
 }
 
 // ------------------------------------------------- coil compression basis and apply
@@ -650,6 +729,64 @@ extern "C" ksj_gpu_status ksj_gpu_coil_compress(uint32_t channels, uint32_t virt
     KSJ_COMPRESS_CASE(9) KSJ_COMPRESS_CASE(10) KSJ_COMPRESS_CASE(11) KSJ_COMPRESS_CASE(12)
     KSJ_COMPRESS_CASE(13) KSJ_COMPRESS_CASE(14) KSJ_COMPRESS_CASE(15) KSJ_COMPRESS_CASE(16)
 #undef KSJ_COMPRESS_CASE
+    default: return KSJ_GPU_ERROR_UNSUPPORTED;
+  }
+}
+
+// Whitening matrix of a noise covariance (noise_model_estimate.cpp:163-167,
+// whitening.hpp:27-51): W = V diag(1 / sqrt(max(lambda, floor))) V^H over the
+// eigenpairs of the Hermitian covariance (double-precision cyclic Jacobi),
+// W(r, c) = sum_k V(r, k) / sqrt(max(lambda_k, floor)) conj(V(c, k)).
+extern "C" ksj_gpu_status ksj_whitening_matrix(uint32_t channels, const void* covariance, float eigenvalue_floor,
+                                               void* whitening) {
+  if (channels == 0 || channels > 64 || covariance == nullptr || whitening == nullptr || !(eigenvalue_floor > 0.0f))
+    return KSJ_GPU_ERROR_INVALID_ARGUMENT;
+  const int n = static_cast<int>(channels);
+  const float* cov = static_cast<const float*>(covariance);
+  std::vector<std::complex<double>> a(static_cast<size_t>(n) * n), vec(static_cast<size_t>(n) * n);
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) {
+      const int lo = i >= j ? i * n + j : j * n + i;
+      const std::complex<double> v(cov[2 * lo], cov[2 * lo + 1]);
+      if (!std::isfinite(v.real()) || !std::isfinite(v.imag())) return KSJ_GPU_ERROR_NONFINITE_INPUT;
+      a[static_cast<size_t>(i) * n + j] = i >= j ? v : std::conj(v);
+    }
+  hermitian_jacobi(n, a.data(), vec.data());
+  std::vector<double> scale(static_cast<size_t>(n));
+  for (int k = 0; k < n; ++k)
+    scale[k] = 1.0 / std::sqrt(std::max(a[static_cast<size_t>(k) * n + k].real(), static_cast<double>(eigenvalue_floor)));
+  float* out = static_cast<float*>(whitening);
+  for (int r = 0; r < n; ++r)
+    for (int c = 0; c < n; ++c) {
+      std::complex<double> sum = 0.0;
+      for (int k = 0; k < n; ++k)
+        sum += vec[static_cast<size_t>(r) * n + k] * scale[k] * std::conj(vec[static_cast<size_t>(c) * n + k]);
+      out[2 * (r * n + c)] = static_cast<float>(sum.real());
+      out[2 * (r * n + c) + 1] = static_cast<float>(sum.imag());
+    }
+  return KSJ_GPU_OK;
+}
+
+// Y = W X (noncartesian_noise_prewhiten.cpp:140-146): the square form of the
+// compression apply, W complex64 [channels][channels].
+extern "C" ksj_gpu_status ksj_gpu_noise_prewhiten(uint32_t channels, uint32_t samples, const void* d_whitening,
+                                                  const void* d_kspace, void* d_out, void* stream) {
+  if (channels == 0 || channels > 32 || samples == 0 || d_whitening == nullptr || d_kspace == nullptr ||
+      d_out == nullptr)
+    return KSJ_GPU_ERROR_INVALID_ARGUMENT;
+  cudaStream_t cs = static_cast<cudaStream_t>(stream);
+  switch (channels) {
+#define KSJ_WHITEN_CASE(V) \
+  case V: return launch_compress<V>(channels, samples, d_whitening, d_kspace, d_out, cs);
+    KSJ_WHITEN_CASE(1) KSJ_WHITEN_CASE(2) KSJ_WHITEN_CASE(3) KSJ_WHITEN_CASE(4)
+    KSJ_WHITEN_CASE(5) KSJ_WHITEN_CASE(6) KSJ_WHITEN_CASE(7) KSJ_WHITEN_CASE(8)
+    KSJ_WHITEN_CASE(9) KSJ_WHITEN_CASE(10) KSJ_WHITEN_CASE(11) KSJ_WHITEN_CASE(12)
+    KSJ_WHITEN_CASE(13) KSJ_WHITEN_CASE(14) KSJ_WHITEN_CASE(15) KSJ_WHITEN_CASE(16)
+    KSJ_WHITEN_CASE(17) KSJ_WHITEN_CASE(18) KSJ_WHITEN_CASE(19) KSJ_WHITEN_CASE(20)
+    KSJ_WHITEN_CASE(21) KSJ_WHITEN_CASE(22) KSJ_WHITEN_CASE(23) KSJ_WHITEN_CASE(24)
+    KSJ_WHITEN_CASE(25) KSJ_WHITEN_CASE(26) KSJ_WHITEN_CASE(27) KSJ_WHITEN_CASE(28)
+    KSJ_WHITEN_CASE(29) KSJ_WHITEN_CASE(30) KSJ_WHITEN_CASE(31) KSJ_WHITEN_CASE(32)
+#undef KSJ_WHITEN_CASE
     default: return KSJ_GPU_ERROR_UNSUPPORTED;
   }
 }

@@ -88,6 +88,12 @@ def lib() -> ctypes.CDLL:
         L.ksj_coil_compression_basis.argtypes = [u32, u32, vp, vp, vp]
         L.ksj_gpu_coil_compress.restype = ctypes.c_int32
         L.ksj_gpu_coil_compress.argtypes = [u32, u32, u32, vp, vp, vp, vp]
+        L.ksj_gpu_noise_covariance.restype = ctypes.c_int32
+        L.ksj_gpu_noise_covariance.argtypes = [u32, u32, vp, vp, vp, sz, vp]
+        L.ksj_whitening_matrix.restype = ctypes.c_int32
+        L.ksj_whitening_matrix.argtypes = [u32, vp, ctypes.c_float, vp]
+        L.ksj_gpu_noise_prewhiten.restype = ctypes.c_int32
+        L.ksj_gpu_noise_prewhiten.argtypes = [u32, u32, vp, vp, vp, vp]
         L.ksj_gpu_gridding3_workspace_bytes.restype = sz
         L.ksj_gpu_gridding3_workspace_bytes.argtypes = [ctypes.POINTER(Gridding3Desc)]
         L.ksj_gpu_gridding3_adjoint.restype = ctypes.c_int32
@@ -391,6 +397,54 @@ def coil_compress(basis: torch.Tensor, kspace: torch.Tensor, stream=None) -> tor
     out = torch.empty((v, m), dtype=torch.complex64, device=kspace.device)
     _check(lib().ksj_gpu_coil_compress(c, v, m, basis.contiguous().data_ptr(), kspace.contiguous().data_ptr(),
                                        out.data_ptr(), _stream(stream)), "coil_compress")
+    return out
+
+
+NOISE_EIGENVALUE_FLOOR = 1.0e-6  # noise_model_estimate.cpp:38
+
+
+def noise_covariance(noise: torch.Tensor, stream=None) -> torch.Tensor:
+    """[C, M] complex64 channel-major noise samples -> [C, C] complex64 noise
+    covariance (means removed, 1/M, conj on the row index as the reference
+    forms it); the product sums on the tensor cores."""
+    c, m = noise.shape
+    L = lib()
+    n = int(L.ksj_gpu_coil_covariance_workspace_bytes(c, m))
+    if n == 0:
+        raise GpuError(1, "noise_covariance workspace")
+    ws = torch.empty(n, dtype=torch.uint8, device=noise.device)
+    out = torch.empty((c, c), dtype=torch.complex64, device=noise.device)
+    _check(L.ksj_gpu_noise_covariance(c, m, noise.contiguous().data_ptr(), out.data_ptr(), ws.data_ptr(), ws.numel(),
+                                      _stream(stream)), "noise_covariance")
+    return out
+
+
+def whitening_matrix(covariance, floor: float = NOISE_EIGENVALUE_FLOOR):
+    """Host: noise covariance [C, C] complex64 (numpy) -> whitening matrix
+    W = V diag(1/sqrt(max(lambda, floor))) V^H, [C, C] complex64."""
+    import numpy as np
+
+    cov = np.ascontiguousarray(covariance, dtype=np.complex64)
+    w = np.zeros_like(cov)
+    _check(lib().ksj_whitening_matrix(cov.shape[0], cov.ctypes.data, floor, w.ctypes.data), "whitening_matrix")
+    return w
+
+
+def noise_model(noise: torch.Tensor, stream=None) -> torch.Tensor:
+    """noise_model_estimate: [C, M] noise samples -> the [C, C] whitening
+    matrix on the same device (covariance on the GPU, eigensolve on the host)."""
+    cov = noise_covariance(noise, stream).cpu().numpy()
+    return torch.from_numpy(whitening_matrix(cov)).to(noise.device)
+
+
+def noise_prewhiten(whitening: torch.Tensor, kspace: torch.Tensor, stream=None) -> torch.Tensor:
+    """noncartesian_noise_prewhiten: W [C, C], kspace [C, M] complex64 -> W kspace."""
+    c, m = kspace.shape
+    if tuple(whitening.shape) != (c, c):
+        raise GpuError(1, "noise_prewhiten: whitening must be [C, C]")
+    out = torch.empty((c, m), dtype=torch.complex64, device=kspace.device)
+    _check(lib().ksj_gpu_noise_prewhiten(c, m, whitening.contiguous().data_ptr(), kspace.contiguous().data_ptr(),
+                                         out.data_ptr(), _stream(stream)), "noise_prewhiten")
     return out
 
 
