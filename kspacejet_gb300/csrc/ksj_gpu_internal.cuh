@@ -361,9 +361,10 @@ __device__ __forceinline__ void dft_reg(float2* v) {
 //   B  for each (k1, line): the N2-point DFT over n2 of those N2 contiguous
 //      columns gives X[k1 + N1 k2], handed to emit(k, line, value) instead of
 //      being stored back.
-// tw[t] = exp(2 pi i t / N).  Synchronises the block between the steps; the
+// tw[t] = exp(2 pi i t / N).  Synchronises the block between the steps
+// (kBarId 0), or only the nthreads threads of named barrier kBarId; the
 // caller synchronises before (the block is complete) as needed after.
-template <int N1, int N2, typename Emit>
+template <int N1, int N2, int kBarId = 0, typename Emit>
 __device__ __forceinline__ void fft_two_step(float2* smem, int lg_lines, const float2* __restrict__ tw, int tid,
                                              int nthreads, Emit&& emit) {
   const int lines = 1 << lg_lines;
@@ -379,7 +380,10 @@ __device__ __forceinline__ void fft_two_step(float2* smem, int lg_lines, const f
 #pragma unroll
     for (int k1 = 0; k1 < N1; ++k1) e[(N2 * k1) << lg_lines] = v[k1];
   }
-  __syncthreads();
+  if constexpr (kBarId == 0)
+    __syncthreads();
+  else
+    asm volatile("bar.sync %0, %1;" ::"n"(kBarId), "r"(nthreads) : "memory");
   for (int u = tid; u < N1 * lines; u += nthreads) {
     const int line = u & (lines - 1), k1 = u >> lg_lines;
     const float2* e = smem + ((N2 * k1) << lg_lines) + line;
@@ -393,17 +397,17 @@ __device__ __forceinline__ void fft_two_step(float2* smem, int lg_lines, const f
 }
 
 // Row lengths up to kMaxN with a two-step form (N1 = 16): false for any other n.
-template <int kMaxN, typename Emit>
+template <int kMaxN, int kBarId = 0, typename Emit>
 __device__ __forceinline__ bool fft_two_step_rows(int n, float2* smem, int lg_lines, const float2* tw, int tid,
                                                   int nthreads, Emit&& emit) {
   switch (n) {
-    case 128: fft_two_step<16, 8>(smem, lg_lines, tw, tid, nthreads, emit); return true;
-    case 192: fft_two_step<16, 12>(smem, lg_lines, tw, tid, nthreads, emit); return true;
-    case 256: fft_two_step<16, 16>(smem, lg_lines, tw, tid, nthreads, emit); return true;
-    case 384: fft_two_step<16, 24>(smem, lg_lines, tw, tid, nthreads, emit); return true;
+    case 128: fft_two_step<16, 8, kBarId>(smem, lg_lines, tw, tid, nthreads, emit); return true;
+    case 192: fft_two_step<16, 12, kBarId>(smem, lg_lines, tw, tid, nthreads, emit); return true;
+    case 256: fft_two_step<16, 16, kBarId>(smem, lg_lines, tw, tid, nthreads, emit); return true;
+    case 384: fft_two_step<16, 24, kBarId>(smem, lg_lines, tw, tid, nthreads, emit); return true;
     case 512:
       if constexpr (kMaxN >= 512) {
-        fft_two_step<16, 32>(smem, lg_lines, tw, tid, nthreads, emit);
+        fft_two_step<16, 32, kBarId>(smem, lg_lines, tw, tid, nthreads, emit);
         return true;
       }
       return false;
@@ -658,6 +662,11 @@ __device__ __forceinline__ void fence_proxy_async_shared() { asm volatile("fence
 
 __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+
+// One arrival (release, CTA scope).
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
 }
 
 __device__ __forceinline__ bool mbar_try_wait_parity(uint64_t* bar, uint32_t parity) {

@@ -241,6 +241,46 @@ def test_tunings_are_byte_identical(native, cuda, orc, channels):
         assert oracle.rel_l2(outs[gpu.OUTPUT_COIL_MAJOR][0, c], ref) <= TOL_FP64
 
 
+@pytest.mark.parametrize("channels,grid,width", [(32, 128, 4), (40, 192, 4), (32, 384, 6)])
+def test_two_step_rows_byte_identical_across_row_kernels(native, cuda, orc, channels, grid, width):
+    """Grid lengths with the two-step transform (128 .. 384): the row pass with
+    one or two CTAs per SM, the pipelined row pass (rows_blocks 3: gridding
+    warps and transform warps on alternate row buffers, several passes), and
+    the shared-memory accumulation of smaller coil groups all give the same
+    bytes, for RSS and coil-last output; the default is checked against FP64."""
+    import ctypes
+
+    import torch
+    from kspacejet_gb300 import gpu
+
+    image = grid // 2
+    tr, ks = _kb_case(orc, image, grid, width, channels=channels, spokes=20, seed=7)
+    frames = 3
+    k = torch.from_numpy(np.stack([ks, ks[:, ::-1].copy(), ks])).to(cuda)
+    t = torch.from_numpy(np.stack([tr, tr[::-1].copy(), tr[::-1].copy()])).to(cuda)
+    for mode in (gpu.OUTPUT_RSS, gpu.OUTPUT_COIL_LAST):
+        g = gpu.kb_gridding(image=image, grid=grid, channels=channels, samples=tr.shape[0], frames=frames,
+                            width=width, output=mode)
+        ws = g.new_workspace(cuda)
+        base = g.new_output(cuda)
+        g.run(k, t, base, ws)
+        want = base.cpu().numpy()
+        ran = []
+        for cg, rb, fpp in ((32, 1, 0), (32, 2, 0), (32, 3, 0), (32, 3, 1), (32, 3, 2), (16, 2, 0), (8, 1, 1)):
+            tun = gpu.GriddingTuning(ctypes.sizeof(gpu.GriddingTuning), cg, 0, 0, fpp, rb, 1)
+            o = g.new_output(cuda)
+            o.fill_(float("nan")) if o.dtype == torch.float32 else o.real.fill_(float("nan"))
+            g.run(k, t, o, ws, tuning=tun)
+            assert g.flags(ws) == 0
+            assert o.cpu().numpy().tobytes() == want.tobytes(), (mode, cg, rb, fpp)
+            ran.append((cg, rb, fpp))
+        assert (32, 3, 1) in ran
+        if mode == gpu.OUTPUT_COIL_LAST:
+            d64 = np.hypot(tr[:, 0].astype(np.float64), tr[:, 1].astype(np.float64))
+            ref = orc.kb_gridding(grid, image, ks[0].astype(np.complex128), tr.astype(np.float64), d64, width=width)
+            assert oracle.rel_l2(want[0][..., 0], ref) <= TOL_FP64
+
+
 def test_bf16_sample_storage_bound(native, cuda, orc):
     """BF16 sample storage, FP32 arithmetic: stated bound 1e-2 rel L2 against
     the FP32-storage result (bfloat16 keeps 8 mantissa bits: ~2e-3 per value)."""

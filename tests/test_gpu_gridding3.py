@@ -90,6 +90,22 @@ def test_gridding3_tunings_agree(native, cuda):
         assert got.tobytes() == base.tobytes(), (cg, parts, rb, fpp)
 
 
+def test_gridding3_pipelined_rows_agree(native, cuda):
+    """A grid with the two-step transform (128^3): the pipelined row pass
+    (rows_blocks 3, 32-coil groups) gives the bytes of the other row kernels."""
+    import ctypes
+
+    from kspacejet_gb300 import gpu
+
+    tr, ks = _case(64, 128, 300, 3, seed=12)
+    base = _run(cuda, 64, 128, 4, tr, ks, gpu.OUTPUT_RSS,
+                tuning=gpu.GriddingTuning(ctypes.sizeof(gpu.GriddingTuning), 32, 0, 0, 0, 2, 1))
+    for rb, fpp in ((3, 0), (3, 40), (1, 0)):
+        t = gpu.GriddingTuning(ctypes.sizeof(gpu.GriddingTuning), 32, 0, 0, fpp, rb, 1)
+        got = _run(cuda, 64, 128, 4, tr, ks, gpu.OUTPUT_RSS, tuning=t)
+        assert got.tobytes() == base.tobytes(), (rb, fpp)
+
+
 def test_gridding3_64_cube_subproblem(native, cuda, orc):
     """The kooshball configuration's accuracy check on a 64^3 sub-problem
     (sigma 1.5, W=4, 96 readout x 2000 spokes): against the FP64 Kaiser-Bessel
