@@ -22,6 +22,7 @@ scaling, no collective on the data path).
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import math
 import os
@@ -239,7 +240,13 @@ def run_ours(args) -> dict | None:
     ws = g.new_workspace(dev)
     stream = torch.cuda.current_stream()
     clocks = ClockSampler(local_rank).__enter__()
-    tuning = g.tune(k, t, out, ws)
+    if args.tuning:
+        # a fixed tuning (coil_group, column_block, frames_per_pass, rows_blocks_per_sm, coil_parts), e.g. to
+        # profile the kernels the autotuner picks in a plain run (its candidate timings are not valid under ncu)
+        cg, cb, fpp, rb, parts = (int(v) for v in args.tuning.split(","))
+        tuning = gpu.GriddingTuning(ctypes.sizeof(gpu.GriddingTuning), cg, cb, 0, fpp, rb, parts)
+    else:
+        tuning = g.tune(k, t, out, ws)
     for _ in range(args.warmup):
         g.run(k, t, out, ws, tuning=tuning)
     torch.cuda.synchronize()
@@ -702,6 +709,7 @@ def main() -> int:
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--frames", type=int, default=FRAMES,
                     help="frames per call (default: the 96-frame workload; fewer only for small profiling cases)")
+    ap.add_argument("--tuning", default="", help="fixed gridding tuning cg,cb,fpp,rb,parts instead of the autotuner")
     ap.add_argument("--serve", action="store_true", help="served-stream benchmark (separate JSON line)")
     ap.add_argument("--rows", action="store_true", help="the other hot-path rows (one JSON line each)")
     ap.add_argument("--spokes3", type=int, default=40000, help="--rows: spokes of the 3-D kooshball (0 skips it)")
