@@ -60,7 +60,7 @@ constexpr int kMaxGrid = 512;
 constexpr int kMaxThreads = 512;
 constexpr int kColsThreads = 256;  // k_cols block size
 constexpr int kAhead = 8;         // coil loads in flight per warp in k_rows
-constexpr int kAheadRegs = 4;     // the same for the register-cell form (a shorter unrolled body)
+constexpr int kAheadRegs = 4;     // the same for the register-cell form at 80 registers (a shorter unrolled body)
 constexpr uint32_t kFlagBytes = 256;
 
 // Per (frame, sample) record written by k_prepare, read by k_rows.
@@ -289,7 +289,9 @@ ksj_gpu_status make_shape(const ksj_gpu_gridding_desc* d, const ksj_gpu_gridding
   if (fpp <= 0) fpp = s->frames;
   s->frames_per_pass = std::min(fpp, s->frames);
   int rb = has(offsetof(ksj_gpu_gridding_tuning, rows_blocks_per_sm) + 4) ? static_cast<int>(t->rows_blocks_per_sm) : 0;
-  if (rb == 0) rb = 1;
+  // default: two row CTAs per SM wherever the row kernel fits them (384
+  // threads; the coil group above was sized for two CTAs' shared memory)
+  if (rb == 0) rb = rows_threads_for(s->grid_cols) <= 384 && rows_smem(cg) <= 115712 ? 2 : 1;
   if (rb != 1 && rb != 2 && rb != 3) return KSJ_GPU_ERROR_INVALID_ARGUMENT;
   s->rows_blocks = rb;
   int parts = has(offsetof(ksj_gpu_gridding_tuning, coil_parts) + 4) ? static_cast<int>(t->coil_parts) : 0;
@@ -1002,7 +1004,7 @@ __device__ __forceinline__ void chunk_taps_wrapped(float2 (&r)[kChunk], int c0, 
 // are stored once at its end (an empty list stores zeros).  kWrap admits
 // entries whose taps wrap around the grid inside the chunk.  `meta` is the
 // warp's staging buffer.
-template <int W, uint32_t kFormat, bool kWrap>
+template <int W, uint32_t kFormat, bool kWrap, int kAR = kAheadRegs>
 __device__ __forceinline__ void grid_chunk_regs(const RowsArgs& a, size_t sample_base, bool coil_ok, int lane,
                                                 float2* acc, int col_lo, const float4* xent, int n, float4* meta) {
   constexpr int kMV = meta_vecs(W);
@@ -1025,16 +1027,16 @@ __device__ __forceinline__ void grid_chunk_regs(const RowsArgs& a, size_t sample
       const uint32_t sk = __float_as_uint(meta[i * kMV].y);
       return load_sample<kFormat>(ks, sample_base + static_cast<size_t>(sk) * a.channels);
     };
-    float2 yv[kAheadRegs];
+    float2 yv[kAR];
 #pragma unroll
-    for (int k = 0; k < kAheadRegs; ++k) yv[k] = (coil_ok && k < cnt) ? fetch(k) : make_float2(0.0f, 0.0f);
-    for (int i0 = 0; i0 < cnt; i0 += kAheadRegs) {
+    for (int k = 0; k < kAR; ++k) yv[k] = (coil_ok && k < cnt) ? fetch(k) : make_float2(0.0f, 0.0f);
+    for (int i0 = 0; i0 < cnt; i0 += kAR) {
 #pragma unroll
-      for (int k = 0; k < kAheadRegs; ++k) {
+      for (int k = 0; k < kAR; ++k) {
         const int i = i0 + k;
         if (i >= cnt) break;
         const float2 y = yv[k];
-        yv[k] = (coil_ok && i + kAheadRegs < cnt) ? fetch(i + kAheadRegs) : make_float2(0.0f, 0.0f);
+        yv[k] = (coil_ok && i + kAR < cnt) ? fetch(i + kAR) : make_float2(0.0f, 0.0f);
         const float4 m0 = meta[i * kMV];
         float wt[4 * (kMV - 1)];
 #pragma unroll
@@ -1065,7 +1067,7 @@ __device__ __forceinline__ void grid_chunk_regs(const RowsArgs& a, size_t sample
 // Gridding of one row by whole 32-coil warps: warps take the row's chunks
 // from the shared counter in the order task_chunk gives (longest list
 // first).  Every chunk is a task, so every cell of the row is stored.
-template <int W, uint32_t kFormat, bool kWrap>
+template <int W, uint32_t kFormat, bool kWrap, int kAR>
 __device__ __forceinline__ void rows_grid_regs(const RowsArgs& a, int f, int cgi, int lane, float2* acc,
                                                const uint32_t* offs, const int* task_chunk, int* task_next,
                                                float4* meta) {
@@ -1082,7 +1084,7 @@ __device__ __forceinline__ void rows_grid_regs(const RowsArgs& a, int f, int cgi
     const uint32_t begin = offs[chunk];
     const int n = static_cast<int>(offs[chunk + 1] - begin);
     const float4* xent = a.expanded + (static_cast<size_t>(f) * a.entries_per_frame + begin) * kMV;
-    grid_chunk_regs<W, kFormat, kWrap>(a, sample_base, coil_ok, lane, acc, chunk * kChunk, xent, n, meta);
+    grid_chunk_regs<W, kFormat, kWrap, kAR>(a, sample_base, coil_ok, lane, acc, chunk * kChunk, xent, n, meta);
   }
 }
 
@@ -1275,12 +1277,13 @@ __global__ void __launch_bounds__(kThreads, kBlocks) k_rows(RowsArgs a) {
   __syncthreads();
 
   if constexpr (kCG == 32) {
+    constexpr int kAR = kAheadRegs;  // a deeper prefetch measured slower in both instances (code size)
     // taps wrap around the grid inside one chunk only on grids narrower than
     // kChunk + W - 1 columns; the loop for those keeps a per-tap form
     if (a.grid_cols < kChunk + W - 1)
-      rows_grid_regs<W, kFormat, true>(a, f, cgi, lane, acc, offs, task_chunk, &task_next, meta);
+      rows_grid_regs<W, kFormat, true, kAR>(a, f, cgi, lane, acc, offs, task_chunk, &task_next, meta);
     else
-      rows_grid_regs<W, kFormat, false>(a, f, cgi, lane, acc, offs, task_chunk, &task_next, meta);
+      rows_grid_regs<W, kFormat, false, kAR>(a, f, cgi, lane, acc, offs, task_chunk, &task_next, meta);
   } else {
   // ---- gridding.  A task is (column chunk, coil part): the chunk's sorted
   // list applied to a subset of the coil group.  Cells of different coils are
