@@ -685,6 +685,17 @@ def run_rows(args) -> list[dict]:
                       "config": {"workload": f"256 x {args.spokes3} spokes kooshball, grid 384^3, KB W=4, "
                                              "10 iterations", "samples": m3}})
 
+    # exact direct forward NUDFT (the reference's nufft2_forward on its Eigen backend): 128^2 image,
+    # 8 coils, 34 spokes x 256 readout
+    imf = torch.from_numpy((rng.standard_normal((128, 128, 8)) + 1j * rng.standard_normal((128, 128, 8))).astype(np.complex64)).to(dev)
+    trf = torch.from_numpy(synth.golden_angle_radial(256, 34)).to(dev)
+    ms = _time_gpu(lambda: gpu.direct_forward(imf, trf), 1, max(1, min(s, 5)))
+    pairs = 128 * 128 * trf.shape[0]
+    lines.append({"metric": "direct forward NUDFT: (sample, pixel) pairs/s", "value": pairs / (ms / 1e3),
+                  "unit": "pairs/s", "ms_per_call": ms, "dtype": "f32 (exact phase per pair)",
+                  "config": {"workload": "128 x 128 image, 8 coils, 34 x 256 golden-angle samples",
+                             "complex_macs": pairs * 8}})
+
     # Walsh 7x7 on the compressed 8-coil image (256 x 256), and RSS of 32 coils
     img = torch.from_numpy((rng.standard_normal((256, 256, 8)) + 1j * rng.standard_normal((256, 256, 8))).astype(np.complex64)).to(dev)
     ms = _time_gpu(lambda: gpu.walsh_combine(img, window=7, iterations=24), w, s)

@@ -22,6 +22,9 @@
  *       <- ksj::nufft::direct_nudft2_adjoint, per channel
  *          (libs/numerics/kspacejet-nufft/include/kspacejet/nufft/direct_nudft.hpp:62-69) and
  *          providers/kspacejet-noncartesian-recon/src/operators/noncartesian_adjoint_reconstruct.cpp:352-368
+ *   ksj_gpu_direct_forward
+ *       <- ksj::nufft::direct_nudft2_forward / nufft2_forward on the Eigen backend, per channel
+ *          (libs/numerics/kspacejet-nufft/include/kspacejet/nufft/direct_nudft.hpp:14-21, src/nufft.cpp:29)
  *   ksj_gpu_rss_coil_last
  *       <- ksj::stats::root_sum_of_squares_across(cube, image, Dim::dim2)
  *          (libs/numerics/kspacejet-stats/include/kspacejet/stats/norms.hpp:207-218) as called by
@@ -222,6 +225,17 @@ KSJ_GPU_API ksj_gpu_status ksj_gpu_direct_adjoint(uint32_t rows, uint32_t cols, 
                                                   uint32_t channels, uint32_t samples, const void* d_kspace,
                                                   const float* d_traj, void* d_out, void* d_workspace,
                                                   size_t workspace_bytes, void* stream);
+
+/* Exact direct forward NUDFT (the reference's nufft2_forward on its Eigen
+ * backend, nufft.cpp:29 -> eigen_nufft_direct_nudft.cpp:51-74), per channel:
+ *   y(c)(s) = sum_{r, col} x(c)(r, col) exp(-i (k_row,s (r - row_origin) + k_col,s (col - col_origin)))
+ * summed in pixel (row-major) order.  d_image coil-last complex64
+ * [row][col][channel] (the layout ksj_gpu_direct_adjoint writes), d_traj
+ * [sample][2], d_out [channel][sample] complex64 (the layout it reads): the
+ * two are adjoint to each other.  No workspace. */
+KSJ_GPU_API ksj_gpu_status ksj_gpu_direct_forward(uint32_t rows, uint32_t cols, double row_origin, double col_origin,
+                                                  uint32_t channels, uint32_t samples, const void* d_image,
+                                                  const float* d_traj, void* d_out, void* stream);
 
 /* The direct NUDFT adjoint above without a caller workspace and without any
  * allocation.  No counterpart in the reference: its direct adjoint

@@ -136,6 +136,59 @@ __global__ void __launch_bounds__(kDirectPixels) k_direct_adjoint(const float2* 
   }
 }
 
+// y[c][s] = sum_p x[p][c] exp(-i (k_r,s (r - r0) + k_c,s (col - c0))), p = r
+// cols + col in pixel order, summed in float in that order as
+// direct_forward_impl does (eigen_nufft_direct_nudft.cpp:51-74, the
+// reference's nufft2_forward on its Eigen backend, nufft.cpp:29).  One thread
+// per sample and a group of kDirectCoils coils per block row; each pixel
+// tile's positions and coil values are staged in shared memory.  The phase of
+// every (sample, pixel) pair is formed exactly and reduced by 2 pi before
+// sincosf (the reference rounds it to float first).
+constexpr int kForwardSamples = 128;  // threads (samples) per block
+constexpr int kForwardTile = 256;     // pixels staged per iteration
+__global__ void __launch_bounds__(kForwardSamples) k_direct_forward(const float2* __restrict__ image,
+                                                                   const float2* __restrict__ traj, float2* out,
+                                                                   int rows, int cols, float row_origin,
+                                                                   float col_origin, int channels, int samples) {
+  __shared__ float2 s_pos[kForwardTile];
+  __shared__ float2 s_x[kDirectCoils][kForwardTile];
+  const int s = blockIdx.x * kForwardSamples + threadIdx.x;
+  const int c0 = blockIdx.y * kDirectCoils;
+  const int nc = min(kDirectCoils, channels - c0);
+  const bool live = s < samples;
+  const float2 k = live ? traj[s] : make_float2(0.0f, 0.0f);
+  const int pixels = rows * cols;
+  float2 acc[kDirectCoils];
+#pragma unroll
+  for (int c = 0; c < kDirectCoils; ++c) acc[c] = make_float2(0.0f, 0.0f);
+  for (int p0 = 0; p0 < pixels; p0 += kForwardTile) {
+    const int np = min(kForwardTile, pixels - p0);
+    __syncthreads();
+    for (int i = threadIdx.x; i < np; i += kForwardSamples) {
+      const int r = (p0 + i) / cols, col = p0 + i - ((p0 + i) / cols) * cols;
+      s_pos[i] = make_float2(__fsub_rn(static_cast<float>(r), row_origin), __fsub_rn(static_cast<float>(col), col_origin));
+    }
+    for (int i = threadIdx.x; i < np * nc; i += kForwardSamples) {
+      const int q = i / nc, c = i - q * nc;
+      s_x[c][q] = image[static_cast<size_t>(p0 + q) * channels + c0 + c];
+    }
+    __syncthreads();
+    for (int q = 0; q < np; ++q) {
+      const float2 pos = s_pos[q];
+      const float2 e = exp_i_dot(k.x, pos.x, k.y, pos.y, -1.0f);
+#pragma unroll
+      for (int c = 0; c < kDirectCoils; ++c) {
+        if (c < nc) acc[c] = cadd(acc[c], cmul(s_x[c][q], e));
+      }
+    }
+  }
+  if (live) {
+#pragma unroll
+    for (int c = 0; c < kDirectCoils; ++c)
+      if (c < nc) out[static_cast<size_t>(c0 + c) * samples + s] = acc[c];
+  }
+}
+
 // --------------------------------------------------------------------- RSS
 
 // out[p] = sqrt(sum_c re^2 + im^2), a float sum in channel order with every
@@ -212,6 +265,28 @@ extern "C" ksj_gpu_status ksj_gpu_direct_adjoint(uint32_t rows, uint32_t cols, d
   k_transpose<unsigned long long><<<tg, dim3(32, 8), 0, cs>>>(reinterpret_cast<const unsigned long long*>(tmp),
                                                               static_cast<unsigned long long*>(d_out),
                                                               static_cast<int>(channels), pixels);
+  return check_launch();
+}
+
+extern "C" ksj_gpu_status ksj_gpu_direct_forward(uint32_t rows, uint32_t cols, double row_origin, double col_origin,
+                                                 uint32_t channels, uint32_t samples, const void* d_image,
+                                                 const float* d_traj, void* d_out, void* stream) {
+  if (rows == 0 || cols == 0 || channels == 0 || samples == 0 || d_image == nullptr || d_traj == nullptr ||
+      d_out == nullptr)
+    return KSJ_GPU_ERROR_INVALID_ARGUMENT;
+  if (rows > 8192 || cols > 8192 || static_cast<uint64_t>(rows) * cols > (1u << 26) || samples > (1u << 30))
+    return KSJ_GPU_ERROR_UNSUPPORTED;
+  const float ro = static_cast<float>(row_origin), co = static_cast<float>(col_origin);
+  if (static_cast<double>(ro) != row_origin || static_cast<double>(co) != col_origin)
+    return KSJ_GPU_ERROR_UNSUPPORTED;
+  cudaStream_t cs = static_cast<cudaStream_t>(stream);
+  const dim3 grid((samples + kForwardSamples - 1) / kForwardSamples, (channels + kDirectCoils - 1) / kDirectCoils);
+  LaunchScope scope("k_direct_forward", cs);
+  k_direct_forward<<<grid, kForwardSamples, 0, cs>>>(static_cast<const float2*>(d_image),
+                                                     reinterpret_cast<const float2*>(d_traj),
+                                                     static_cast<float2*>(d_out), static_cast<int>(rows),
+                                                     static_cast<int>(cols), ro, co, static_cast<int>(channels),
+                                                     static_cast<int>(samples));
   return check_launch();
 }
 

@@ -71,6 +71,8 @@ def lib() -> ctypes.CDLL:
                                             ctypes.POINTER(GriddingTuning)]
         L.ksj_gpu_direct_workspace_bytes.restype = sz
         L.ksj_gpu_direct_workspace_bytes.argtypes = [u32, u32, u32]
+        L.ksj_gpu_direct_forward.restype = ctypes.c_int32
+        L.ksj_gpu_direct_forward.argtypes = [u32, u32, ctypes.c_double, ctypes.c_double, u32, u32, vp, vp, vp, vp]
         L.ksj_gpu_direct_adjoint.restype = ctypes.c_int32
         L.ksj_gpu_direct_adjoint.argtypes = [u32, u32, ctypes.c_double, ctypes.c_double, u32, u32, vp, vp, vp, vp,
                                              sz, vp]
@@ -351,6 +353,19 @@ def direct_adjoint(kspace: torch.Tensor, traj: torch.Tensor, rows: int, cols: in
     out = torch.empty((rows, cols, c), dtype=torch.complex64, device=kspace.device)
     _check(L.ksj_gpu_direct_adjoint(rows, cols, ro, co, c, m, kspace.data_ptr(), traj.data_ptr(), out.data_ptr(),
                                     ws.data_ptr(), ws.numel(), _stream(stream)), "direct_adjoint")
+    return out
+
+
+def direct_forward(image: torch.Tensor, traj: torch.Tensor, origin: tuple[float, float] | None = None,
+                   stream=None) -> torch.Tensor:
+    """Exact direct NUDFT forward: image [rows, cols, C] complex64 (coil-last), traj [M, 2] -> [C, M]."""
+    rows, cols, c = image.shape
+    m = traj.shape[0]
+    ro, co = origin if origin is not None else ((rows - 1) / 2.0, (cols - 1) / 2.0)
+    out = torch.empty((c, m), dtype=torch.complex64, device=image.device)
+    _check(lib().ksj_gpu_direct_forward(rows, cols, ro, co, c, m, image.contiguous().data_ptr(),
+                                        traj.contiguous().data_ptr(), out.data_ptr(), _stream(stream)),
+           "direct_forward")
     return out
 
 
