@@ -131,6 +131,25 @@ KSJ_GPU_API ksj_gpu_status ksj_gpu_gridding_adjoint(const ksj_gpu_gridding_desc*
                                                     const float* d_traj, const float* d_dcf, void* d_out,
                                                     void* d_workspace, size_t workspace_bytes, void* stream);
 
+/* The same reconstruction from and to host memory: h_kspace, h_traj, h_dcf
+ * and h_out have the layouts of the device form above and should be pinned
+ * (page-locked) for the copies to run asynchronously.  The trajectory is
+ * copied first and the binning lists are built while the samples stream in on
+ * a second stream in passes of frames; each pass is transposed, gridded and
+ * transformed as soon as its samples have arrived, and its images are copied
+ * back while the next pass computes.  Unless the tuning fixes
+ * frames_per_pass, the frames are split into 4 passes.  Returns at
+ * once; `stream` completes after the last image copy.  The output bytes equal
+ * those of ksj_gpu_gridding_adjoint.  The device workspace is
+ * ksj_gpu_gridding_host_workspace_bytes(desc) bytes (the device form's
+ * workspace plus device copies of the inputs and images), 256-byte aligned.
+ * No counterpart in the reference (its Provider copies and computes in turn). */
+KSJ_GPU_API size_t ksj_gpu_gridding_host_workspace_bytes(const ksj_gpu_gridding_desc* desc);
+KSJ_GPU_API ksj_gpu_status ksj_gpu_gridding_adjoint_host(const ksj_gpu_gridding_desc* desc,
+                                                         const ksj_gpu_gridding_tuning* tuning, const void* h_kspace,
+                                                         const float* h_traj, const float* h_dcf, void* h_out,
+                                                         void* d_workspace, size_t workspace_bytes, void* stream);
+
 /* The sorted binning lists of the last call that used `d_workspace`, copied to
  * host memory: for every frame, list (grid_row, column_chunk) in row-major
  * order, the sample indices that touch it in increasing order (read from the

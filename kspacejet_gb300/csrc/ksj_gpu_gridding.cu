@@ -1779,10 +1779,22 @@ ksj_gpu_status build_lists(const Shape& s, const ksj_gpu_gridding_desc* d, const
   return KSJ_GPU_OK;
 }
 
+// Host buffers of ksj_gpu_gridding_adjoint_host: pass p's samples reach
+// device memory on the copy stream (event in[p]); the stream waits for them
+// before the pass's transpose, and the pass's images go back to the host on
+// the copy stream once the pass is done (event done[p]).
+struct HostIo {
+  cudaStream_t copy;
+  const cudaEvent_t* in;
+  const cudaEvent_t* done;
+  void* h_out;
+  size_t out_frame_bytes;
+};
+
 template <int W, uint32_t kFormat>
 ksj_gpu_status launch_all(const Shape& s, const Layout& l, const ksj_gpu_gridding_desc* d, const void* d_kspace,
                           const float* d_traj, const float* d_dcf, void* d_out, unsigned char* ws,
-                          cudaStream_t stream) {
+                          cudaStream_t stream, const HostIo* io = nullptr) {
   uint32_t* flags = reinterpret_cast<uint32_t*>(ws + l.flags);
   unsigned char* records = ws + l.records;
   uint32_t* counts = reinterpret_cast<uint32_t*>(ws + l.counts);
@@ -1813,12 +1825,16 @@ ksj_gpu_status launch_all(const Shape& s, const Layout& l, const ksj_gpu_griddin
                                              reinterpret_cast<uint32_t*>(ws + l.long_lists), stream);
     if (st != KSJ_GPU_OK) return st;
   }
-  {
-    const dim3 tg((s.samples + 31) / 32, (s.channels + 31) / 32, s.frames);
+  const size_t frame_samples = static_cast<size_t>(s.samples) * s.channels;  // elements per frame
+  auto to_coil_last = [&](int f0, int nf) {
+    const size_t eb = sample_bytes(d->sample_format);
+    const dim3 tg((s.samples + 31) / 32, (s.channels + 31) / 32, nf);
     LaunchScope scope("k_samples_coil_last", stream);
-    k_samples_coil_last<kFormat><<<tg, dim3(32, 8), 0, stream>>>(d_kspace, ws + l.samples_t, s.channels, s.samples,
-                                                                 flags);
-  }
+    k_samples_coil_last<kFormat><<<tg, dim3(32, 8), 0, stream>>>(
+        static_cast<const unsigned char*>(d_kspace) + f0 * frame_samples * eb, ws + l.samples_t + f0 * frame_samples * eb,
+        s.channels, s.samples, flags);
+  };
+  if (io == nullptr) to_coil_last(0, s.frames);
   RowsArgs r{};
   r.samples_t = ws + l.samples_t;
   r.sample_frame_stride = static_cast<size_t>(s.samples) * s.channels;
@@ -1873,8 +1889,13 @@ ksj_gpu_status launch_all(const Shape& s, const Layout& l, const ksj_gpu_griddin
   if (!cols_kernel_setup(cols_kernel, cols_smem)) return KSJ_GPU_ERROR_CUDA;
 
   // frames in passes sized so one pass's row-transformed grid stays in L2
-  for (int f0 = 0; f0 < s.frames; f0 += s.frames_per_pass) {
+  const int pixels = s.out_rows * s.out_cols;
+  for (int f0 = 0, pass = 0; f0 < s.frames; f0 += s.frames_per_pass, ++pass) {
     const int nf = std::min(s.frames_per_pass, s.frames - f0);
+    if (io != nullptr) {
+      if (cudaStreamWaitEvent(stream, io->in[pass], 0) != cudaSuccess) return KSJ_GPU_ERROR_CUDA;
+      to_coil_last(f0, nf);
+    }
     r.frame0 = f0;
     c.frame0 = f0;
     rows_launch.launch(r, s.grid_rows, (s.channels + s.coil_group - 1) / s.coil_group, nf, stream);
@@ -1883,15 +1904,24 @@ ksj_gpu_status launch_all(const Shape& s, const Layout& l, const ksj_gpu_griddin
       const dim3 grid((s.out_cols + s.column_block - 1) / s.column_block, nf);
       cols_kernel<<<grid, kColsThreads, cols_smem, stream>>>(map, c);
     }
-  }
-  if (coil_major) {
-    // [frame][pixel][channel] -> [frame][channel][pixel]
-    const int pixels = s.out_rows * s.out_cols;
-    const dim3 tg((s.channels + 31) / 32, (pixels + 31) / 32, s.frames);
-    LaunchScope scope("k_images_coil_major", stream);
-    k_transpose<unsigned long long><<<tg, dim3(32, 8), 0, stream>>>(
-        reinterpret_cast<const unsigned long long*>(ws + l.coil_last), static_cast<unsigned long long*>(d_out),
-        pixels, s.channels);
+    if (coil_major) {
+      // [frame][pixel][channel] -> [frame][channel][pixel], this pass's frames
+      const size_t fe = static_cast<size_t>(pixels) * s.channels;
+      const dim3 tg((s.channels + 31) / 32, (pixels + 31) / 32, nf);
+      LaunchScope scope("k_images_coil_major", stream);
+      k_transpose<unsigned long long><<<tg, dim3(32, 8), 0, stream>>>(
+          reinterpret_cast<const unsigned long long*>(ws + l.coil_last) + f0 * fe,
+          static_cast<unsigned long long*>(d_out) + f0 * fe, pixels, s.channels);
+    }
+    if (io != nullptr) {
+      const size_t off = static_cast<size_t>(f0) * io->out_frame_bytes;
+      if (cudaEventRecord(io->done[pass], stream) != cudaSuccess ||
+          cudaStreamWaitEvent(io->copy, io->done[pass], 0) != cudaSuccess ||
+          cudaMemcpyAsync(static_cast<unsigned char*>(io->h_out) + off, static_cast<unsigned char*>(d_out) + off,
+                          static_cast<size_t>(nf) * io->out_frame_bytes, cudaMemcpyDeviceToHost, io->copy) !=
+              cudaSuccess)
+        return KSJ_GPU_ERROR_CUDA;
+    }
   }
   return check_launch();
 }
@@ -2661,9 +2691,66 @@ ksj_gpu_status launch_pipe_menon3(const Shape& s, const PmLayout3& l, uint32_t i
 
 template <int W>
 ksj_gpu_status dispatch_format(const Shape& s, const Layout& l, const ksj_gpu_gridding_desc* d, const void* k,
-                               const float* t, const float* w, void* o, unsigned char* ws, cudaStream_t st) {
-  if (d->sample_format == KSJ_GPU_SAMPLES_BF16) return launch_all<W, KSJ_GPU_SAMPLES_BF16>(s, l, d, k, t, w, o, ws, st);
-  return launch_all<W, KSJ_GPU_SAMPLES_CF32>(s, l, d, k, t, w, o, ws, st);
+                               const float* t, const float* w, void* o, unsigned char* ws, cudaStream_t st,
+                               const HostIo* io = nullptr) {
+  if (d->sample_format == KSJ_GPU_SAMPLES_BF16)
+    return launch_all<W, KSJ_GPU_SAMPLES_BF16>(s, l, d, k, t, w, o, ws, st, io);
+  return launch_all<W, KSJ_GPU_SAMPLES_CF32>(s, l, d, k, t, w, o, ws, st, io);
+}
+
+ksj_gpu_status dispatch_width(const Shape& s, const Layout& l, const ksj_gpu_gridding_desc* d, const void* k,
+                              const float* t, const float* w, void* o, unsigned char* ws, cudaStream_t st,
+                              const HostIo* io = nullptr) {
+  switch (s.width) {
+    case 2: return dispatch_format<2>(s, l, d, k, t, w, o, ws, st, io);
+    case 4: return dispatch_format<4>(s, l, d, k, t, w, o, ws, st, io);
+    case 6: return dispatch_format<6>(s, l, d, k, t, w, o, ws, st, io);
+    case 8: return dispatch_format<8>(s, l, d, k, t, w, o, ws, st, io);
+    default: return KSJ_GPU_ERROR_UNSUPPORTED;
+  }
+}
+
+// Workspace of the host-buffer entry point: the device workspace, then the
+// device copies of the samples, trajectory, density weights and images.
+struct HostLayout {
+  Layout dev;
+  size_t kspace, traj, dcf, out, total;
+};
+
+size_t image_frame_bytes(const Shape& s, const ksj_gpu_gridding_desc* d) {
+  const size_t px = static_cast<size_t>(s.out_rows) * s.out_cols;
+  return d->output == KSJ_GPU_OUTPUT_RSS ? px * sizeof(float) : px * s.channels * sizeof(float2);
+}
+
+HostLayout make_host_layout(const Shape& s, const ksj_gpu_gridding_desc* d) {
+  HostLayout h{};
+  h.dev = make_layout(s, d);
+  size_t off = h.dev.total;
+  auto take = [&](size_t bytes) {
+    const size_t at = off;
+    off = align_up(off + bytes, 256);
+    return at;
+  };
+  const size_t fm = static_cast<size_t>(s.frames) * s.samples;
+  h.kspace = take(fm * s.channels * sample_bytes(d->sample_format));
+  h.traj = take(fm * 2 * sizeof(float));
+  h.dcf = d->dcf_mode == KSJ_GPU_DCF_EXTERNAL ? take(fm * sizeof(float)) : off;
+  h.out = take(static_cast<size_t>(s.frames) * image_frame_bytes(s, d));
+  h.total = off;
+  return h;
+}
+
+// One non-blocking stream per device for the host-buffer entry point's copies.
+cudaStream_t copy_stream(int device) {
+  static std::mutex m;
+  static std::map<int, cudaStream_t> streams;
+  std::lock_guard<std::mutex> lock(m);
+  auto it = streams.find(device);
+  if (it != streams.end()) return it->second;
+  cudaStream_t st = nullptr;
+  if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return nullptr;
+  streams[device] = st;
+  return st;
 }
 
 }  // namespace
@@ -2694,13 +2781,84 @@ extern "C" ksj_gpu_status ksj_gpu_gridding_adjoint(const ksj_gpu_gridding_desc* 
     return KSJ_GPU_ERROR_INVALID_ARGUMENT;
   unsigned char* ws = static_cast<unsigned char*>(d_workspace);
   cudaStream_t cs = static_cast<cudaStream_t>(stream);
-  switch (s.width) {
-    case 2: return dispatch_format<2>(s, l, desc, d_kspace, d_traj, d_dcf, d_out, ws, cs);
-    case 4: return dispatch_format<4>(s, l, desc, d_kspace, d_traj, d_dcf, d_out, ws, cs);
-    case 6: return dispatch_format<6>(s, l, desc, d_kspace, d_traj, d_dcf, d_out, ws, cs);
-    case 8: return dispatch_format<8>(s, l, desc, d_kspace, d_traj, d_dcf, d_out, ws, cs);
-    default: return KSJ_GPU_ERROR_UNSUPPORTED;
+  return dispatch_width(s, l, desc, d_kspace, d_traj, d_dcf, d_out, ws, cs);
+}
+
+extern "C" size_t ksj_gpu_gridding_host_workspace_bytes(const ksj_gpu_gridding_desc* desc) {
+  Shape s{};
+  if (make_shape(desc, nullptr, &s) != KSJ_GPU_OK) return 0;
+  return make_host_layout(s, desc).total;
+}
+
+extern "C" ksj_gpu_status ksj_gpu_gridding_adjoint_host(const ksj_gpu_gridding_desc* desc,
+                                                        const ksj_gpu_gridding_tuning* tuning, const void* h_kspace,
+                                                        const float* h_traj, const float* h_dcf, void* h_out,
+                                                        void* d_workspace, size_t workspace_bytes, void* stream) {
+  Shape s{};
+  const ksj_gpu_status st = make_shape(desc, tuning, &s);
+  if (st != KSJ_GPU_OK) return st;
+  if (h_kspace == nullptr || h_traj == nullptr || h_out == nullptr) return KSJ_GPU_ERROR_INVALID_ARGUMENT;
+  if (desc->dcf_mode == KSJ_GPU_DCF_EXTERNAL && h_dcf == nullptr) return KSJ_GPU_ERROR_INVALID_ARGUMENT;
+  // copies and passes overlap: unless the tuning fixes the passes, 4 of them
+  // (each pass ends in a partly filled wave, so more passes cost device time;
+  // fewer leave more of the copy exposed: 4 measured best for 96 frames)
+  const bool fixed_passes = tuning != nullptr &&
+                            tuning->struct_size >= offsetof(ksj_gpu_gridding_tuning, frames_per_pass) + 4 &&
+                            tuning->frames_per_pass != 0;
+  if (!fixed_passes) s.frames_per_pass = std::max(1, (s.frames + 3) / 4);
+  const HostLayout h = make_host_layout(s, desc);
+  if (d_workspace == nullptr || (reinterpret_cast<uintptr_t>(d_workspace) & 255u) != 0 || workspace_bytes < h.total)
+    return KSJ_GPU_ERROR_WORKSPACE;
+  int device = 0;
+  if (cudaGetDevice(&device) != cudaSuccess) return KSJ_GPU_ERROR_CUDA;
+  cudaStream_t cs = static_cast<cudaStream_t>(stream);
+  cudaStream_t copy = copy_stream(device);
+  if (copy == nullptr) return KSJ_GPU_ERROR_CUDA;
+  unsigned char* ws = static_cast<unsigned char*>(d_workspace);
+  const size_t fm = static_cast<size_t>(s.frames) * s.samples;
+  const size_t frame_bytes = static_cast<size_t>(s.samples) * s.channels * sample_bytes(desc->sample_format);
+  const int passes = (s.frames + s.frames_per_pass - 1) / s.frames_per_pass;
+  std::vector<cudaEvent_t> events(static_cast<size_t>(2 * passes + 2), nullptr);
+  auto release = [&]() {
+    for (cudaEvent_t e : events)
+      if (e != nullptr) cudaEventDestroy(e);
+  };
+  for (cudaEvent_t& e : events)
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
+      release();
+      return KSJ_GPU_ERROR_CUDA;
+    }
+  cudaEvent_t* in = events.data();
+  cudaEvent_t* done = in + passes;
+  cudaEvent_t start = done[passes], end = done[passes + 1];
+  ksj_gpu_status result = KSJ_GPU_OK;
+  // the trajectory (and weights) first, on the stream, for the binning; the
+  // copy stream starts after everything already queued on the stream (the
+  // staging buffers may still be read by an earlier call)
+  if (cudaMemcpyAsync(ws + h.traj, h_traj, fm * 2 * sizeof(float), cudaMemcpyHostToDevice, cs) != cudaSuccess ||
+      (desc->dcf_mode == KSJ_GPU_DCF_EXTERNAL &&
+       cudaMemcpyAsync(ws + h.dcf, h_dcf, fm * sizeof(float), cudaMemcpyHostToDevice, cs) != cudaSuccess) ||
+      cudaEventRecord(start, cs) != cudaSuccess || cudaStreamWaitEvent(copy, start, 0) != cudaSuccess)
+    result = KSJ_GPU_ERROR_CUDA;
+  for (int p = 0; p < passes && result == KSJ_GPU_OK; ++p) {
+    const int f0 = p * s.frames_per_pass, nf = std::min(s.frames_per_pass, s.frames - f0);
+    if (cudaMemcpyAsync(ws + h.kspace + f0 * frame_bytes, static_cast<const unsigned char*>(h_kspace) + f0 * frame_bytes,
+                        static_cast<size_t>(nf) * frame_bytes, cudaMemcpyHostToDevice, copy) != cudaSuccess ||
+        cudaEventRecord(in[p], copy) != cudaSuccess)
+      result = KSJ_GPU_ERROR_CUDA;
   }
+  if (result == KSJ_GPU_OK) {
+    const HostIo io{copy, in, done, h_out, image_frame_bytes(s, desc)};
+    result = dispatch_width(s, h.dev, desc, ws + h.kspace, reinterpret_cast<const float*>(ws + h.traj),
+                            desc->dcf_mode == KSJ_GPU_DCF_EXTERNAL ? reinterpret_cast<const float*>(ws + h.dcf)
+                                                                   : nullptr,
+                            ws + h.out, ws, cs, &io);
+  }
+  // the stream completes only after the last image copy
+  if (cudaEventRecord(end, copy) != cudaSuccess || cudaStreamWaitEvent(cs, end, 0) != cudaSuccess)
+    if (result == KSJ_GPU_OK) result = KSJ_GPU_ERROR_CUDA;
+  release();
+  return result;
 }
 
 extern "C" ksj_gpu_status ksj_gpu_gridding_binning(const ksj_gpu_gridding_desc* desc,

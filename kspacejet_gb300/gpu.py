@@ -58,6 +58,11 @@ def lib() -> ctypes.CDLL:
         vp, u32, u64, sz = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_size_t
         L.ksj_gpu_gridding_workspace_bytes.restype = sz
         L.ksj_gpu_gridding_workspace_bytes.argtypes = [ctypes.POINTER(GriddingDesc)]
+        L.ksj_gpu_gridding_host_workspace_bytes.restype = sz
+        L.ksj_gpu_gridding_host_workspace_bytes.argtypes = [ctypes.POINTER(GriddingDesc)]
+        L.ksj_gpu_gridding_adjoint_host.restype = ctypes.c_int32
+        L.ksj_gpu_gridding_adjoint_host.argtypes = [ctypes.POINTER(GriddingDesc), ctypes.POINTER(GriddingTuning), vp,
+                                                    vp, vp, vp, vp, sz, vp]
         L.ksj_gpu_gridding_adjoint.restype = ctypes.c_int32
         L.ksj_gpu_gridding_adjoint.argtypes = [ctypes.POINTER(GriddingDesc), ctypes.POINTER(GriddingTuning), vp, vp,
                                                vp, vp, vp, sz, vp]
@@ -215,6 +220,34 @@ class Gridding:
                                             dcf.data_ptr() if dcf is not None else None, out.data_ptr(),
                                             workspace.data_ptr(), workspace.numel(), _stream(stream))
         _check(st, "gridding_adjoint")
+
+    def host_workspace_bytes(self) -> int:
+        d = self.desc()
+        n = lib().ksj_gpu_gridding_host_workspace_bytes(ctypes.byref(d))
+        if n == 0:
+            raise GpuError(1, "gridding_host_workspace_bytes")
+        return int(n)
+
+    def new_host_workspace(self, device="cuda") -> torch.Tensor:
+        """Device workspace of run_host (the device workspace plus device copies of inputs and images)."""
+        return torch.empty(self.host_workspace_bytes(), dtype=torch.uint8, device=device)
+
+    def run_host(self, kspace: torch.Tensor, traj: torch.Tensor, out: torch.Tensor, workspace: torch.Tensor,
+                 dcf: torch.Tensor | None = None, tuning: GriddingTuning | None = None,
+                 stream: torch.cuda.Stream | None = None) -> None:
+        """ksj_gpu_gridding_adjoint_host: kspace, traj, dcf and out are contiguous host (CPU) tensors, pinned for
+        the copies to overlap the passes; asynchronous on `stream` (synchronise before reading `out`)."""
+        d = self.desc()
+        for t in (kspace, traj, out) + ((dcf,) if dcf is not None else ()):
+            if t.is_cuda or not t.is_contiguous():
+                raise ValueError("kspace, traj, dcf and out must be contiguous host tensors")
+        if not workspace.is_cuda:
+            raise ValueError("the workspace is device memory")
+        st = lib().ksj_gpu_gridding_adjoint_host(ctypes.byref(d), ctypes.byref(tuning) if tuning else None,
+                                                 kspace.data_ptr(), traj.data_ptr(),
+                                                 dcf.data_ptr() if dcf is not None else None, out.data_ptr(),
+                                                 workspace.data_ptr(), workspace.numel(), _stream(stream))
+        _check(st, "gridding_adjoint_host")
 
     def flags(self, workspace: torch.Tensor, stream: torch.cuda.Stream | None = None) -> int:
         v = ctypes.c_uint32()

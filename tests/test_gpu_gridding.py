@@ -330,3 +330,55 @@ def test_rss_kernel_is_bit_exact(native, cuda, orc, fixtures):
     y = (rng.standard_normal((97, 65, 13)) + 1j * rng.standard_normal((97, 65, 13))).astype(np.complex64)
     out = gpu.rss_coil_last(torch.from_numpy(y).to(cuda)).cpu().numpy()
     assert out.tobytes() == orc.rss(y).tobytes()
+
+
+@pytest.mark.parametrize("output,fmt,dcf_mode,pinned,fpp", [
+    ("rss", "cf32", "ramp", True, 0), ("coil_last", "cf32", "external", True, 0),
+    ("coil_major", "bf16", "ramp", False, 0), ("rss", "cf32", "ramp", True, 2)])
+def test_host_entry_point_equals_device_entry_point(native, cuda, orc, output, fmt, dcf_mode, pinned, fpp):
+    """ksj_gpu_gridding_adjoint_host (host buffers, copies overlapped with the
+    frame passes) gives the bytes of ksj_gpu_gridding_adjoint on device copies
+    of the same inputs: every output form, both sample formats, external
+    weights, pinned and pageable host memory, automatic and fixed passes."""
+    import ctypes
+
+    import torch
+    from kspacejet_gb300 import gpu
+
+    mode = {"rss": gpu.OUTPUT_RSS, "coil_last": gpu.OUTPUT_COIL_LAST, "coil_major": gpu.OUTPUT_COIL_MAJOR}[output]
+    sf = gpu.SAMPLES_BF16 if fmt == "bf16" else gpu.SAMPLES_CF32
+    dm = gpu.DCF_EXTERNAL if dcf_mode == "external" else gpu.DCF_ANALYTIC_RAMP
+    frames, channels = 5, 6
+    trs, kss = [], []
+    for f in range(frames):
+        tr, ks = _kb_case(orc, 64, 128, 4, channels=channels, spokes=16, seed=20 + f)
+        trs.append(tr)
+        kss.append(ks)
+    tr = np.stack(trs)
+    ks = np.stack(kss)
+    g = gpu.kb_gridding(image=64, grid=128, channels=channels, samples=tr.shape[1], frames=frames, output=mode,
+                        dcf=dm, sample_format=sf)
+    kt = torch.from_numpy(ks)
+    if sf == gpu.SAMPLES_BF16:
+        kt = torch.view_as_real(kt).to(torch.bfloat16).contiguous()
+    tt = torch.from_numpy(tr)
+    dcf = torch.from_numpy(np.random.default_rng(3).uniform(0.5, 2.0, tr.shape[:2]).astype(np.float32))
+    tun = gpu.GriddingTuning(ctypes.sizeof(gpu.GriddingTuning), 0, 0, 0, fpp, 0, 0)
+    ws = g.new_workspace(cuda)
+    dev_out = g.new_output(cuda)
+    g.run(kt.to(cuda), tt.to(cuda), dev_out, ws, dcf=dcf.to(cuda) if dm == gpu.DCF_EXTERNAL else None, tuning=tun)
+    want = dev_out.cpu().numpy()
+    if pinned:
+        kt, tt, dcf = kt.pin_memory(), tt.pin_memory(), dcf.pin_memory()
+    host_out = torch.empty(g.output_shape(), dtype=g.output_dtype())
+    if pinned:
+        host_out = host_out.pin_memory()
+    wsh = g.new_host_workspace(cuda)
+    for _ in range(2):
+        host_out.fill_(float("nan")) if host_out.dtype == torch.float32 else host_out.real.fill_(float("nan"))
+        g.run_host(kt, tt, host_out, wsh, dcf=dcf if dm == gpu.DCF_EXTERNAL else None, tuning=tun)
+        torch.cuda.synchronize()
+        assert host_out.numpy().tobytes() == want.tobytes()
+    assert g.flags(wsh) == 0
+    with pytest.raises(ValueError):
+        g.run_host(kt.to(cuda), tt, host_out, wsh)
