@@ -137,8 +137,9 @@ KSJ_GPU_API ksj_gpu_status ksj_gpu_gridding_adjoint(const ksj_gpu_gridding_desc*
  * copied first and the binning lists are built while the samples stream in on
  * a second stream in passes of frames; each pass is transposed, gridded and
  * transformed as soon as its samples have arrived, and its images are copied
- * back while the next pass computes.  Unless the tuning fixes
- * frames_per_pass, the frames are split into 4 passes.  Returns at
+ * back while the next pass computes; odd passes run on a second compute
+ * stream so consecutive passes overlap.  Unless the tuning fixes
+ * frames_per_pass, the frames are split into 8 passes.  Returns at
  * once; `stream` completes after the last image copy.  The output bytes equal
  * those of ksj_gpu_gridding_adjoint.  The device workspace is
  * ksj_gpu_gridding_host_workspace_bytes(desc) bytes (the device form's

@@ -1780,13 +1780,17 @@ ksj_gpu_status build_lists(const Shape& s, const ksj_gpu_gridding_desc* d, const
 }
 
 // Host buffers of ksj_gpu_gridding_adjoint_host: pass p's samples reach
-// device memory on the copy stream (event in[p]); the stream waits for them
-// before the pass's transpose, and the pass's images go back to the host on
-// the copy stream once the pass is done (event done[p]).
+// device memory on the copy stream (event in[p]); the pass waits for them
+// before its transpose, and its images go back to the host on the copy
+// stream once the pass is done (event done[p]).  Odd passes run on a second
+// compute stream (`alt`, joined after the binning through `ready` and back
+// through `alt_done`), so a pass's last, partly filled wave overlaps the
+// next pass.
 struct HostIo {
-  cudaStream_t copy;
+  cudaStream_t copy, alt;
   const cudaEvent_t* in;
   const cudaEvent_t* done;
+  cudaEvent_t ready, alt_done;
   void* h_out;
   size_t out_frame_bytes;
 };
@@ -1826,15 +1830,15 @@ ksj_gpu_status launch_all(const Shape& s, const Layout& l, const ksj_gpu_griddin
     if (st != KSJ_GPU_OK) return st;
   }
   const size_t frame_samples = static_cast<size_t>(s.samples) * s.channels;  // elements per frame
-  auto to_coil_last = [&](int f0, int nf) {
+  auto to_coil_last = [&](int f0, int nf, cudaStream_t st) {
     const size_t eb = sample_bytes(d->sample_format);
     const dim3 tg((s.samples + 31) / 32, (s.channels + 31) / 32, nf);
-    LaunchScope scope("k_samples_coil_last", stream);
-    k_samples_coil_last<kFormat><<<tg, dim3(32, 8), 0, stream>>>(
+    LaunchScope scope("k_samples_coil_last", st);
+    k_samples_coil_last<kFormat><<<tg, dim3(32, 8), 0, st>>>(
         static_cast<const unsigned char*>(d_kspace) + f0 * frame_samples * eb, ws + l.samples_t + f0 * frame_samples * eb,
         s.channels, s.samples, flags);
   };
-  if (io == nullptr) to_coil_last(0, s.frames);
+  if (io == nullptr) to_coil_last(0, s.frames, stream);
   RowsArgs r{};
   r.samples_t = ws + l.samples_t;
   r.sample_frame_stride = static_cast<size_t>(s.samples) * s.channels;
@@ -1890,32 +1894,41 @@ ksj_gpu_status launch_all(const Shape& s, const Layout& l, const ksj_gpu_griddin
 
   // frames in passes sized so one pass's row-transformed grid stays in L2
   const int pixels = s.out_rows * s.out_cols;
+  bool alt_used = false;
+  if (io != nullptr && s.frames > s.frames_per_pass &&
+      (cudaEventRecord(io->ready, stream) != cudaSuccess || cudaStreamWaitEvent(io->alt, io->ready, 0) != cudaSuccess))
+    return KSJ_GPU_ERROR_CUDA;
   for (int f0 = 0, pass = 0; f0 < s.frames; f0 += s.frames_per_pass, ++pass) {
     const int nf = std::min(s.frames_per_pass, s.frames - f0);
+    cudaStream_t ps = stream;
     if (io != nullptr) {
-      if (cudaStreamWaitEvent(stream, io->in[pass], 0) != cudaSuccess) return KSJ_GPU_ERROR_CUDA;
-      to_coil_last(f0, nf);
+      if (pass & 1) {
+        ps = io->alt;
+        alt_used = true;
+      }
+      if (cudaStreamWaitEvent(ps, io->in[pass], 0) != cudaSuccess) return KSJ_GPU_ERROR_CUDA;
+      to_coil_last(f0, nf, ps);
     }
     r.frame0 = f0;
     c.frame0 = f0;
-    rows_launch.launch(r, s.grid_rows, (s.channels + s.coil_group - 1) / s.coil_group, nf, stream);
+    rows_launch.launch(r, s.grid_rows, (s.channels + s.coil_group - 1) / s.coil_group, nf, ps);
     {
-      LaunchScope scope("k_cols", stream);
+      LaunchScope scope("k_cols", ps);
       const dim3 grid((s.out_cols + s.column_block - 1) / s.column_block, nf);
-      cols_kernel<<<grid, kColsThreads, cols_smem, stream>>>(map, c);
+      cols_kernel<<<grid, kColsThreads, cols_smem, ps>>>(map, c);
     }
     if (coil_major) {
       // [frame][pixel][channel] -> [frame][channel][pixel], this pass's frames
       const size_t fe = static_cast<size_t>(pixels) * s.channels;
       const dim3 tg((s.channels + 31) / 32, (pixels + 31) / 32, nf);
-      LaunchScope scope("k_images_coil_major", stream);
-      k_transpose<unsigned long long><<<tg, dim3(32, 8), 0, stream>>>(
+      LaunchScope scope("k_images_coil_major", ps);
+      k_transpose<unsigned long long><<<tg, dim3(32, 8), 0, ps>>>(
           reinterpret_cast<const unsigned long long*>(ws + l.coil_last) + f0 * fe,
           static_cast<unsigned long long*>(d_out) + f0 * fe, pixels, s.channels);
     }
     if (io != nullptr) {
       const size_t off = static_cast<size_t>(f0) * io->out_frame_bytes;
-      if (cudaEventRecord(io->done[pass], stream) != cudaSuccess ||
+      if (cudaEventRecord(io->done[pass], ps) != cudaSuccess ||
           cudaStreamWaitEvent(io->copy, io->done[pass], 0) != cudaSuccess ||
           cudaMemcpyAsync(static_cast<unsigned char*>(io->h_out) + off, static_cast<unsigned char*>(d_out) + off,
                           static_cast<size_t>(nf) * io->out_frame_bytes, cudaMemcpyDeviceToHost, io->copy) !=
@@ -1923,6 +1936,10 @@ ksj_gpu_status launch_all(const Shape& s, const Layout& l, const ksj_gpu_griddin
         return KSJ_GPU_ERROR_CUDA;
     }
   }
+  // the second compute stream joins back before the call's stream goes on
+  if (alt_used &&
+      (cudaEventRecord(io->alt_done, io->alt) != cudaSuccess || cudaStreamWaitEvent(stream, io->alt_done, 0) != cudaSuccess))
+    return KSJ_GPU_ERROR_CUDA;
   return check_launch();
 }
 
@@ -2740,16 +2757,17 @@ HostLayout make_host_layout(const Shape& s, const ksj_gpu_gridding_desc* d) {
   return h;
 }
 
-// One non-blocking stream per device for the host-buffer entry point's copies.
-cudaStream_t copy_stream(int device) {
+// Non-blocking streams per device for the host-buffer entry point: which 0
+// carries the copies, which 1 the odd frame passes.
+cudaStream_t side_stream(int device, int which) {
   static std::mutex m;
-  static std::map<int, cudaStream_t> streams;
+  static std::map<std::pair<int, int>, cudaStream_t> streams;
   std::lock_guard<std::mutex> lock(m);
-  auto it = streams.find(device);
+  auto it = streams.find({device, which});
   if (it != streams.end()) return it->second;
   cudaStream_t st = nullptr;
   if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return nullptr;
-  streams[device] = st;
+  streams[{device, which}] = st;
   return st;
 }
 
@@ -2799,26 +2817,26 @@ extern "C" ksj_gpu_status ksj_gpu_gridding_adjoint_host(const ksj_gpu_gridding_d
   if (st != KSJ_GPU_OK) return st;
   if (h_kspace == nullptr || h_traj == nullptr || h_out == nullptr) return KSJ_GPU_ERROR_INVALID_ARGUMENT;
   if (desc->dcf_mode == KSJ_GPU_DCF_EXTERNAL && h_dcf == nullptr) return KSJ_GPU_ERROR_INVALID_ARGUMENT;
-  // copies and passes overlap: unless the tuning fixes the passes, 4 of them
-  // (each pass ends in a partly filled wave, so more passes cost device time;
-  // fewer leave more of the copy exposed: 4 measured best for 96 frames)
+  // copies and passes overlap: unless the tuning fixes the passes, 8 of them
+  // (fewer leave more of the first copy exposed; more add launches; with odd
+  // passes on a second stream, 8 measured best for 96 frames)
   const bool fixed_passes = tuning != nullptr &&
                             tuning->struct_size >= offsetof(ksj_gpu_gridding_tuning, frames_per_pass) + 4 &&
                             tuning->frames_per_pass != 0;
-  if (!fixed_passes) s.frames_per_pass = std::max(1, (s.frames + 3) / 4);
+  if (!fixed_passes) s.frames_per_pass = std::max(1, (s.frames + 7) / 8);
   const HostLayout h = make_host_layout(s, desc);
   if (d_workspace == nullptr || (reinterpret_cast<uintptr_t>(d_workspace) & 255u) != 0 || workspace_bytes < h.total)
     return KSJ_GPU_ERROR_WORKSPACE;
   int device = 0;
   if (cudaGetDevice(&device) != cudaSuccess) return KSJ_GPU_ERROR_CUDA;
   cudaStream_t cs = static_cast<cudaStream_t>(stream);
-  cudaStream_t copy = copy_stream(device);
-  if (copy == nullptr) return KSJ_GPU_ERROR_CUDA;
+  cudaStream_t copy = side_stream(device, 0), alt = side_stream(device, 1);
+  if (copy == nullptr || alt == nullptr) return KSJ_GPU_ERROR_CUDA;
   unsigned char* ws = static_cast<unsigned char*>(d_workspace);
   const size_t fm = static_cast<size_t>(s.frames) * s.samples;
   const size_t frame_bytes = static_cast<size_t>(s.samples) * s.channels * sample_bytes(desc->sample_format);
   const int passes = (s.frames + s.frames_per_pass - 1) / s.frames_per_pass;
-  std::vector<cudaEvent_t> events(static_cast<size_t>(2 * passes + 2), nullptr);
+  std::vector<cudaEvent_t> events(static_cast<size_t>(2 * passes + 4), nullptr);
   auto release = [&]() {
     for (cudaEvent_t e : events)
       if (e != nullptr) cudaEventDestroy(e);
@@ -2830,7 +2848,7 @@ extern "C" ksj_gpu_status ksj_gpu_gridding_adjoint_host(const ksj_gpu_gridding_d
     }
   cudaEvent_t* in = events.data();
   cudaEvent_t* done = in + passes;
-  cudaEvent_t start = done[passes], end = done[passes + 1];
+  cudaEvent_t start = done[passes], end = done[passes + 1], ready = done[passes + 2], alt_done = done[passes + 3];
   ksj_gpu_status result = KSJ_GPU_OK;
   // the trajectory (and weights) first, on the stream, for the binning; the
   // copy stream starts after everything already queued on the stream (the
@@ -2848,7 +2866,7 @@ extern "C" ksj_gpu_status ksj_gpu_gridding_adjoint_host(const ksj_gpu_gridding_d
       result = KSJ_GPU_ERROR_CUDA;
   }
   if (result == KSJ_GPU_OK) {
-    const HostIo io{copy, in, done, h_out, image_frame_bytes(s, desc)};
+    const HostIo io{copy, alt, in, done, ready, alt_done, h_out, image_frame_bytes(s, desc)};
     result = dispatch_width(s, h.dev, desc, ws + h.kspace, reinterpret_cast<const float*>(ws + h.traj),
                             desc->dcf_mode == KSJ_GPU_DCF_EXTERNAL ? reinterpret_cast<const float*>(ws + h.dcf)
                                                                    : nullptr,
