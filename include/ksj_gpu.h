@@ -138,8 +138,8 @@ KSJ_GPU_API ksj_gpu_status ksj_gpu_gridding_adjoint(const ksj_gpu_gridding_desc*
  * a second stream in passes of frames; each pass is transposed, gridded and
  * transformed as soon as its samples have arrived, and its images are copied
  * back while the next pass computes; odd passes run on a second compute
- * stream so consecutive passes overlap.  Unless the tuning fixes
- * frames_per_pass, the frames are split into 8 passes.  Returns at
+ * stream so consecutive passes overlap.  The frames are split into at least
+ * 8 passes (a tuning's smaller frames_per_pass is kept).  Returns at
  * once; `stream` completes after the last image copy.  The output bytes equal
  * those of ksj_gpu_gridding_adjoint.  The device workspace is
  * ksj_gpu_gridding_host_workspace_bytes(desc) bytes (the device form's

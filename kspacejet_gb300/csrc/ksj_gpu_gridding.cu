@@ -1779,13 +1779,13 @@ ksj_gpu_status build_lists(const Shape& s, const ksj_gpu_gridding_desc* d, const
   return KSJ_GPU_OK;
 }
 
-// Host buffers of ksj_gpu_gridding_adjoint_host: pass p's samples reach
-// device memory on the copy stream (event in[p]); the pass waits for them
-// before its transpose, and its images go back to the host on the copy
-// stream once the pass is done (event done[p]).  Odd passes run on a second
+// Streams and events of a multi-pass call.  Odd passes run on a second
 // compute stream (`alt`, joined after the binning through `ready` and back
 // through `alt_done`), so a pass's last, partly filled wave overlaps the
-// next pass.
+// next pass.  With host buffers (ksj_gpu_gridding_adjoint_host, `copy` set):
+// pass p's samples reach device memory on the copy stream (event in[p]); the
+// pass waits for them before its transpose, and its images go back to the
+// host on the copy stream once the pass is done (event done[p]).
 struct HostIo {
   cudaStream_t copy, alt;
   const cudaEvent_t* in;
@@ -1838,7 +1838,7 @@ ksj_gpu_status launch_all(const Shape& s, const Layout& l, const ksj_gpu_griddin
         static_cast<const unsigned char*>(d_kspace) + f0 * frame_samples * eb, ws + l.samples_t + f0 * frame_samples * eb,
         s.channels, s.samples, flags);
   };
-  if (io == nullptr) to_coil_last(0, s.frames, stream);
+  if (io == nullptr || io->copy == nullptr) to_coil_last(0, s.frames, stream);
   RowsArgs r{};
   r.samples_t = ws + l.samples_t;
   r.sample_frame_stride = static_cast<size_t>(s.samples) * s.channels;
@@ -1906,8 +1906,10 @@ ksj_gpu_status launch_all(const Shape& s, const Layout& l, const ksj_gpu_griddin
         ps = io->alt;
         alt_used = true;
       }
-      if (cudaStreamWaitEvent(ps, io->in[pass], 0) != cudaSuccess) return KSJ_GPU_ERROR_CUDA;
-      to_coil_last(f0, nf, ps);
+      if (io->copy != nullptr) {
+        if (cudaStreamWaitEvent(ps, io->in[pass], 0) != cudaSuccess) return KSJ_GPU_ERROR_CUDA;
+        to_coil_last(f0, nf, ps);
+      }
     }
     r.frame0 = f0;
     c.frame0 = f0;
@@ -1926,7 +1928,7 @@ ksj_gpu_status launch_all(const Shape& s, const Layout& l, const ksj_gpu_griddin
           reinterpret_cast<const unsigned long long*>(ws + l.coil_last) + f0 * fe,
           static_cast<unsigned long long*>(d_out) + f0 * fe, pixels, s.channels);
     }
-    if (io != nullptr) {
+    if (io != nullptr && io->copy != nullptr) {
       const size_t off = static_cast<size_t>(f0) * io->out_frame_bytes;
       if (cudaEventRecord(io->done[pass], ps) != cudaSuccess ||
           cudaStreamWaitEvent(io->copy, io->done[pass], 0) != cudaSuccess ||
@@ -2799,7 +2801,22 @@ extern "C" ksj_gpu_status ksj_gpu_gridding_adjoint(const ksj_gpu_gridding_desc* 
     return KSJ_GPU_ERROR_INVALID_ARGUMENT;
   unsigned char* ws = static_cast<unsigned char*>(d_workspace);
   cudaStream_t cs = static_cast<cudaStream_t>(stream);
-  return dispatch_width(s, l, desc, d_kspace, d_traj, d_dcf, d_out, ws, cs);
+  if (s.frames_per_pass >= s.frames) return dispatch_width(s, l, desc, d_kspace, d_traj, d_dcf, d_out, ws, cs);
+  // several passes: odd ones on the second compute stream
+  int device = 0;
+  if (cudaGetDevice(&device) != cudaSuccess) return KSJ_GPU_ERROR_CUDA;
+  cudaStream_t alt = side_stream(device, 1);
+  cudaEvent_t ready = nullptr, alt_done = nullptr;
+  if (alt == nullptr || cudaEventCreateWithFlags(&ready, cudaEventDisableTiming) != cudaSuccess) return KSJ_GPU_ERROR_CUDA;
+  if (cudaEventCreateWithFlags(&alt_done, cudaEventDisableTiming) != cudaSuccess) {
+    cudaEventDestroy(ready);
+    return KSJ_GPU_ERROR_CUDA;
+  }
+  const HostIo io{nullptr, alt, nullptr, nullptr, ready, alt_done, nullptr, 0};
+  const ksj_gpu_status result = dispatch_width(s, l, desc, d_kspace, d_traj, d_dcf, d_out, ws, cs, &io);
+  cudaEventDestroy(ready);
+  cudaEventDestroy(alt_done);
+  return result;
 }
 
 extern "C" size_t ksj_gpu_gridding_host_workspace_bytes(const ksj_gpu_gridding_desc* desc) {
@@ -2817,13 +2834,10 @@ extern "C" ksj_gpu_status ksj_gpu_gridding_adjoint_host(const ksj_gpu_gridding_d
   if (st != KSJ_GPU_OK) return st;
   if (h_kspace == nullptr || h_traj == nullptr || h_out == nullptr) return KSJ_GPU_ERROR_INVALID_ARGUMENT;
   if (desc->dcf_mode == KSJ_GPU_DCF_EXTERNAL && h_dcf == nullptr) return KSJ_GPU_ERROR_INVALID_ARGUMENT;
-  // copies and passes overlap: unless the tuning fixes the passes, 8 of them
-  // (fewer leave more of the first copy exposed; more add launches; with odd
-  // passes on a second stream, 8 measured best for 96 frames)
-  const bool fixed_passes = tuning != nullptr &&
-                            tuning->struct_size >= offsetof(ksj_gpu_gridding_tuning, frames_per_pass) + 4 &&
-                            tuning->frames_per_pass != 0;
-  if (!fixed_passes) s.frames_per_pass = std::max(1, (s.frames + 7) / 8);
+  // copies and passes overlap: at least 8 passes (fewer leave more of the
+  // first copy exposed; with odd passes on a second stream, 8 measured best
+  // for 96 frames); a tuning with smaller passes keeps them
+  s.frames_per_pass = std::min(s.frames_per_pass, std::max(1, (s.frames + 7) / 8));
   const HostLayout h = make_host_layout(s, desc);
   if (d_workspace == nullptr || (reinterpret_cast<uintptr_t>(d_workspace) & 255u) != 0 || workspace_bytes < h.total)
     return KSJ_GPU_ERROR_WORKSPACE;
@@ -2964,7 +2978,7 @@ extern "C" ksj_gpu_status ksj_gpu_gridding_tune(const ksj_gpu_gridding_desc* des
     if (cg > 1 && cg / 2 >= desc->channels) continue;
     if (cg * 4 < desc->channels && cg < 8) continue;
     for (uint32_t cbm : {1u, 2u})
-    for (uint32_t fpp : {0u, 12u})
+    for (uint32_t fpp : {0u, 12u, 48u})
     for (uint32_t rb : {1u, 2u, 3u})
     for (uint32_t parts : {1u, 2u}) {
       if (fpp >= desc->frames) continue;
