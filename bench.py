@@ -694,6 +694,19 @@ def run_rows(args) -> list[dict]:
                   "config": {"workload": "128 x 128 image, 8 coils, 34 x 256 golden-angle samples",
                              "complex_macs": pairs * 8}})
 
+    # Cartesian coil images: 8 frames x 32 coils x 256 x 256, coil-last output
+    kc = torch.from_numpy((rng.standard_normal((8, 32, 256, 256)) + 1j * rng.standard_normal((8, 32, 256, 256))).astype(np.complex64)).to(dev)
+    ms = _time_gpu(lambda: gpu.cartesian_ifft2(kc), w, s)
+    byts = 2 * kc.numel() * 8  # k-space read, coil-last images written
+    lines.append({"metric": "Cartesian coil images: images/s", "value": 8 * 32 / (ms / 1e3), "unit": "images/s",
+                  "ms_per_call": ms, "dtype": "f32",
+                  "config": {"workload": "8 frames x 32 coils x 256 x 256, inverse 2-D DFT, coil-last"},
+                  "roofline": {"bound": "hbm", "achieved": round(byts / (ms / 1e3) / 1e9, 1), "peak": hbm,
+                               "unit": "GB/s", "frac": round(byts / (ms / 1e3) / 1e9 / hbm, 4),
+                               "note": "algorithmic bytes = k-space in + images out; the transpose and the "
+                                       "row-transformed intermediate add 4 more passes"}})
+    del kc
+
     # Walsh 7x7 on the compressed 8-coil image (256 x 256), and RSS of 32 coils
     img = torch.from_numpy((rng.standard_normal((256, 256, 8)) + 1j * rng.standard_normal((256, 256, 8))).astype(np.complex64)).to(dev)
     ms = _time_gpu(lambda: gpu.walsh_combine(img, window=7, iterations=24), w, s)

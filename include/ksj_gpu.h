@@ -25,6 +25,8 @@
  *   ksj_gpu_direct_forward
  *       <- ksj::nufft::direct_nudft2_forward / nufft2_forward on the Eigen backend, per channel
  *          (libs/numerics/kspacejet-nufft/include/kspacejet/nufft/direct_nudft.hpp:14-21, src/nufft.cpp:29)
+ *   ksj_gpu_cartesian_ifft2
+ *       <- providers/kspacejet-cartesian-recon/src/operators/cartesian_ifft2_coil_images.cpp:372-407
  *   ksj_gpu_rss_coil_last
  *       <- ksj::stats::root_sum_of_squares_across(cube, image, Dim::dim2)
  *          (libs/numerics/kspacejet-stats/include/kspacejet/stats/norms.hpp:207-218) as called by
@@ -358,6 +360,24 @@ KSJ_GPU_API ksj_gpu_status ksj_gpu_noise_prewhiten(uint32_t channels, uint32_t s
 KSJ_GPU_API ksj_gpu_status ksj_gpu_coil_compress(uint32_t channels, uint32_t virtual_channels, uint32_t samples,
                                                  const void* d_basis, const void* d_kspace, void* d_out,
                                                  void* stream);
+
+/* ------------------------------------------------- Cartesian coil images */
+
+/* cartesian_ifft2_coil_images (providers/kspacejet-cartesian-recon/src/
+ * operators/cartesian_ifft2_coil_images.cpp:372-407): per frame and channel
+ * the inverse 2-D DFT normalised by 1 / (rows cols), no shift
+ * (fft2_inplace_with_workspace, Direction::inverse, Normalization::inverse).
+ * d_kspace complex64 [frame][channel][row][col] (channel-major, as the
+ * reference's ksj.kspace-frame) -> d_out per `output`: KSJ_GPU_OUTPUT_COIL_LAST
+ * complex64 [frame][row][col][channel] (the reference's coil-image frame) or
+ * KSJ_GPU_OUTPUT_RSS float32 [frame][row][col].  rows and cols 2^a or 3 * 2^a
+ * up to 512 (the reference also takes other lengths: KSJ_GPU_ERROR_UNSUPPORTED
+ * here), channels 1..64.  Workspace: ksj_gpu_cartesian_workspace_bytes. */
+KSJ_GPU_API size_t ksj_gpu_cartesian_workspace_bytes(uint32_t rows, uint32_t cols, uint32_t channels,
+                                                     uint32_t frames);
+KSJ_GPU_API ksj_gpu_status ksj_gpu_cartesian_ifft2(uint32_t rows, uint32_t cols, uint32_t channels, uint32_t frames,
+                                                   uint32_t output, const void* d_kspace, void* d_out,
+                                                   void* d_workspace, size_t workspace_bytes, void* stream);
 
 /* --------------------------------------------------------------- context */
 

@@ -2729,6 +2729,133 @@ ksj_gpu_status dispatch_width(const Shape& s, const Layout& l, const ksj_gpu_gri
   }
 }
 
+// ------------------------------------------------ Cartesian coil images
+//
+// cartesian_ifft2_coil_images (providers/kspacejet-cartesian-recon/src/
+// operators/cartesian_ifft2_coil_images.cpp:372-407): per channel, the
+// inverse 2-D DFT normalised by 1 / (rows cols) (fft2_inplace_with_workspace
+// with Direction::inverse and Normalization::inverse: 1/cols on the row pass,
+// 1/rows on the column pass, libs/numerics/kspacejet-fft/src/eigen/
+// eigen_fft_transforms.cpp:148-205), no shift; channel-major k-space in,
+// coil-last images out.  Here: [frame][channel][pixel] ->
+// [frame][pixel][channel] (k_transpose), the row transform per (frame, row,
+// coil group) (k_cart_rows), then the column pass k_cols with its
+// deapodisation factors set to 1/rows and 1/cols and no crop or shift.
+
+constexpr int kCartThreads = 256;
+
+// Twiddles, the normalisation factors and the position of output k of each
+// axis's transform (two-step slot or digit-reversed position).
+__global__ void k_cart_tables(float2* tw_rows, int rows, float2* tw_cols, int cols, float* inv_dr, float* inv_dc,
+                              int* pos_rows, int* pos_cols, DifPlan plan_rows, DifPlan plan_cols) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < rows) {
+    tw_rows[i] = twiddle(i, rows);
+    inv_dr[i] = 1.0f / static_cast<float>(rows);
+    pos_rows[i] = has_two_step_rows(rows) ? two_step_slot(i, rows) : dif_position(plan_rows, i);
+  }
+  if (i < cols) {
+    tw_cols[i] = twiddle(i, cols);
+    inv_dc[i] = 1.0f / static_cast<float>(cols);
+    pos_cols[i] = dif_position(plan_cols, i);
+  }
+}
+
+// One block per (frame, row, coil group of cg): the row's cg coil lines
+// [column][coil] from the coil-last samples, transformed along the row; every
+// column written to [frame][row][column][cpitch].
+template <int kN>
+__global__ void __launch_bounds__(kCartThreads) k_cart_rows(const float2* __restrict__ coil_last, float2* inter,
+                                                            const float2* __restrict__ tw_cols,
+                                                            const int* __restrict__ pos_cols, DifPlan plan, int rows,
+                                                            int cols, int channels, int cg, int cpitch) {
+  extern __shared__ __align__(16) float2 cart_smem[];
+  float2* acc = cart_smem;
+  float2* tw = cart_smem + static_cast<size_t>(cols) * cg;
+  const int row = blockIdx.x, cgi = blockIdx.y, f = blockIdx.z;
+  const int lg = ilog2(cg);
+  const float2* src = coil_last + (static_cast<size_t>(f) * rows + row) * cols * channels;
+  for (int i = threadIdx.x; i < cols * cg; i += blockDim.x) {
+    const int col = i >> lg, gc = cgi * cg + (i & (cg - 1));
+    acc[i] = gc < channels ? __ldg(src + static_cast<size_t>(col) * channels + gc) : make_float2(0.0f, 0.0f);
+  }
+  for (int i = threadIdx.x; i < cols; i += blockDim.x) tw[i] = tw_cols[i];
+  __syncthreads();
+  float2* dst = inter + (static_cast<size_t>(f) * rows + row) * cols * cpitch + cgi * cg;
+  const int live = min(cg, channels - cgi * cg);
+  auto emit = [&](int k, int line, float2 v) {
+    if (line < live) dst[static_cast<size_t>(k) * cpitch + line] = v;
+  };
+  if constexpr (kN != 0) {
+    fft_two_step<16, kN / 16>(acc, lg, tw, threadIdx.x, blockDim.x, emit);
+  } else {
+    dif_lines(acc, lg, plan, tw, threadIdx.x, blockDim.x);
+    const int c = threadIdx.x & (cg - 1);
+    if (c < live)
+      for (int k = threadIdx.x >> lg; k < cols; k += blockDim.x >> lg)
+        dst[static_cast<size_t>(k) * cpitch + c] = acc[(__ldg(pos_cols + k) << lg) + c];
+  }
+}
+
+using CartRowsKernel = void (*)(const float2*, float2*, const float2*, const int*, DifPlan, int, int, int, int, int);
+
+CartRowsKernel cart_rows_for(int n) {
+  switch (n) {
+    case 128: return k_cart_rows<128>;
+    case 192: return k_cart_rows<192>;
+    case 256: return k_cart_rows<256>;
+    case 384: return k_cart_rows<384>;
+    case 512: return k_cart_rows<512>;
+    default: return k_cart_rows<0>;
+  }
+}
+
+// The shape of a Cartesian call as the column pass reads it.
+struct CartShape {
+  Shape s;
+  int cg;  // coils per row block
+  size_t flags, coil_last, inter, tables, total;
+};
+
+ksj_gpu_status make_cart_shape(uint32_t rows, uint32_t cols, uint32_t channels, uint32_t frames, CartShape* c) {
+  if (rows < 2 || cols < 2 || channels == 0 || channels > 64 || frames == 0) return KSJ_GPU_ERROR_INVALID_ARGUMENT;
+  if (!is_fft_size(rows) || !is_fft_size(cols)) return KSJ_GPU_ERROR_UNSUPPORTED;
+  Shape& s = c->s;
+  s = Shape{};
+  s.frames = static_cast<int>(frames);
+  s.channels = static_cast<int>(channels);
+  s.rows = s.grid_rows = s.out_rows = static_cast<int>(rows);
+  s.cols = s.grid_cols = s.out_cols = static_cast<int>(cols);
+  s.col_group = 2;
+  while (s.col_group < s.channels && s.col_group < 32) s.col_group <<= 1;
+  s.cpitch = (s.channels + s.col_group - 1) / s.col_group * s.col_group;
+  const int cgroups = s.cpitch / s.col_group;
+  auto tile = [&](int b) {
+    return static_cast<size_t>(s.grid_rows) * b * s.col_group * sizeof(float2) * (cgroups > 1 ? 2 : 1);
+  };
+  int cb = std::max(1, 32 / s.col_group);
+  while (cb > 1 && (tile(cb) > 110 * 1024 || cb > s.out_cols)) cb >>= 1;
+  if (tile(cb) > 200 * 1024) return KSJ_GPU_ERROR_UNSUPPORTED;
+  s.column_block = cb;
+  s.frames_per_pass = s.frames;
+  make_dif_plan(s.grid_rows, &s.plan_rows);
+  make_dif_plan(s.grid_cols, &s.plan_cols);
+  c->cg = s.col_group;
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    const size_t at = off;
+    off = align_up(off + bytes, 256);
+    return at;
+  };
+  const size_t px = static_cast<size_t>(frames) * rows * cols;
+  c->flags = take(kFlagBytes);
+  c->coil_last = take(px * channels * sizeof(float2));
+  c->inter = take(px * s.cpitch * sizeof(float2));
+  c->tables = take((static_cast<size_t>(rows) + cols) * (sizeof(float2) + sizeof(float) + sizeof(int)));
+  c->total = off;
+  return KSJ_GPU_OK;
+}
+
 // Workspace of the host-buffer entry point: the device workspace, then the
 // device copies of the samples, trajectory, density weights and images.
 struct HostLayout {
@@ -3119,4 +3246,94 @@ extern "C" ksj_gpu_status ksj_gpu_pipe_menon_dcf3(const ksj_gpu_gridding3_desc* 
     case 8: return launch_pipe_menon3<8>(s, l, iterations, d_traj, d_dcf, ws, cs);
     default: return KSJ_GPU_ERROR_UNSUPPORTED;
   }
+}
+
+extern "C" size_t ksj_gpu_cartesian_workspace_bytes(uint32_t rows, uint32_t cols, uint32_t channels,
+                                                    uint32_t frames) {
+  CartShape c{};
+  return make_cart_shape(rows, cols, channels, frames, &c) == KSJ_GPU_OK ? c.total : 0;
+}
+
+extern "C" ksj_gpu_status ksj_gpu_cartesian_ifft2(uint32_t rows, uint32_t cols, uint32_t channels, uint32_t frames,
+                                                  uint32_t output, const void* d_kspace, void* d_out,
+                                                  void* d_workspace, size_t workspace_bytes, void* stream) {
+  CartShape cs{};
+  const ksj_gpu_status st = make_cart_shape(rows, cols, channels, frames, &cs);
+  if (st != KSJ_GPU_OK) return st;
+  if (d_kspace == nullptr || d_out == nullptr || (output != KSJ_GPU_OUTPUT_COIL_LAST && output != KSJ_GPU_OUTPUT_RSS) ||
+      (reinterpret_cast<uintptr_t>(d_kspace) & 7u) != 0 || (reinterpret_cast<uintptr_t>(d_out) & 7u) != 0)
+    return KSJ_GPU_ERROR_INVALID_ARGUMENT;
+  if (d_workspace == nullptr || (reinterpret_cast<uintptr_t>(d_workspace) & 255u) != 0 || workspace_bytes < cs.total)
+    return KSJ_GPU_ERROR_WORKSPACE;
+  const Shape& s = cs.s;
+  cudaStream_t cstream = static_cast<cudaStream_t>(stream);
+  unsigned char* ws = static_cast<unsigned char*>(d_workspace);
+  uint32_t* flags = reinterpret_cast<uint32_t*>(ws + cs.flags);
+  float2* coil_last = reinterpret_cast<float2*>(ws + cs.coil_last);
+  float2* inter = reinterpret_cast<float2*>(ws + cs.inter);
+  float2* tw_rows = reinterpret_cast<float2*>(ws + cs.tables);
+  float2* tw_cols = tw_rows + rows;
+  float* inv_dr = reinterpret_cast<float*>(tw_cols + cols);
+  float* inv_dc = inv_dr + rows;
+  int* pos_rows = reinterpret_cast<int*>(inv_dc + cols);
+  int* pos_cols = pos_rows + rows;
+  if (cudaMemsetAsync(flags, 0, kFlagBytes, cstream) != cudaSuccess) return KSJ_GPU_ERROR_CUDA;
+  {
+    const int n = static_cast<int>(std::max(rows, cols));
+    LaunchScope scope("k_cart_tables", cstream);
+    k_cart_tables<<<(n + 255) / 256, 256, 0, cstream>>>(tw_rows, static_cast<int>(rows), tw_cols,
+                                                       static_cast<int>(cols), inv_dr, inv_dc, pos_rows, pos_cols,
+                                                       s.plan_rows, s.plan_cols);
+  }
+  {
+    // [frame][channel][pixel] -> [frame][pixel][channel]
+    const int pixels = static_cast<int>(rows * cols);
+    const dim3 tg((pixels + 31) / 32, (channels + 31) / 32, frames);
+    LaunchScope scope("k_kspace_coil_last", cstream);
+    k_transpose<unsigned long long><<<tg, dim3(32, 8), 0, cstream>>>(
+        static_cast<const unsigned long long*>(d_kspace), reinterpret_cast<unsigned long long*>(coil_last),
+        static_cast<int>(channels), pixels);
+  }
+  {
+    const CartRowsKernel rk = cart_rows_for(static_cast<int>(cols));
+    const size_t smem = (static_cast<size_t>(cols) * cs.cg + cols) * sizeof(float2);
+    if (cudaFuncSetAttribute(rk, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)) != cudaSuccess)
+      return KSJ_GPU_ERROR_CUDA;
+    const dim3 grid(rows, (channels + cs.cg - 1) / cs.cg, frames);
+    LaunchScope scope("k_cart_rows", cstream);
+    rk<<<grid, kCartThreads, smem, cstream>>>(coil_last, inter, tw_cols, pos_cols, s.plan_cols, static_cast<int>(rows),
+                                             static_cast<int>(cols), static_cast<int>(channels), cs.cg, s.cpitch);
+  }
+  ColsArgs c{};
+  c.tw_rows = tw_rows;
+  c.inv_dr = inv_dr;
+  c.inv_dc = inv_dc;
+  c.pos_rows = pos_rows;
+  c.flags = flags;
+  c.frames = s.frames;
+  c.channels = s.channels;
+  c.grid_rows = s.grid_rows;
+  c.out_rows = s.out_rows;
+  c.out_cols = s.out_cols;
+  c.kb = 1;  // apply the factors: here the normalisation
+  c.row_shift = 0;
+  c.column_block = s.column_block;
+  c.col_group = s.col_group;
+  c.groups = s.cpitch / s.col_group;
+  c.plan = s.plan_rows;
+  c.output = output;
+  c.out = d_out;
+  c.out_pitch = s.channels;
+  c.frame0 = 0;
+  CUtensorMap map;
+  if (!make_inter_map(s, inter, &map, &c.box_rows, &c.boxes)) return KSJ_GPU_ERROR_CUDA;
+  const size_t cols_smem = cols_smem_bytes(s);
+  const ColsKernel cols_kernel = cols_kernel_for(s.grid_rows);
+  if (!cols_kernel_setup(cols_kernel, cols_smem)) return KSJ_GPU_ERROR_CUDA;
+  {
+    LaunchScope scope("k_cols", cstream);
+    cols_kernel<<<dim3((s.out_cols + s.column_block - 1) / s.column_block, s.frames), kColsThreads, cols_smem, cstream>>>(
+        map, c);
+  }
+  return check_launch();
 }

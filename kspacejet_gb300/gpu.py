@@ -76,6 +76,10 @@ def lib() -> ctypes.CDLL:
                                             ctypes.POINTER(GriddingTuning)]
         L.ksj_gpu_direct_workspace_bytes.restype = sz
         L.ksj_gpu_direct_workspace_bytes.argtypes = [u32, u32, u32]
+        L.ksj_gpu_cartesian_workspace_bytes.restype = sz
+        L.ksj_gpu_cartesian_workspace_bytes.argtypes = [u32, u32, u32, u32]
+        L.ksj_gpu_cartesian_ifft2.restype = ctypes.c_int32
+        L.ksj_gpu_cartesian_ifft2.argtypes = [u32, u32, u32, u32, u32, vp, vp, vp, sz, vp]
         L.ksj_gpu_direct_forward.restype = ctypes.c_int32
         L.ksj_gpu_direct_forward.argtypes = [u32, u32, ctypes.c_double, ctypes.c_double, u32, u32, vp, vp, vp, vp]
         L.ksj_gpu_direct_adjoint.restype = ctypes.c_int32
@@ -400,6 +404,25 @@ def direct_forward(image: torch.Tensor, traj: torch.Tensor, origin: tuple[float,
                                         traj.contiguous().data_ptr(), out.data_ptr(), _stream(stream)),
            "direct_forward")
     return out
+
+
+def cartesian_ifft2(kspace: torch.Tensor, output: int = OUTPUT_COIL_LAST, stream=None) -> torch.Tensor:
+    """cartesian_ifft2_coil_images: kspace [F, C, rows, cols] (or [C, rows, cols]) complex64 channel-major ->
+    coil-last images [F, rows, cols, C] complex64, or RSS [F, rows, cols] float32 (leading F dropped if absent)."""
+    k = kspace if kspace.dim() == 4 else kspace.unsqueeze(0)
+    f, c, rows, cols = k.shape
+    L = lib()
+    n = int(L.ksj_gpu_cartesian_workspace_bytes(rows, cols, c, f))
+    if n == 0:
+        raise GpuError(1, "cartesian_workspace_bytes")
+    ws = torch.empty(n, dtype=torch.uint8, device=k.device)
+    if output == OUTPUT_RSS:
+        out = torch.empty((f, rows, cols), dtype=torch.float32, device=k.device)
+    else:
+        out = torch.empty((f, rows, cols, c), dtype=torch.complex64, device=k.device)
+    _check(L.ksj_gpu_cartesian_ifft2(rows, cols, c, f, output, k.contiguous().data_ptr(), out.data_ptr(),
+                                     ws.data_ptr(), ws.numel(), _stream(stream)), "cartesian_ifft2")
+    return out if kspace.dim() == 4 else out[0]
 
 
 def walsh_combine(coil_last: torch.Tensor, window: int = 7, iterations: int = 24, stream=None) -> torch.Tensor:

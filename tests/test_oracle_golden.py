@@ -145,3 +145,16 @@ def test_kaiser_bessel_oracle_approximates_exact_nudft(orc):
     e6 = oracle.rel_l2(orc.kb_gridding(g, n, y, tr, None, width=6), exact)
     assert e4 < 5e-3 and e6 < 2e-4 and e6 < e4 / 5
     assert orc.kb_kernel(0.0, 4, orc.kb_beta(4, 2.0)) == 1.0
+
+
+def test_cartesian_oracle_pinned_to_reference_known_answer():
+    """cartesian_recon_provider_tests.cpp:339-366: channels 2, 2 x 2, DC values
+    4 and 8i -> coil-last (1, 2i) at every pixel."""
+    from oracle.cartesian import ifft2_coil_images
+
+    k = np.zeros((2, 2, 2), dtype=np.complex64)
+    k[0, 0, 0] = 4.0
+    k[1, 0, 0] = 8.0j
+    img = ifft2_coil_images(k)
+    assert img.shape == (2, 2, 2)
+    assert np.abs(img[..., 0] - 1.0).max() <= 1e-5 and np.abs(img[..., 1] - 2.0j).max() <= 1e-5
