@@ -27,6 +27,8 @@
  *          (libs/numerics/kspacejet-nufft/include/kspacejet/nufft/direct_nudft.hpp:14-21, src/nufft.cpp:29)
  *   ksj_gpu_cartesian_ifft2
  *       <- providers/kspacejet-cartesian-recon/src/operators/cartesian_ifft2_coil_images.cpp:372-407
+ *   ksj_gpu_normalize_trajectory, ksj_gpu_aggregate_acquisitions
+ *       <- libs/recon/kspacejet-recon-runtime/src/noncartesian_rss_hdf5.cpp:776-833, 1077-1103
  *   ksj_gpu_rss_coil_last
  *       <- ksj::stats::root_sum_of_squares_across(cube, image, Dim::dim2)
  *          (libs/numerics/kspacejet-stats/include/kspacejet/stats/norms.hpp:207-218) as called by
@@ -360,6 +362,32 @@ KSJ_GPU_API ksj_gpu_status ksj_gpu_noise_prewhiten(uint32_t channels, uint32_t s
 KSJ_GPU_API ksj_gpu_status ksj_gpu_coil_compress(uint32_t channels, uint32_t virtual_channels, uint32_t samples,
                                                  const void* d_basis, const void* d_kspace, void* d_out,
                                                  void* stream);
+
+/* -------------------------------------------------------------- ingress */
+
+/* Trajectory units of the ISMRMRD route (RadialHdf5TrajectoryUnits). */
+#define KSJ_GPU_TRAJ_CYCLES_PER_FOV 1u       /* |k| <= 0.5, scaled by 2 pi */
+#define KSJ_GPU_TRAJ_RADIANS_PER_PIXEL 2u    /* |k| <= pi, unscaled */
+#define KSJ_GPU_TRAJ_ENCODED_MATRIX_INDEX 3u /* |k| <= encoded / 2, scaled by 2 pi / encoded */
+
+/* ISMRMRD [kx, ky] float32 pairs -> [row = ky, column = kx] radians per pixel
+ * (libs/recon/kspacejet-recon-runtime/src/noncartesian_rss_hdf5.cpp:776-833),
+ * on the device so the trajectory stays resident: each raw coordinate checked
+ * (finite, inside its unit's inclusive Nyquist interval; a failure ORs
+ * KSJ_GPU_FLAG_BAD_TRAJECTORY into *d_flags) and scaled with the reference's
+ * float factor in one rounded multiply (bit-identical).  encoded_rows /
+ * encoded_cols are the XML encoded dimensions (used by
+ * KSJ_GPU_TRAJ_ENCODED_MATRIX_INDEX, >= 2). */
+KSJ_GPU_API ksj_gpu_status ksj_gpu_normalize_trajectory(uint32_t samples, uint32_t units, uint32_t encoded_rows,
+                                                        uint32_t encoded_cols, const float* d_raw, float* d_out,
+                                                        uint32_t* d_flags, void* stream);
+
+/* Per-acquisition channel-major blocks complex64 [acquisition][channel][n] ->
+ * one channel-major frame [channel][acquisition * n]
+ * (noncartesian_rss_hdf5.cpp:1077-1083, acquisitions of equal length). */
+KSJ_GPU_API ksj_gpu_status ksj_gpu_aggregate_acquisitions(uint32_t acquisitions, uint32_t channels,
+                                                          uint32_t samples_per_acquisition, const void* d_in,
+                                                          void* d_out, void* stream);
 
 /* ------------------------------------------------- Cartesian coil images */
 

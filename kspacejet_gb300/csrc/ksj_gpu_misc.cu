@@ -189,6 +189,40 @@ __global__ void __launch_bounds__(kForwardSamples) k_direct_forward(const float2
   }
 }
 
+// ------------------------------------------------------------- ingress
+
+// ISMRMRD trajectories [kx, ky] -> the reconstruction's [row = ky, column =
+// kx] in radians per pixel (noncartesian_rss_hdf5.cpp:776-833): each raw
+// coordinate is checked (finite, inside its unit's inclusive Nyquist
+// interval) and scaled by its axis's float factor with one rounded multiply,
+// as the reference does.  A failing sample raises KSJ_GPU_FLAG_BAD_TRAJECTORY
+// in *flags (its output is still written).
+__global__ void __launch_bounds__(256) k_normalize_trajectory(const float2* __restrict__ raw, float2* out, int m,
+                                                              float row_limit, float col_limit, float row_scale,
+                                                              float col_scale, uint32_t* flags) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= m) return;
+  const float2 k = raw[s];  // (kx, ky)
+  const bool ok = isfinite(k.x) && isfinite(k.y) && fabsf(k.x) <= col_limit && fabsf(k.y) <= row_limit;
+  if (!ok) atomicOr(flags, KSJ_GPU_FLAG_BAD_TRAJECTORY);
+  out[s] = make_float2(__fmul_rn(k.y, row_scale), __fmul_rn(k.x, col_scale));
+}
+
+// Per-acquisition channel-major blocks [acquisition][channel][n] ->
+// [channel][acquisition * n] (noncartesian_rss_hdf5.cpp:1077-1083), 16-byte
+// vectors where n allows.
+__global__ void __launch_bounds__(256) k_aggregate_acquisitions(const float2* __restrict__ in, float2* out,
+                                                                int acquisitions, int channels, int n) {
+  const size_t total = static_cast<size_t>(acquisitions) * channels * n;
+  for (size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < total;
+       i += static_cast<size_t>(gridDim.x) * blockDim.x) {
+    const size_t a = i / (static_cast<size_t>(channels) * n);
+    const size_t rem = i - a * channels * n;
+    const size_t c = rem / n, j = rem - c * n;
+    out[(c * acquisitions + a) * n + j] = in[i];
+  }
+}
+
 // --------------------------------------------------------------------- RSS
 
 // out[p] = sqrt(sum_c re^2 + im^2), a float sum in channel order with every
@@ -287,6 +321,57 @@ extern "C" ksj_gpu_status ksj_gpu_direct_forward(uint32_t rows, uint32_t cols, d
                                                      static_cast<float2*>(d_out), static_cast<int>(rows),
                                                      static_cast<int>(cols), ro, co, static_cast<int>(channels),
                                                      static_cast<int>(samples));
+  return check_launch();
+}
+
+extern "C" ksj_gpu_status ksj_gpu_normalize_trajectory(uint32_t samples, uint32_t units, uint32_t encoded_rows,
+                                                       uint32_t encoded_cols, const float* d_raw, float* d_out,
+                                                       uint32_t* d_flags, void* stream) {
+  if (samples == 0 || d_raw == nullptr || d_out == nullptr || d_flags == nullptr) return KSJ_GPU_ERROR_INVALID_ARGUMENT;
+  constexpr float kPi = 3.14159265358979323846f;
+  const float two_pi = 2.0f * kPi;  // the reference's 2.0F * pi_v<float>, rounded once
+  float row_limit, col_limit, row_scale, col_scale;
+  switch (units) {
+    case KSJ_GPU_TRAJ_CYCLES_PER_FOV:
+      row_limit = col_limit = 0.5f;
+      row_scale = col_scale = two_pi;
+      break;
+    case KSJ_GPU_TRAJ_RADIANS_PER_PIXEL:
+      row_limit = col_limit = kPi;
+      row_scale = col_scale = 1.0f;
+      break;
+    case KSJ_GPU_TRAJ_ENCODED_MATRIX_INDEX:
+      if (encoded_rows < 2 || encoded_cols < 2) return KSJ_GPU_ERROR_INVALID_ARGUMENT;
+      row_limit = static_cast<float>(encoded_rows) / 2.0f;
+      col_limit = static_cast<float>(encoded_cols) / 2.0f;
+      row_scale = two_pi / static_cast<float>(encoded_rows);
+      col_scale = two_pi / static_cast<float>(encoded_cols);
+      break;
+    default:
+      return KSJ_GPU_ERROR_INVALID_ARGUMENT;  // unspecified or unknown units
+  }
+  cudaStream_t cs = static_cast<cudaStream_t>(stream);
+  LaunchScope scope("k_normalize_trajectory", cs);
+  k_normalize_trajectory<<<(samples + 255) / 256, 256, 0, cs>>>(reinterpret_cast<const float2*>(d_raw),
+                                                                 reinterpret_cast<float2*>(d_out),
+                                                                 static_cast<int>(samples), row_limit, col_limit,
+                                                                 row_scale, col_scale, d_flags);
+  return check_launch();
+}
+
+extern "C" ksj_gpu_status ksj_gpu_aggregate_acquisitions(uint32_t acquisitions, uint32_t channels,
+                                                         uint32_t samples_per_acquisition, const void* d_in,
+                                                         void* d_out, void* stream) {
+  if (acquisitions == 0 || channels == 0 || samples_per_acquisition == 0 || d_in == nullptr || d_out == nullptr)
+    return KSJ_GPU_ERROR_INVALID_ARGUMENT;
+  const size_t total = static_cast<size_t>(acquisitions) * channels * samples_per_acquisition;
+  if (total > (static_cast<size_t>(1) << 34)) return KSJ_GPU_ERROR_UNSUPPORTED;
+  cudaStream_t cs = static_cast<cudaStream_t>(stream);
+  const unsigned blocks = static_cast<unsigned>(std::min<size_t>((total + 255) / 256, 152 * 16));
+  LaunchScope scope("k_aggregate_acquisitions", cs);
+  k_aggregate_acquisitions<<<blocks, 256, 0, cs>>>(static_cast<const float2*>(d_in), static_cast<float2*>(d_out),
+                                                   static_cast<int>(acquisitions), static_cast<int>(channels),
+                                                   static_cast<int>(samples_per_acquisition));
   return check_launch();
 }
 

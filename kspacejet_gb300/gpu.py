@@ -76,6 +76,10 @@ def lib() -> ctypes.CDLL:
                                             ctypes.POINTER(GriddingTuning)]
         L.ksj_gpu_direct_workspace_bytes.restype = sz
         L.ksj_gpu_direct_workspace_bytes.argtypes = [u32, u32, u32]
+        L.ksj_gpu_normalize_trajectory.restype = ctypes.c_int32
+        L.ksj_gpu_normalize_trajectory.argtypes = [u32, u32, u32, u32, vp, vp, vp, vp]
+        L.ksj_gpu_aggregate_acquisitions.restype = ctypes.c_int32
+        L.ksj_gpu_aggregate_acquisitions.argtypes = [u32, u32, u32, vp, vp, vp]
         L.ksj_gpu_cartesian_workspace_bytes.restype = sz
         L.ksj_gpu_cartesian_workspace_bytes.argtypes = [u32, u32, u32, u32]
         L.ksj_gpu_cartesian_ifft2.restype = ctypes.c_int32
@@ -403,6 +407,30 @@ def direct_forward(image: torch.Tensor, traj: torch.Tensor, origin: tuple[float,
     _check(lib().ksj_gpu_direct_forward(rows, cols, ro, co, c, m, image.contiguous().data_ptr(),
                                         traj.contiguous().data_ptr(), out.data_ptr(), _stream(stream)),
            "direct_forward")
+    return out
+
+
+TRAJ_CYCLES_PER_FOV, TRAJ_RADIANS_PER_PIXEL, TRAJ_ENCODED_MATRIX_INDEX = 1, 2, 3
+
+
+def normalize_trajectory(raw: torch.Tensor, units: int, encoded: tuple[int, int] = (0, 0),
+                         stream=None) -> tuple[torch.Tensor, int]:
+    """ISMRMRD [M, 2] (kx, ky) float32 on the GPU -> ([M, 2] (row = ky, column = kx) radians per pixel, flags)."""
+    m = raw.shape[0]
+    out = torch.empty((m, 2), dtype=torch.float32, device=raw.device)
+    flags = torch.zeros(1, dtype=torch.int32, device=raw.device)
+    _check(lib().ksj_gpu_normalize_trajectory(m, units, encoded[0], encoded[1], raw.contiguous().data_ptr(),
+                                              out.data_ptr(), flags.data_ptr(), _stream(stream)),
+           "normalize_trajectory")
+    return out, int(flags.item())
+
+
+def aggregate_acquisitions(blocks: torch.Tensor, stream=None) -> torch.Tensor:
+    """Per-acquisition channel-major blocks [A, C, n] complex64 -> one channel-major frame [C, A * n]."""
+    a, c, n = blocks.shape
+    out = torch.empty((c, a * n), dtype=torch.complex64, device=blocks.device)
+    _check(lib().ksj_gpu_aggregate_acquisitions(a, c, n, blocks.contiguous().data_ptr(), out.data_ptr(),
+                                                _stream(stream)), "aggregate_acquisitions")
     return out
 
 

@@ -158,3 +158,23 @@ def test_cartesian_oracle_pinned_to_reference_known_answer():
     img = ifft2_coil_images(k)
     assert img.shape == (2, 2, 2)
     assert np.abs(img[..., 0] - 1.0).max() <= 1e-5 and np.abs(img[..., 1] - 2.0j).max() <= 1e-5
+
+
+def test_ingress_oracle_pinned_to_reference_unit_equivalence():
+    """radial_rss_hdf5_tests.cpp:353-390: cycles per FOV 0.5, radians per
+    pixel pi and encoded index 1 on a 2 x 2 matrix are the same coordinate
+    (float pi), and raw [kx, ky] lands as [row = ky, column = kx]
+    (:136-144)."""
+    from oracle import ingress
+
+    pi_f = np.float32(np.pi)
+    for units, v in ((ingress.CYCLES_PER_FOV, 0.5), (ingress.RADIANS_PER_PIXEL, float(pi_f)),
+                     (ingress.ENCODED_MATRIX_INDEX, 1.0)):
+        out, ok = ingress.normalize_trajectory(np.array([[v, 0.0], [-v, 0.0]], dtype=np.float32), units, 2, 2)
+        assert ok.all()
+        assert out[0, 1] == pi_f and out[1, 1] == -pi_f and out[0, 0] == 0.0
+    out, ok = ingress.normalize_trajectory(np.array([[-0.25, 0.125]], dtype=np.float32), ingress.CYCLES_PER_FOV)
+    assert out[0, 0] == np.float32(0.125) * np.float32(2 * pi_f) and out[0, 1] == np.float32(-0.25) * np.float32(2 * pi_f)
+    _, ok = ingress.normalize_trajectory(np.array([[0.5000001, 0.0], [np.nan, 0.0]], dtype=np.float32),
+                                         ingress.CYCLES_PER_FOV)
+    assert not ok.any()
