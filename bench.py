@@ -694,6 +694,25 @@ def run_rows(args) -> list[dict]:
                   "config": {"workload": "128 x 128 image, 8 coils, 34 x 256 golden-angle samples",
                              "complex_macs": pairs * 8}})
 
+    # Kaiser-Bessel forward NUFFT on the batched shape: 96 frames of 192^2 x 32 coil images -> 34 x 384 samples
+    trh, _ = make_inputs()
+    trk = torch.from_numpy(trh).to(dev)
+    fop = gpu.kb_gridding(image=IMAGE, grid=GRID, channels=COILS, samples=trh.shape[1], frames=FRAMES, width=WIDTH,
+                          dcf=gpu.DCF_NONE, output=gpu.OUTPUT_COIL_LAST)
+    fimg = torch.randn((FRAMES, IMAGE, IMAGE, COILS), dtype=torch.complex64, device=dev)
+    fws = torch.empty(fop.forward_workspace_bytes(), dtype=torch.uint8, device=dev)
+    gpu.timing_reset()
+    gpu.timing_enable(True)
+    ms = _time_gpu(lambda: fop.forward(fimg, trk, fws), w, s)
+    kern = {n_: round(t_ / c_, 4) for n_, c_, t_ in gpu.timing_read()}
+    gpu.timing_enable(False)
+    lines.append({"metric": "Kaiser-Bessel forward NUFFT: samples/s", "value": FRAMES * COILS * trh.shape[1] / (ms / 1e3),
+                  "unit": "samples/s", "ms_per_call": ms, "dtype": "f32",
+                  "config": {"workload": f"{FRAMES} frames x {COILS} coils, {IMAGE}^2 images -> {SPOKES} x {READOUT} "
+                                         f"samples per frame, KB W={WIDTH}, grid {GRID}"},
+                  "kernels_ms": kern})
+    del fimg, fws
+
     # Cartesian coil images: 8 frames x 32 coils x 256 x 256, coil-last output
     kc = torch.from_numpy((rng.standard_normal((8, 32, 256, 256)) + 1j * rng.standard_normal((8, 32, 256, 256))).astype(np.complex64)).to(dev)
     ms = _time_gpu(lambda: gpu.cartesian_ifft2(kc), w, s)

@@ -250,6 +250,24 @@ KSJ_GPU_API ksj_gpu_status ksj_gpu_direct_adjoint(uint32_t rows, uint32_t cols, 
                                                   const float* d_traj, void* d_out, void* d_workspace,
                                                   size_t workspace_bytes, void* stream);
 
+/* Kaiser-Bessel forward NUFFT: the exact transpose of ksj_gpu_gridding_adjoint
+ * with KSJ_GPU_KERNEL_KAISER_BESSEL and no density weights (the same taps,
+ * weights, phase, crop positions and deapodisation), i.e. the fast
+ * approximation of ksj_gpu_direct_forward that the gridding adjoint pairs
+ * with.  desc: kernel KAISER_BESSEL, square image and grid (grid <= 512,
+ * 2^a or 3 * 2^a), width 2/4/6/8, complex64 samples; dcf_mode and output are
+ * ignored.  d_image complex64 coil-last [frame][row][col][channel]; d_traj
+ * [frame][sample][2]; d_samples complex64 [frame][channel][sample].  A
+ * non-finite or far out-of-range coordinate gives 0 and raises
+ * KSJ_GPU_FLAG_BAD_TRAJECTORY (ksj_gpu_read_flags on the workspace).
+ * Workspace: ksj_gpu_kb_forward_workspace_bytes (the row-transformed image
+ * and the transformed grid, frames x grid^2 x channels complex64).  No
+ * counterpart in the reference (its forward is the direct NUDFT, or BART). */
+KSJ_GPU_API size_t ksj_gpu_kb_forward_workspace_bytes(const ksj_gpu_gridding_desc* desc);
+KSJ_GPU_API ksj_gpu_status ksj_gpu_kb_forward(const ksj_gpu_gridding_desc* desc, const void* d_image,
+                                              const float* d_traj, void* d_samples, void* d_workspace,
+                                              size_t workspace_bytes, void* stream);
+
 /* Exact direct forward NUDFT (the reference's nufft2_forward on its Eigen
  * backend, nufft.cpp:29 -> eigen_nufft_direct_nudft.cpp:51-74), per channel:
  *   y(c)(s) = sum_{r, col} x(c)(r, col) exp(-i (k_row,s (r - row_origin) + k_col,s (col - col_origin)))

@@ -38,7 +38,7 @@ NVCC_FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-
 CXX_FLAGS = ["-std=c++20", "-O2", "-fPIC", "-fvisibility=hidden", "-Wall", "-Wno-unused-const-variable",
              "-I" + str(INCLUDE)]
 
-CU_SOURCES = ["ksj_gpu_gridding.cu", "ksj_gpu_misc.cu", "ksj_gpu_combine.cu", "ksj_serve.cu"]
+CU_SOURCES = ["ksj_gpu_gridding.cu", "ksj_gpu_misc.cu", "ksj_gpu_combine.cu", "ksj_gpu_forward.cu", "ksj_serve.cu"]
 GPU_HEADERS = [CSRC / "ksj_gpu_internal.cuh", INCLUDE / "ksj_gpu.h", INCLUDE / "ksj_serve.h"]
 PLUGIN_HEADERS = [CSRC / "provider/abi_support.hpp", INCLUDE / "ksj_provider_abi.h", INCLUDE / "ksj_gpu.h"]
 

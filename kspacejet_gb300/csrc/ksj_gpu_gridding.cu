@@ -358,23 +358,7 @@ __global__ void k_tables(float2* tw_rows, int grid_rows, float2* tw_cols, int gr
   if (i < out_cols) pos_cols[i] = dif_position(plan_cols, source(i, out_cols, grid_cols));
   if (i < grid_rows) tw_rows[i] = twiddle(i, grid_rows);
   if (i < grid_cols) tw_cols[i] = twiddle(i, grid_cols);
-  auto inv_psi = [&](int p, int n, int g) -> float {
-    if (!kb) return 1.0f;
-    const double q = static_cast<double>(p - n / 2);
-    const double a = 3.14159265358979323846 * width * q / g;
-    const double z2 = beta * beta - a * a;
-    double shape;
-    if (z2 > 1e-12) {
-      const double z = sqrt(z2);
-      shape = sinh(z) / z;
-    } else if (z2 < -1e-12) {
-      const double z = sqrt(-z2);
-      shape = sin(z) / z;
-    } else {
-      shape = 1.0;
-    }
-    return static_cast<float>(i0_beta / (width * shape));
-  };
+  auto inv_psi = [&](int p, int n, int g) -> float { return kb ? kb_inv_deapod(p, n, g, width, beta, i0_beta) : 1.0f; };
   if (i < out_rows) inv_dr[i] = inv_psi(i, out_rows, grid_rows);
   if (i < out_cols) inv_dc[i] = inv_psi(i, out_cols, grid_cols);
 }

@@ -8,6 +8,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <cmath>
+
 #include "ksj_gpu.h"
 
 namespace ksj_gpu {
@@ -165,6 +167,36 @@ __device__ __forceinline__ float kb_weight(float d, float two_over_w, float beta
   const float t = d * two_over_w;
   const float a = fmaxf(fmaf(-t, t, 1.0f), 0.0f);
   return cyl_bessel_i0f(beta * sqrtf(a)) * inv_i0_beta;
+}
+
+// 1 / psi(q) for kept pixel p of n (q = p - n/2) on a grid of g: psi the
+// continuous Fourier transform of the normalised Kaiser-Bessel kernel,
+// W sinh(z)/z / I0(beta), z = sqrt(beta^2 - (pi W q / g)^2) (Jackson et al.
+// 1991), evaluated in FP64 and rounded once.
+__device__ __forceinline__ float kb_inv_deapod(int p, int n, int g, int width, double beta, double i0_beta) {
+  const double q = static_cast<double>(p - n / 2);
+  const double a = 3.14159265358979323846 * width * q / g;
+  const double z2 = beta * beta - a * a;
+  double shape;
+  if (z2 > 1e-12) {
+    const double z = sqrt(z2);
+    shape = sinh(z) / z;
+  } else if (z2 < -1e-12) {
+    const double z = sqrt(-z2);
+    shape = sin(z) / z;
+  } else {
+    shape = 1.0;
+  }
+  return static_cast<float>(i0_beta / (width * shape));
+}
+
+// The default Kaiser-Bessel shape for width W and oversampling sigma (Beatty
+// et al. 2005): pi sqrt((W / sigma)^2 (sigma - 1/2)^2 - 0.8); 0 when that is
+// not real.
+inline double kb_default_beta(int width, double sigma) {
+  const double a = (static_cast<double>(width) / sigma) * (sigma - 0.5);
+  const double arg = a * a - 0.8;
+  return arg > 0.0 ? 3.14159265358979323846 * std::sqrt(arg) : 0.0;
 }
 
 // ----------------------------------------------------------------- bfloat16

@@ -84,6 +84,10 @@ def lib() -> ctypes.CDLL:
         L.ksj_gpu_cartesian_workspace_bytes.argtypes = [u32, u32, u32, u32]
         L.ksj_gpu_cartesian_ifft2.restype = ctypes.c_int32
         L.ksj_gpu_cartesian_ifft2.argtypes = [u32, u32, u32, u32, u32, vp, vp, vp, sz, vp]
+        L.ksj_gpu_kb_forward_workspace_bytes.restype = sz
+        L.ksj_gpu_kb_forward_workspace_bytes.argtypes = [ctypes.POINTER(GriddingDesc)]
+        L.ksj_gpu_kb_forward.restype = ctypes.c_int32
+        L.ksj_gpu_kb_forward.argtypes = [ctypes.POINTER(GriddingDesc), vp, vp, vp, vp, sz, vp]
         L.ksj_gpu_direct_forward.restype = ctypes.c_int32
         L.ksj_gpu_direct_forward.argtypes = [u32, u32, ctypes.c_double, ctypes.c_double, u32, u32, vp, vp, vp, vp]
         L.ksj_gpu_direct_adjoint.restype = ctypes.c_int32
@@ -256,6 +260,26 @@ class Gridding:
                                                  dcf.data_ptr() if dcf is not None else None, out.data_ptr(),
                                                  workspace.data_ptr(), workspace.numel(), _stream(stream))
         _check(st, "gridding_adjoint_host")
+
+    def forward_workspace_bytes(self) -> int:
+        d = self.desc()
+        n = lib().ksj_gpu_kb_forward_workspace_bytes(ctypes.byref(d))
+        if n == 0:
+            raise GpuError(1, "kb_forward_workspace_bytes")
+        return int(n)
+
+    def forward(self, image: torch.Tensor, traj: torch.Tensor, workspace: torch.Tensor | None = None,
+                stream: torch.cuda.Stream | None = None) -> torch.Tensor:
+        """ksj_gpu_kb_forward: coil-last images [F, rows, cols, C] complex64 (F may be omitted when frames == 1),
+        traj [F, M, 2] -> samples [F, C, M] complex64 (the transpose of run() without density weights)."""
+        d = self.desc()
+        if workspace is None:
+            workspace = torch.empty(self.forward_workspace_bytes(), dtype=torch.uint8, device=image.device)
+        out = torch.empty((self.frames, self.channels, self.samples), dtype=torch.complex64, device=image.device)
+        _check(lib().ksj_gpu_kb_forward(ctypes.byref(d), image.contiguous().data_ptr(), traj.contiguous().data_ptr(),
+                                        out.data_ptr(), workspace.data_ptr(), workspace.numel(), _stream(stream)),
+               "kb_forward")
+        return out
 
     def flags(self, workspace: torch.Tensor, stream: torch.cuda.Stream | None = None) -> int:
         v = ctypes.c_uint32()

@@ -200,6 +200,22 @@ class Oracle(_Base):
         return out
 
 
+    def kb_forward(self, grid: int, n: int, image: np.ndarray, traj: np.ndarray, width: int = 4,
+                   sigma: float | None = None, beta: float | None = None) -> np.ndarray:
+        """Kaiser-Bessel forward in double precision (one coil, origin (n-1)/2): the exact transpose of
+        kb_gridding without density weights."""
+        image = np.ascontiguousarray(image, dtype=np.complex128)
+        traj = np.ascontiguousarray(traj, dtype=np.float64)
+        if beta is None:
+            beta = self.kb_beta(width, sigma if sigma is not None else grid / n)
+        out = np.zeros(traj.shape[0], dtype=np.complex128)
+        fn = self._fn("kb_forward2_f64", ctypes.c_int,
+                      [_i64, _i64, ctypes.c_int, _dbl, _dbl, _dbl, _ptr, _ptr, _i64, _ptr])
+        rc = fn(grid, n, width, beta, (n - 1) / 2.0, (n - 1) / 2.0, _p(image), _p(traj), traj.shape[0], _p(out))
+        if rc != 0:
+            raise OracleError("KB forward rejected its configuration")
+        return out
+
     def pipe_menon_dcf(self, traj: np.ndarray, grid_rows: int, grid_cols: int, width: int = 4,
                        beta: float | None = None, sigma: float = 2.0, iterations: int = 10) -> np.ndarray:
         """Pipe-Menon density compensation, grid-based, double precision (one frame)."""

@@ -570,6 +570,56 @@ KSJO_EXPORT int ksjo_kb_gridding2_adjoint_f64(int64_t g, int64_t n, int width, d
   return 0;
 }
 
+/* Kaiser-Bessel forward (double precision): the exact transpose of
+ * ksjo_kb_gridding2_adjoint_f64 without density weights.  image n x n ->
+ * deapodised (1 / (psi(q_r) psi(q_c))), placed at grid (q_r mod g, q_c mod g),
+ * q = p - n/2; forward 2-D DFT exp(-2 pi i (k . j) / g) (exact, directly
+ * evaluated); per sample y = conj(exp(i k . delta)) sum over the taps
+ * (row-major) of phi(j_r - u_r) phi(j_c - u_c) grid[j_r mod g][j_c mod g]. */
+KSJO_EXPORT int ksjo_kb_forward2_f64(int64_t g, int64_t n, int width, double beta, double row_origin,
+                                     double col_origin, const double* image_in, const double* traj, int64_t m,
+                                     double* samples_out) {
+  if (g < n || g < width || (width % 2) != 0) return -1;
+  const cf64* image = (const cf64*)image_in;
+  cf64* samples = (cf64*)samples_out;
+  cf64* grid = (cf64*)calloc((size_t)(g * g), sizeof(cf64));
+  for (int64_t pr = 0; pr < n; ++pr) {
+    const int64_t qr = pr - n / 2;
+    const double ar = ksjo_kb_deapod((double)qr, width, beta, g);
+    for (int64_t pc = 0; pc < n; ++pc) {
+      const int64_t qc = pc - n / 2;
+      const double ac = ksjo_kb_deapod((double)qc, width, beta, g);
+      const cf64 x = cscale_d(image[pr * n + pc], 1.0 / (ar * ac));
+      grid[(((qr % g) + g) % g) * g + (((qc % g) + g) % g)] = (cf64){x.re, -x.im};  /* conj */
+    }
+  }
+  idft2_rows_cols_f64(grid, g, g, 1);  /* conj(IDFT(conj x)) = DFT x */
+  for (int64_t i = 0; i < g * g; ++i) grid[i].im = -grid[i].im;
+  const double half = (double)(n / 2);
+  const double dr = half - row_origin, dc = half - col_origin;
+  for (int64_t s = 0; s < m; ++s) {
+    const double kr = traj[2 * s], kc = traj[2 * s + 1];
+    const double ur = kr * (double)g / (2.0 * kPiD), uc = kc * (double)g / (2.0 * kPiD);
+    const double ph = kr * dr + kc * dc;
+    const cf64 e = {cos(ph), -sin(ph)};
+    const int64_t r0 = (int64_t)floor(ur) - width / 2 + 1;
+    const int64_t c0 = (int64_t)floor(uc) - width / 2 + 1;
+    cf64 acc = {0.0, 0.0};
+    for (int a = 0; a < width; ++a) {
+      const double wr = ksjo_kb_kernel((double)(r0 + a) - ur, width, beta);
+      const int64_t rr = (((r0 + a) % g) + g) % g;
+      for (int b = 0; b < width; ++b) {
+        const double wc = ksjo_kb_kernel((double)(c0 + b) - uc, width, beta);
+        const int64_t cc = (((c0 + b) % g) + g) % g;
+        acc = cadd_d(acc, cscale_d(grid[rr * g + cc], wr * wc));
+      }
+    }
+    samples[s] = cmul_d(acc, e);
+  }
+  free(grid);
+  return 0;
+}
+
 /* ------------------------------------------------------------ Pipe-Menon */
 
 /* Iterative density compensation (Pipe & Menon, MRM 41:179-186, 1999) in
