@@ -299,9 +299,7 @@ def run_ours(args) -> dict | None:
     # launches inside the timed region: a graph replays the captured call's launches
     per_call_launches = None
 
-    # ---- the same call issued directly, with per-kernel event timing (roofline)
-    gpu.timing_reset()
-    gpu.timing_enable(True)
+    # ---- the same call issued directly (launch count; the ncu launch list's range)
     l0 = gpu.launch_count()
     d0 = torch.cuda.Event(enable_timing=True)
     d1 = torch.cuda.Event(enable_timing=True)
@@ -314,6 +312,19 @@ def run_ours(args) -> dict | None:
         torch.cuda.synchronize()
     torch.cuda.nvtx.range_pop()
     per_call_launches = (gpu.launch_count() - l0) // args.steps
+    # ---- per-kernel event timing (roofline): the tuned call with all frames in one
+    # pass, so no two of its launches overlap and each launch's events time it alone
+    # (the tuned call may run two passes concurrently on two streams)
+    tuning_k = gpu.GriddingTuning(ctypes.sizeof(gpu.GriddingTuning), tuning.coil_group, tuning.column_block,
+                                  tuning.list_capacity, 0, tuning.rows_blocks_per_sm, tuning.coil_parts)
+    for _ in range(2):
+        g.run(k, t, out, ws, tuning=tuning_k)
+    torch.cuda.synchronize()
+    gpu.timing_reset()
+    gpu.timing_enable(True)
+    for _ in range(args.steps):
+        g.run(k, t, out, ws, tuning=tuning_k)
+    torch.cuda.synchronize()
     gpu.timing_enable(False)
     kernels = gpu.timing_read()
     direct_ms = d0.elapsed_time(d1) / args.steps
@@ -400,7 +411,9 @@ def run_ours(args) -> dict | None:
         traffic = read_traffic() if name == "k_rows" else None
         roofline = {"bound": "hbm", "kernel": name, "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
                     "frac": round(ach / peak, 4), "peak_source": f"{peak_src} hbm_gbs",
-                    "algorithmic_bytes_per_launch": bytes_per.get(name), "traffic": traffic}
+                    "algorithmic_bytes_per_launch": bytes_per.get(name), "traffic": traffic,
+                    "timing": "CUDA events around each launch of the tuned call run with all frames in one "
+                              "pass (no concurrent launches)"}
     return {
         "metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
