@@ -110,10 +110,7 @@ typedef struct ksj_gpu_gridding_tuning {
   uint32_t column_block;    /* columns per column-pass tile: a power of two (1..32) */
   uint32_t list_capacity;   /* per-warp sorted-list buffer, entries (power of two, 64..2048) */
   uint32_t frames_per_pass; /* frames per row/column pass (the row-transformed grid of one pass stays in L2) */
-  uint32_t rows_blocks_per_sm; /* 1 or 2 resident row CTAs per SM (2 caps registers at 80 per thread);
-                                   3: the pipelined row pass (one persistent CTA per SM, gridding and
-                                   transform warps on alternate row buffers; 32-coil groups, two-step
-                                   row lengths up to 384) */
+  uint32_t rows_blocks_per_sm; /* 1 or 2 resident row CTAs per SM (2 caps registers at 80 per thread) */
   uint32_t coil_parts;      /* 1 or 2: a row CTA's coil group is split into this many independent list tasks */
 } ksj_gpu_gridding_tuning;
 

@@ -99,40 +99,7 @@ inline size_t rows_smem_for(int grid_cols, int cg, int width, int threads) {
 }
 inline int rows_threads_for(int grid_cols) { return std::max(64, (grid_cols + 31) / 32 * 32); }
 
-// Warps and shared memory of the pipelined row pass (k_rows_pipe).
-constexpr uint32_t kWaitLimit = 1u << 22;  // mbarrier polls before a wait gives up
-constexpr int kPipeGridWarps = 16;
-constexpr int kPipeFftWarps = 8;
-constexpr int kPipeThreads = 32 * (kPipeGridWarps + kPipeFftWarps);
-constexpr int kPipeFftBar = 1;  // named barrier of the transform warps
-
-struct PipeSmem {
-  size_t acc, tw, meta, bars, ctl, total;
-};
-__host__ __device__ inline PipeSmem pipe_smem_for(int grid_cols, int width) {
-  PipeSmem l{};
-  size_t off = 0;
-  auto take = [&](size_t bytes) {
-    const size_t at = off;
-    off = (off + bytes + 15) & ~size_t{15};
-    return at;
-  };
-  l.acc = take(static_cast<size_t>(2) * grid_cols * 32 * sizeof(float2));
-  l.tw = take(static_cast<size_t>(grid_cols) * sizeof(float2));
-  l.meta = take(static_cast<size_t>(kPipeGridWarps) * meta_batch(width) * meta_vecs(width) * 16);
-  l.bars = take(4 * sizeof(uint64_t));
-  l.ctl = take(4 * sizeof(int));
-  l.total = off;
-  return l;
-}
-
-// The pipelined form takes rows of a two-step length up to 384 columns with
-// 32-coil groups taken whole.
-inline bool pipe_eligible(int grid_cols, int width, int coil_group, int coil_parts) {
-  return coil_group == 32 && coil_parts == 1 && has_two_step_rows(grid_cols) && grid_cols <= 384 &&
-         pipe_smem_for(grid_cols, width).total <= 227 * 1024;
-}
-
+constexpr uint32_t kWaitLimit = 1u << 22;  // polls before a bounded wait gives up
 
 struct Shape {
   int frames, channels, samples;
@@ -292,12 +259,11 @@ ksj_gpu_status make_shape(const ksj_gpu_gridding_desc* d, const ksj_gpu_gridding
   // default: two row CTAs per SM wherever the row kernel fits them (384
   // threads; the coil group above was sized for two CTAs' shared memory)
   if (rb == 0) rb = rows_threads_for(s->grid_cols) <= 384 && rows_smem(cg) <= 115712 ? 2 : 1;
-  if (rb != 1 && rb != 2 && rb != 3) return KSJ_GPU_ERROR_INVALID_ARGUMENT;
+  if (rb != 1 && rb != 2) return KSJ_GPU_ERROR_INVALID_ARGUMENT;
   s->rows_blocks = rb;
   int parts = has(offsetof(ksj_gpu_gridding_tuning, coil_parts) + 4) ? static_cast<int>(t->coil_parts) : 0;
   if (parts == 0) parts = 1;
   if ((parts != 1 && parts != 2) || parts > cg) return KSJ_GPU_ERROR_INVALID_ARGUMENT;
-  if (rb == 3 && !pipe_eligible(s->grid_cols, s->width, cg, parts)) return KSJ_GPU_ERROR_INVALID_ARGUMENT;
   s->coil_parts = parts;
   return KSJ_GPU_OK;
 }
@@ -1072,136 +1038,6 @@ __device__ __forceinline__ void rows_grid_regs(const RowsArgs& a, int f, int cgi
   }
 }
 
-// ---- the pipelined row pass (persistent, warp-specialised) ----------------
-//
-// One CTA per SM walks row units u = blockIdx.x, blockIdx.x + gridDim.x, ...
-// (unit = (frame, coil group, grid row), rows fastest) with two row buffers:
-// kPipeGridWarps warps grid unit i into buffer i & 1 while kPipeFftWarps
-// warps transform unit i - 1 from the other buffer and write its kept
-// columns.  Gridding warps take the row's chunks longest first from the
-// buffer's task counter and, done with the row, arrive on full[b]; they wait
-// on empty[b] before gridding into it again.  The transform warps wait on
-// full[b], reset the buffer's counter, transform (their own named barrier
-// between the two steps), and arrive on empty[b].  A warp that finishes its
-// lists moves on to the next row instead of waiting for the row's longest
-// list.  Every wait is bounded: on a timeout the waiting warps raise
-// KSJ_GPU_FLAG_WAIT_TIMEOUT and leave (the transform warps together, through
-// a shared abort flag read after their barrier).  Same per-cell order and
-// per-line transform arithmetic as k_rows: the same bytes.
-template <int W, uint32_t kFormat>
-__global__ void __launch_bounds__(kPipeThreads, 1) k_rows_pipe(RowsArgs a, int units) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  constexpr int kMV = meta_vecs(W);
-  constexpr int kBatch = meta_batch(W);
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int gcols = a.grid_cols;
-  const PipeSmem L = pipe_smem_for(gcols, W);
-  float2* acc_base = reinterpret_cast<float2*>(smem_raw + L.acc);
-  float2* tw = reinterpret_cast<float2*>(smem_raw + L.tw);
-  uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + L.bars);  // full[0], full[1], empty[0], empty[1]
-  int* ctl = reinterpret_cast<int*>(smem_raw + L.ctl);              // task counter per buffer, abort flag
-  const int groups = (a.channels + 31) / 32;
-  for (int i = tid; i < gcols; i += blockDim.x) tw[i] = a.tw_cols[i];
-  if (tid == 0) {
-    mbar_init(&bars[0], kPipeGridWarps);
-    mbar_init(&bars[1], kPipeGridWarps);
-    mbar_init(&bars[2], kPipeFftWarps);
-    mbar_init(&bars[3], kPipeFftWarps);
-    ctl[0] = 0;
-    ctl[1] = 0;
-    ctl[2] = 0;
-    mbar_init_fence();
-  }
-  __syncthreads();
-  auto unit_of = [&](int u, int* f, int* row, int* cgi) {
-    *row = u % a.grid_rows;
-    const int q = u / a.grid_rows;
-    *cgi = q % groups;
-    *f = a.frame0 + q / groups;
-  };
-
-  if (warp < kPipeGridWarps) {
-    float4* meta = reinterpret_cast<float4*>(smem_raw + L.meta) + warp * kBatch * kMV;
-    for (int i = 0;; ++i) {
-      const int u = i * static_cast<int>(gridDim.x) + static_cast<int>(blockIdx.x);
-      if (u >= units) break;
-      const int b = i & 1;
-      if (i >= 2 && !mbar_wait_bounded(&bars[2 + b], static_cast<uint32_t>((i >> 1) - 1) & 1u, kWaitLimit)) {
-        if (lane == 0) atomicOr(a.flags, KSJ_GPU_FLAG_WAIT_TIMEOUT);
-        return;
-      }
-      int f, row, cgi;
-      unit_of(u, &f, &row, &cgi);
-      // the row's list starts (lane c: list c; lane nchunks: the end) and its
-      // chunks longest first (a bitonic sort of length << 8 | chunk across the warp)
-      const uint32_t* off = a.offsets + static_cast<size_t>(f) * (a.lists_per_frame + 1) + row * a.nchunks;
-      const uint32_t my_off = lane <= a.nchunks ? __ldg(off + lane) : 0u;
-      const uint32_t next_off = __shfl_down_sync(0xffffffffu, my_off, 1);
-      int key = -1;
-      if (lane < a.nchunks) key = static_cast<int>(min(next_off - my_off, 1u << 22) << 8) | lane;
-#pragma unroll
-      for (int k = 2; k <= 32; k <<= 1) {
-#pragma unroll
-        for (int j = k >> 1; j > 0; j >>= 1) {
-          const int other = __shfl_xor_sync(0xffffffffu, key, j);
-          const bool lower = (lane & j) == 0;
-          const bool desc = (lane & k) == 0;
-          key = (lower == desc) ? max(key, other) : min(key, other);
-        }
-      }
-      const int coil_global = cgi * 32 + lane;
-      const bool coil_ok = coil_global < a.channels;
-      const size_t sample_base = static_cast<size_t>(f) * a.sample_frame_stride + (coil_ok ? coil_global : 0);
-      float2* acc = acc_base + static_cast<size_t>(b) * gcols * 32;
-      for (;;) {
-        int task = 0;
-        if (lane == 0) task = atomicAdd(&ctl[b], 1);
-        task = __shfl_sync(0xffffffffu, task, 0);
-        if (task >= a.nchunks) break;
-        const int chunk = __shfl_sync(0xffffffffu, key, task) & 255;
-        const uint32_t begin = __shfl_sync(0xffffffffu, my_off, chunk);
-        const int n = static_cast<int>(__shfl_sync(0xffffffffu, my_off, chunk + 1) - begin);
-        const float4* xent = a.expanded + (static_cast<size_t>(f) * a.entries_per_frame + begin) * kMV;
-        grid_chunk_regs<W, kFormat, false>(a, sample_base, coil_ok, lane, acc, chunk * kChunk, xent, n, meta);
-      }
-      __threadfence_block();
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&bars[b]);
-    }
-    return;
-  }
-
-  // transform warps
-  const int ft = tid - kPipeGridWarps * 32;
-  constexpr int nft = kPipeFftWarps * 32;
-  for (int i = 0;; ++i) {
-    const int u = i * static_cast<int>(gridDim.x) + static_cast<int>(blockIdx.x);
-    if (u >= units) break;
-    const int b = i & 1;
-    if (!mbar_wait_bounded(&bars[b], static_cast<uint32_t>(i >> 1) & 1u, kWaitLimit)) ctl[2] = 1;
-    asm volatile("bar.sync %0, %1;" ::"n"(kPipeFftBar), "n"(nft) : "memory");
-    if (ctl[2]) {
-      if (ft == 0) atomicOr(a.flags, KSJ_GPU_FLAG_WAIT_TIMEOUT);
-      return;
-    }
-    if (ft == 0) ctl[b] = 0;  // every gridding warp is done with this buffer's counter
-    int f, row, cgi;
-    unit_of(u, &f, &row, &cgi);
-    float2* acc = acc_base + static_cast<size_t>(b) * gcols * 32;
-    float2* dst_row = a.inter + (static_cast<size_t>(f) * a.grid_rows + row) * a.out_cols * a.cpitch + cgi * 32;
-    const int live_lines = min(32, a.channels - cgi * 32);
-    auto emit = [&](int k, int line, float2 v) {
-      int pc = k + a.col_shift;
-      if (pc >= gcols) pc -= gcols;
-      if (pc < a.out_cols && line < live_lines) dst_row[static_cast<size_t>(pc) * a.cpitch + line] = v;
-    };
-    fft_two_step_rows<384, kPipeFftBar>(gcols, acc, 5, tw, ft, nft, emit);
-    __threadfence_block();
-    __syncwarp();
-    if (lane == 0) mbar_arrive(&bars[2 + b]);
-  }
-}
-
 // kBlocks CTAs per SM: 2 for rows of up to 384 columns (384 threads), 1
 // above; two resident CTAs let one block's FFT overlap another's gridding.
 // kCG = 32 fixes a 32-coil group taken whole by one warp (coil_parts 1):
@@ -1582,27 +1418,15 @@ __global__ void __launch_bounds__(kColsThreads) k_cols(const __grid_constant__ C
 
 // ------------------------------------------------------------------ driver
 
-// The row-pass kernel a shape selects (rows_blocks 1 or 2: k_rows with that
-// many CTAs per SM; 3: the pipelined k_rows_pipe), its launch setup and launch.
+// The row-pass kernel a shape selects (rows_blocks: k_rows with that many
+// CTAs per SM), its launch setup and launch.
 struct RowsLauncher {
   void (*kernel)(RowsArgs) = nullptr;
-  void (*pipe)(RowsArgs, int) = nullptr;
-  int threads = 0, sms = 0;
+  int threads = 0;
   size_t smem = 0;
 
   template <int W, uint32_t kFormat>
   bool setup(const Shape& s) {
-    if (s.rows_blocks == 3) {
-      pipe = k_rows_pipe<W, kFormat>;
-      smem = pipe_smem_for(s.grid_cols, W).total;
-      threads = kPipeThreads;
-      int dev = 0;
-      if (cudaGetDevice(&dev) != cudaSuccess ||
-          cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
-        return false;
-      return cudaFuncSetAttribute(pipe, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)) ==
-             cudaSuccess;
-    }
     smem = rows_smem_for(s.grid_cols, s.coil_group, s.width, rows_threads_for(s.grid_cols));
     threads = rows_threads_for(s.grid_cols);
     const bool whole32 = s.coil_group == 32 && s.coil_parts == 1;
@@ -1617,12 +1441,7 @@ struct RowsLauncher {
   // One pass of nf frames of grid_rows rows and `groups` coil groups.
   void launch(const RowsArgs& r, int grid_rows, int groups, int nf, cudaStream_t stream) const {
     LaunchScope scope("k_rows", stream);
-    if (pipe != nullptr) {
-      const int units = grid_rows * groups * nf;
-      pipe<<<std::min(units, sms), threads, smem, stream>>>(r, units);
-    } else {
-      kernel<<<dim3(grid_rows, groups, nf), threads, smem, stream>>>(r);
-    }
+    kernel<<<dim3(grid_rows, groups, nf), threads, smem, stream>>>(r);
   }
 };
 
@@ -3090,7 +2909,7 @@ extern "C" ksj_gpu_status ksj_gpu_gridding_tune(const ksj_gpu_gridding_desc* des
     if (cg * 4 < desc->channels && cg < 8) continue;
     for (uint32_t cbm : {1u, 2u})
     for (uint32_t fpp : {0u, 12u, 48u})
-    for (uint32_t rb : {1u, 2u, 3u})
+    for (uint32_t rb : {1u, 2u})
     for (uint32_t parts : {1u, 2u}) {
       if (fpp >= desc->frames) continue;
       if (parts > 1 && cg < 16) continue;
