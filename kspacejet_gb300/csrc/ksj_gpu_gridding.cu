@@ -1147,6 +1147,7 @@ __global__ void __launch_bounds__(kThreads, kBlocks) k_rows(RowsArgs a) {
       const size_t sample_base = static_cast<size_t>(f) * a.sample_frame_stride + (coil_ok ? coil_global : 0);
       for (int base = 0; base < n; base += kBatch) {
         const int cnt = min(kBatch, n - base);
+        __syncwarp();  // the previous batch is read by every lane before it is replaced
         if (lane < cnt) {
           const float4* src = xent + static_cast<size_t>(base + lane) * kMV;
           float4* m = meta + lane * kMV;

@@ -281,6 +281,48 @@ def test_two_step_rows_byte_identical_across_row_kernels(native, cuda, orc, chan
             assert oracle.rel_l2(want[0][..., 0], ref) <= TOL_FP64
 
 
+@pytest.mark.parametrize("channels,grid,spokes", [(40, 128, 600), (32, 192, 160)])
+def test_long_lists_byte_identical(native, cuda, orc, channels, grid, spokes):
+    """Dense radial sampling: every spoke crosses the grid centre, so the
+    centre rows' lists hold hundreds to thousands of entries (far beyond one
+    32-entry staging batch).  Every row kernel (32-coil register path, smaller
+    coil groups, coil parts, one or two CTAs per SM, frame passes) sums each
+    cell in the same order and gives the same bytes; the result stays within
+    1e-5 of FP64."""
+    import ctypes
+
+    import torch
+    from kspacejet_gb300 import gpu
+
+    image = grid // 2
+    tr, ks = _kb_case(orc, image, grid, 4, channels=channels, spokes=spokes, seed=3)
+    # every spoke has a sample within one grid unit of the centre, so the
+    # centre row's list at the centre column holds at least one entry per spoke
+    u = np.hypot(tr[:, 0], tr[:, 1]) * grid / (2 * np.pi)
+    assert int((u < 1.0).sum()) >= spokes
+    frames = 2
+    k = torch.from_numpy(np.stack([ks, ks[:, ::-1].copy()])).to(cuda)
+    t = torch.from_numpy(np.stack([tr, tr[::-1].copy()])).to(cuda)
+    g = gpu.kb_gridding(image=image, grid=grid, channels=channels, samples=tr.shape[0], frames=frames, width=4,
+                        output=gpu.OUTPUT_COIL_LAST)
+    ws = g.new_workspace(cuda)
+    base = g.new_output(cuda)
+    g.run(k, t, base, ws)
+    assert g.flags(ws) == 0
+    want = base.cpu().numpy()
+    for cg, rb, fpp, parts in ((32, 1, 0, 1), (32, 2, 1, 1), (16, 2, 0, 1), (16, 1, 0, 2), (8, 2, 1, 2), (8, 1, 0, 1)):
+        tun = gpu.GriddingTuning(ctypes.sizeof(gpu.GriddingTuning), cg, 0, 0, fpp, rb, parts)
+        o = g.new_output(cuda)
+        o.real.fill_(float("nan"))
+        g.run(k, t, o, ws, tuning=tun)
+        assert g.flags(ws) == 0
+        assert o.cpu().numpy().tobytes() == want.tobytes(), (cg, rb, fpp, parts)
+    d64 = np.hypot(tr[:, 0].astype(np.float64), tr[:, 1].astype(np.float64))
+    for c in (0, channels - 1):
+        ref = orc.kb_gridding(grid, image, ks[c].astype(np.complex128), tr.astype(np.float64), d64, width=4)
+        assert oracle.rel_l2(want[0][..., c], ref) <= TOL_FP64
+
+
 def test_bf16_sample_storage_bound(native, cuda, orc):
     """BF16 sample storage, FP32 arithmetic: stated bound 1e-2 rel L2 against
     the FP32-storage result (bfloat16 keeps 8 mantissa bits: ~2e-3 per value)."""
