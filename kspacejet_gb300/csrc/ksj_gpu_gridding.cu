@@ -948,19 +948,36 @@ __device__ __forceinline__ void chunk_taps_wrapped(float2 (&r)[kChunk], int c0, 
   }
 }
 
-// One column chunk gridded by a whole 32-coil warp (lane = coil): the chunk's
-// cells stay in registers for the whole list, in the same per-cell order
-// (sample order, starting from zero) as the shared-memory form in k_rows, and
-// are stored once at its end (an empty list stores zeros).  kWrap admits
-// entries whose taps wrap around the grid inside the chunk.  `meta` is the
-// warp's staging buffer.
-template <int W, uint32_t kFormat, bool kWrap, int kAR = kAheadRegs>
-__device__ __forceinline__ void grid_chunk_regs(const RowsArgs& a, size_t sample_base, bool coil_ok, int lane,
-                                                float2* acc, int col_lo, const float4* xent, int n, float4* meta) {
+// Lists longer than kSegMin entries are gridded in segments (at most
+// kSegMax, all but the last of segment_length entries) that different warps
+// take at once, so that a row's long lists do not hold its CTA at the
+// barrier after the gridding while one warp works through each; a cell is then
+// the sum, in segment order, of its segments' partial sums, each partial sum
+// in sample order from zero.  Shorter lists are one segment: the cell is its
+// samples' sum in sample order.  Every row kernel uses the same segments.
+constexpr int kSegMin = 64;
+constexpr int kSegMax = 32;
+
+__host__ __device__ inline int list_segments(int n) {
+  return n <= kSegMin ? 1 : ((n + kSegMin - 1) / kSegMin < kSegMax ? (n + kSegMin - 1) / kSegMin : kSegMax);
+}
+static_assert(kSegMin * kSegMax <= (1 << 22), "segment counts are taken from lengths capped at 2^22");
+__host__ __device__ inline int segment_length(int n) {
+  const int sg = list_segments(n);
+  return (n + sg - 1) / sg;
+}
+
+// One column chunk's list entries (or one segment of them) gridded by a
+// warp, lane = coil: the chunk's 16 cells stay in registers, summed in entry
+// order from zero.  kWrap admits entries whose taps wrap around the grid
+// inside the chunk.  `meta` is the warp's staging buffer.
+template <int W, uint32_t kFormat, bool kWrap, int kAR>
+__device__ __forceinline__ void grid_entries_regs(float2 (&r)[kChunk], const RowsArgs& a, size_t sample_base,
+                                                  bool coil_ok, int lane, int col_lo, const float4* xent, int n,
+                                                  float4* meta) {
   constexpr int kMV = meta_vecs(W);
   constexpr int kBatch = meta_batch(W);
   const void* ks = a.samples_t;
-  float2 r[kChunk];
 #pragma unroll
   for (int t = 0; t < kChunk; ++t) r[t] = make_float2(0.0f, 0.0f);
   for (int base = 0; base < n; base += kBatch) {
@@ -1007,34 +1024,111 @@ __device__ __forceinline__ void grid_chunk_regs(const RowsArgs& a, size_t sample
       }
     }
   }
-  const int width = min(kChunk, a.grid_cols - col_lo);
-  float2* dst = acc + static_cast<size_t>(col_lo) * 32 + lane;
-#pragma unroll
-  for (int t = 0; t < kChunk; ++t)
-    if (t < width) dst[t * 32] = r[t];
 }
 
-// Gridding of one row by whole 32-coil warps: warps take the row's chunks
-// from the shared counter in the order task_chunk gives (longest list
-// first).  Every chunk is a task, so every cell of the row is stored.
+// The chunk's cells from registers into the accumulator (dst: the chunk's
+// first cell of this lane's coil, cells `stride` apart).  A one-segment list
+// (counter null) stores them.  For a segmented list each lane works on its
+// own coil's cells alone: segment 0 stores, segment seg > 0 waits until the
+// list's counter shows all 32 lanes of segments 0 .. seg-1 in, then adds its
+// partial sums; every lane then counts itself in.  Lanes wait on the counter
+// each for itself (no warp-wide sync), fenced on both sides.  The wait is
+// bounded: on a timeout the lane's partial sums are dropped, it still counts
+// itself in (the later segments do not wait out the limit as well) and
+// KSJ_GPU_FLAG_WAIT_TIMEOUT is raised.
+__device__ __forceinline__ void put_chunk(const float2 (&r)[kChunk], float2* dst, int stride, int width, bool live,
+                                          int seg, int* counter, uint32_t* flags) {
+  if (counter == nullptr) {
+    if (live) {
+#pragma unroll
+      for (int t = 0; t < kChunk; ++t)
+        if (t < width) dst[t * stride] = r[t];
+    }
+    return;
+  }
+  // segmented list: every lane of segments 0 .. seg-1 has counted itself in
+  bool ok = true;
+  if (seg > 0) {
+    uint32_t polls = 0;
+    while (*reinterpret_cast<volatile int*>(counter) < 32 * seg) {
+      if (++polls >= kWaitLimit) {
+        ok = false;
+        atomicOr(flags, KSJ_GPU_FLAG_WAIT_TIMEOUT);
+        break;
+      }
+      __nanosleep(32);
+    }
+    __threadfence_block();
+  }
+  if (live && ok) {
+#pragma unroll
+    for (int t = 0; t < kChunk; ++t) {
+      if (t < width) {
+        float2 v = r[t];
+        if (seg > 0) {
+          const float2 c = dst[t * stride];
+          v = make_float2(c.x + v.x, c.y + v.y);
+        }
+        dst[t * stride] = v;
+      }
+    }
+  }
+  __threadfence_block();
+  atomicAdd(counter, 1);
+}
+
+// The row's task table, built by warp 0: rank r is the r-th longest list
+// (chunk[r]), cut into list_segments(len) segments of segment_length(len)
+// entries; tasks base[r] .. base[r + 1] - 1 are its segments (times the coil
+// parts).
+struct RowTasks {
+  int* chunk;
+  int* base;      // nchunks + 1 entries
+  int* combined;  // per (chunk, part): lanes of finished segments
+  int* next;
+};
+
+// (rank, segment) of task q (parts folded out by the caller); a row without
+// segmented lists has task q = rank q.
+__device__ __forceinline__ void task_of(const RowTasks& t, int nchunks, int q, int lane, int* rank, int* seg) {
+  if (t.base[nchunks] == nchunks) {
+    *rank = q;
+    *seg = 0;
+    return;
+  }
+  const unsigned m = __ballot_sync(0xffffffffu, lane < nchunks && t.base[lane] <= q);
+  *rank = __popc(m) - 1;
+  *seg = q - t.base[*rank];
+}
+
+// Gridding of one row by whole 32-coil warps (lane = coil): warps take the
+// row's tasks (list segments, longest lists first) from the shared counter.
+// Every chunk is at least one task, so every cell of the row is stored.
 template <int W, uint32_t kFormat, bool kWrap, int kAR>
 __device__ __forceinline__ void rows_grid_regs(const RowsArgs& a, int f, int cgi, int lane, float2* acc,
-                                               const uint32_t* offs, const int* task_chunk, int* task_next,
-                                               float4* meta) {
+                                               const uint32_t* offs, const RowTasks& tasks, float4* meta) {
   constexpr int kMV = meta_vecs(W);
   const int coil_global = cgi * 32 + lane;
   const bool coil_ok = coil_global < a.channels;
   const size_t sample_base = static_cast<size_t>(f) * a.sample_frame_stride + (coil_ok ? coil_global : 0);
+  const int ntasks = tasks.base[a.nchunks];
   for (;;) {
-    int task = 0;
-    if (lane == 0) task = atomicAdd(task_next, 1);
-    task = __shfl_sync(0xffffffffu, task, 0);
-    if (task >= a.nchunks) break;
-    const int chunk = task_chunk[task];
+    int q = 0;
+    if (lane == 0) q = atomicAdd(tasks.next, 1);
+    q = __shfl_sync(0xffffffffu, q, 0);
+    if (q >= ntasks) break;
+    int rank, seg;
+    task_of(tasks, a.nchunks, q, lane, &rank, &seg);
+    const int chunk = tasks.chunk[rank];
     const uint32_t begin = offs[chunk];
     const int n = static_cast<int>(offs[chunk + 1] - begin);
-    const float4* xent = a.expanded + (static_cast<size_t>(f) * a.entries_per_frame + begin) * kMV;
-    grid_chunk_regs<W, kFormat, kWrap, kAR>(a, sample_base, coil_ok, lane, acc, chunk * kChunk, xent, n, meta);
+    const int sl = segment_length(n);
+    const int e0 = seg * sl, e1 = min(n, e0 + sl);
+    const float4* xent = a.expanded + (static_cast<size_t>(f) * a.entries_per_frame + begin + e0) * kMV;
+    float2 r[kChunk];
+    grid_entries_regs<W, kFormat, kWrap, kAR>(r, a, sample_base, coil_ok, lane, chunk * kChunk, xent, e1 - e0, meta);
+    put_chunk(r, acc + static_cast<size_t>(chunk * kChunk) * 32 + lane, 32, min(kChunk, a.grid_cols - chunk * kChunk),
+              true, seg, list_segments(n) > 1 ? tasks.combined + chunk : nullptr, a.flags);
   }
 }
 
@@ -1068,8 +1162,11 @@ __global__ void __launch_bounds__(kThreads, kBlocks) k_rows(RowsArgs a) {
   const uint32_t* off = a.offsets + static_cast<size_t>(f) * (a.lists_per_frame + 1) + row * a.nchunks;
   for (int i = tid; i <= a.nchunks; i += nthreads) offs[i] = __ldg(off + i);
   // task order: the row's lists longest first (a bitonic sort across warp 0,
-  // one key per lane: length << 8 | chunk), taken from a shared counter
+  // one key per lane: length << 8 | chunk), each cut into its segments, taken
+  // from a shared counter
   __shared__ int task_chunk[kMaxGrid / kChunk];
+  __shared__ int task_base[kMaxGrid / kChunk + 1];
+  __shared__ int task_combined[2 * (kMaxGrid / kChunk)];
   __shared__ int task_next;
   if (warp == 0) {
     int key = -1;
@@ -1087,9 +1184,26 @@ __global__ void __launch_bounds__(kThreads, kBlocks) k_rows(RowsArgs a) {
         key = (lower == desc) ? max(key, other) : min(key, other);
       }
     }
-    if (lane < a.nchunks) task_chunk[lane] = key & 255;
+    // segments per rank and their exclusive prefix (from the key's length,
+    // capped at 2^22 entries: the same count, since kSegMin * kSegMax entries
+    // already take the most segments)
+    const int len = lane < a.nchunks ? (key >> 8) : 0;
+    const int nseg = lane < a.nchunks ? list_segments(len) : 0;
+    int incl = nseg;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const int v = __shfl_up_sync(0xffffffffu, incl, d);
+      if (lane >= d) incl += v;
+    }
+    if (lane < a.nchunks) {
+      task_chunk[lane] = key & 255;
+      task_base[lane] = incl - nseg;
+    }
+    if (lane == a.nchunks - 1) task_base[a.nchunks] = incl;
     if (lane == 0) task_next = 0;
   }
+  for (int i = tid; i < 2 * (kMaxGrid / kChunk); i += nthreads) task_combined[i] = 0;
+  const RowTasks tasks{task_chunk, task_base, task_combined, &task_next};
   // (the 32-coil path stores every cell of the row from registers)
   if (kCG != 32)
     for (int i = tid; i < a.grid_cols * cg; i += nthreads) acc[i] = make_float2(0.0f, 0.0f);
@@ -1101,9 +1215,9 @@ __global__ void __launch_bounds__(kThreads, kBlocks) k_rows(RowsArgs a) {
     // taps wrap around the grid inside one chunk only on grids narrower than
     // kChunk + W - 1 columns; the loop for those keeps a per-tap form
     if (a.grid_cols < kChunk + W - 1)
-      rows_grid_regs<W, kFormat, true, kAR>(a, f, cgi, lane, acc, offs, task_chunk, &task_next, meta);
+      rows_grid_regs<W, kFormat, true, kAR>(a, f, cgi, lane, acc, offs, tasks, meta);
     else
-      rows_grid_regs<W, kFormat, false, kAR>(a, f, cgi, lane, acc, offs, task_chunk, &task_next, meta);
+      rows_grid_regs<W, kFormat, false, kAR>(a, f, cgi, lane, acc, offs, tasks, meta);
   } else {
   // ---- gridding.  A task is (column chunk, coil part): the chunk's sorted
   // list applied to a subset of the coil group.  Cells of different coils are
@@ -1114,9 +1228,12 @@ __global__ void __launch_bounds__(kThreads, kBlocks) k_rows(RowsArgs a) {
   // (vector loads), folds the row weight into the W column weights and stages
   // them in the warp's shared batch; then the warp walks the batch in order
   // with the coil loads of the next kAhead samples always in flight.
+  // A list longer than kSegMin entries is gridded in segments like the
+  // 32-coil path's (lane = coil of the part, cells in registers, segments
+  // combined in order), so that every coil grouping gives the same cells.
   const int parts = kCG ? 1 : a.coil_parts;
   const int cpart = cg / parts;
-  const int ntasks = a.nchunks * parts;
+  const int ntasks = tasks.base[a.nchunks] * parts;
   {
     // lanes: coil = lane % cpp, tap group = lane / cpp
     int cpp = 1;
@@ -1133,13 +1250,30 @@ __global__ void __launch_bounds__(kThreads, kBlocks) k_rows(RowsArgs a) {
       if (lane == 0) task = atomicAdd(&task_next, 1);
       task = __shfl_sync(0xffffffffu, task, 0);
       if (task >= ntasks) break;
-      const int rank = task / parts;
+      const int q = task / parts;
+      const int part = task - q * parts;
+      int rank, seg;
+      task_of(tasks, a.nchunks, q, lane, &rank, &seg);
       const int chunk = task_chunk[rank];
-      const int part = task - rank * parts;
       const uint32_t begin = offs[chunk];
       const int n = static_cast<int>(offs[chunk + 1] - begin);
       const float4* xent = a.expanded + (static_cast<size_t>(f) * a.entries_per_frame + begin) * kMV;
       const int col_lo = chunk * kChunk;
+      if (list_segments(n) > 1) {
+        const int sl = segment_length(n);
+        const int e0 = seg * sl, e1 = min(n, e0 + sl);
+        const bool lane_coil = lane < cpart;
+        const int rc = part * cpart + (lane_coil ? lane : 0);
+        const int rg = cgi * cg + rc;
+        const bool rok = lane_coil && rg < a.channels;
+        const size_t rbase = static_cast<size_t>(f) * a.sample_frame_stride + (rok ? rg : 0);
+        float2 r[kChunk];
+        grid_entries_regs<W, kFormat, true, kAheadRegs>(r, a, rbase, rok, lane, col_lo,
+                                                        xent + static_cast<size_t>(e0) * kMV, e1 - e0, meta);
+        put_chunk(r, acc + addr(rc, col_lo), cg, min(kChunk, a.grid_cols - col_lo), lane_coil, seg,
+                  tasks.combined + part * a.nchunks + chunk, a.flags);
+        continue;
+      }
       const int col_hi = min(col_lo + kChunk, a.grid_cols);
       const int my_coil = part * cpart + lane % cpp;  // coil index within the group
       const int coil_global = cgi * cg + my_coil;
