@@ -63,7 +63,7 @@ typedef int32_t ksj_gpu_status;
 #define KSJ_GPU_FLAG_NONFINITE_SAMPLE (1u << 0)
 #define KSJ_GPU_FLAG_BAD_TRAJECTORY (1u << 1)   /* non-finite, or outside [-pi, pi] where required */
 #define KSJ_GPU_FLAG_BAD_DCF (1u << 2)          /* non-finite or negative external weight */
-#define KSJ_GPU_FLAG_WAIT_TIMEOUT (1u << 3)     /* a bounded device wait on a tile copy gave up; output invalid */
+#define KSJ_GPU_FLAG_WAIT_TIMEOUT (1u << 3)     /* a bounded device wait (a tile copy, a long list's segment order) gave up; output invalid */
 
 /* ------------------------------------------------------------- gridding */
 

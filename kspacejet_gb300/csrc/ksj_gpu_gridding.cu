@@ -2524,21 +2524,12 @@ __global__ void __launch_bounds__(256) k_pm_prepare3(const float* traj, PmRecord
   w[idx] = ok ? 1.0 : 0.0;
 }
 
-// One half-warp per (plane, row, chunk) list; lane l % 16 is a column.
+// Cell (plane, row, col)'s sum over list entries [e0, e1), in entry order
+// from `acc`.
 template <int W>
-__global__ void __launch_bounds__(256) k_pm_grid3(const uint32_t* offsets, const uint32_t* entries,
-                                                  const PmRecord3<W>* pm, const double* w, double* grid, int g,
-                                                  int nchunks, int lists_per_plane) {
-  const size_t hw = (static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 4;
-  const int sub = threadIdx.x & 15;
-  if (hw >= static_cast<size_t>(g) * lists_per_plane) return;
-  const int plane = static_cast<int>(hw / lists_per_plane);
-  const int l = static_cast<int>(hw - static_cast<size_t>(plane) * lists_per_plane);
-  const int row = l / nchunks;
-  const int col = (l - row * nchunks) * kChunk + sub;
-  const uint32_t* off = offsets + static_cast<size_t>(plane) * (lists_per_plane + 1);
-  double acc = 0.0;
-  for (uint32_t e = off[l]; e < off[l + 1]; ++e) {
+__device__ __forceinline__ double pm_cell3(const uint32_t* entries, uint32_t e0, uint32_t e1, const PmRecord3<W>* pm,
+                                           const double* w, int plane, int row, int col, int g, double acc) {
+  for (uint32_t e = e0; e < e1; ++e) {
     const uint32_t sidx = __ldg(entries + e);
     const PmRecord3<W>& r = pm[sidx];
     int dz = plane - r.z0;
@@ -2549,7 +2540,67 @@ __global__ void __launch_bounds__(256) k_pm_grid3(const uint32_t* offsets, const
     if (dc < 0) dc += g;
     if (dz < W && dr < W && dc < W) acc += w[sidx] * ((r.wz[dz] * r.wr[dr]) * r.wc[dc]);
   }
+  return acc;
+}
+
+// One half-warp per (plane, row, chunk) list; lane l % 16 is a column.
+// Lists longer than `capacity` entries (queued by the list sort) are left to
+// k_pm_long3.
+template <int W>
+__global__ void __launch_bounds__(256) k_pm_grid3(const uint32_t* offsets, const uint32_t* entries,
+                                                  const PmRecord3<W>* pm, const double* w, double* grid, int g,
+                                                  int nchunks, int lists_per_plane, int capacity) {
+  const size_t hw = (static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 4;
+  const int sub = threadIdx.x & 15;
+  if (hw >= static_cast<size_t>(g) * lists_per_plane) return;
+  const int plane = static_cast<int>(hw / lists_per_plane);
+  const int l = static_cast<int>(hw - static_cast<size_t>(plane) * lists_per_plane);
+  const int row = l / nchunks;
+  const int col = (l - row * nchunks) * kChunk + sub;
+  const uint32_t* off = offsets + static_cast<size_t>(plane) * (lists_per_plane + 1);
+  const uint32_t begin = off[l], end = off[l + 1];
+  if (static_cast<int>(end - begin) > capacity) return;
+  const double acc = pm_cell3<W>(entries, begin, end, pm, w, plane, row, col, g, 0.0);
   if (col < g) grid[(static_cast<size_t>(plane) * g + row) * g + col] = acc;
+}
+
+// The queued long lists (count at long_lists[0], global list ids after it),
+// one block per list at a time: half-warp h sums the h-th of kPmLongSegs
+// consecutive segments of the list for its 16 columns (in entry order from
+// zero), then the block's first 16 threads add the segments' partial sums in
+// segment order.  The kooshball centre's lists hold up to ~10^5 entries, which
+// one half-warp walks one dependent record load at a time.
+constexpr int kPmLongThreads = 512;
+constexpr int kPmLongSegs = kPmLongThreads / 16;
+
+template <int W>
+__global__ void __launch_bounds__(kPmLongThreads) k_pm_long3(const uint32_t* long_lists, const uint32_t* offsets,
+                                                             const uint32_t* entries, const PmRecord3<W>* pm,
+                                                             const double* w, double* grid, int g, int nchunks,
+                                                             int lists_per_plane) {
+  __shared__ double part[kPmLongSegs][16];
+  const uint32_t queued = long_lists[0];
+  const int h = threadIdx.x >> 4, sub = threadIdx.x & 15;
+  for (uint32_t q = blockIdx.x; q < queued; q += gridDim.x) {
+    const uint32_t gl = long_lists[1 + q];
+    const int plane = static_cast<int>(gl / static_cast<uint32_t>(lists_per_plane));
+    const int l = static_cast<int>(gl - static_cast<uint32_t>(plane) * lists_per_plane);
+    const int row = l / nchunks;
+    const int col = (l - row * nchunks) * kChunk + sub;
+    const uint32_t* off = offsets + static_cast<size_t>(plane) * (lists_per_plane + 1);
+    const uint32_t begin = off[l], n = off[l + 1] - begin;
+    const uint32_t seg = (n + kPmLongSegs - 1) / kPmLongSegs;
+    const uint32_t e0 = begin + min(n, static_cast<uint32_t>(h) * seg);
+    const uint32_t e1 = begin + min(n, static_cast<uint32_t>(h + 1) * seg);
+    part[h][sub] = pm_cell3<W>(entries, e0, e1, pm, w, plane, row, col, g, 0.0);
+    __syncthreads();
+    if (threadIdx.x < 16) {
+      double acc = part[0][sub];
+      for (int k = 1; k < kPmLongSegs; ++k) acc += part[k][sub];
+      if (col < g) grid[(static_cast<size_t>(plane) * g + row) * g + col] = acc;
+    }
+    __syncthreads();
+  }
 }
 
 template <int W>
@@ -2632,12 +2683,20 @@ ksj_gpu_status launch_pipe_menon3(const Shape& s, const PmLayout3& l, uint32_t i
                                                                  1.0 / std::cyl_bessel_i(0.0, static_cast<double>(s.beta)));
   }
   const size_t half_warps = static_cast<size_t>(g) * s.lists_per_frame;
+  // at most this many lists exceed the capacity
+  const size_t long_blocks = std::max<size_t>(1, l.entries_total / (static_cast<size_t>(s.list_capacity) + 1));
   for (uint32_t it = 0; it < iterations; ++it) {
     {
       LaunchScope scope("k_pm_grid3", stream);
       k_pm_grid3<W><<<static_cast<unsigned>((half_warps * 16 + 255) / 256), 256, 0, stream>>>(
           reinterpret_cast<const uint32_t*>(ws + l.offsets), reinterpret_cast<const uint32_t*>(ws + l.entries), pm, w,
-          grid, g, s.nchunks, s.lists_per_frame);
+          grid, g, s.nchunks, s.lists_per_frame, s.list_capacity);
+    }
+    {
+      LaunchScope scope("k_pm_long3", stream);
+      k_pm_long3<W><<<static_cast<unsigned>(std::min<size_t>(long_blocks, 1216)), kPmLongThreads, 0, stream>>>(
+          reinterpret_cast<const uint32_t*>(ws + l.long_lists), reinterpret_cast<const uint32_t*>(ws + l.offsets),
+          reinterpret_cast<const uint32_t*>(ws + l.entries), pm, w, grid, g, s.nchunks, s.lists_per_frame);
     }
     LaunchScope scope("k_pm_update3", stream);
     k_pm_update3<W><<<(s.samples + 255) / 256, 256, 0, stream>>>(pm, grid, w, it + 1 == iterations ? d_dcf : nullptr,

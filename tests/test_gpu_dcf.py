@@ -1,7 +1,8 @@
 """Pipe-Menon density weights (ksj_gpu_pipe_menon_dcf) against the FP64
 oracle restatement of the same grid-based iteration.  Both run in double
-precision with the same tap sets and per-cell summation order; they differ
-only in the Bessel I0 evaluation and in fused multiply-adds (~1e-15); the
+precision with the same tap sets and per-cell summation order (except the
+3-D lists above 512 entries, summed in segments); they differ only in the
+Bessel I0 evaluation, fused multiply-adds and those segment sums (~1e-15); the
 output is float32, so the bound is 1e-7 relative L2 (float32 rounding of the
 weights alone is ~3e-8)."""
 import numpy as np
@@ -55,15 +56,37 @@ def test_pipe_menon_is_deterministic_and_converges(native, cuda, orc):
     assert late < early
 
 
+def _lists3_over(tr, g, width, capacity=512):
+    """(longest, count over `capacity`) of the 3-D (plane, row, 16-column
+    chunk) lists: a sample is in every list its width^3 taps touch."""
+    u = tr.astype(np.float64) * g / (2 * np.pi)
+    t0 = np.floor(u).astype(np.int64) - width // 2 + 1
+    chunks = np.stack([((t0[:, 2] + c) % g) // 16 for c in range(width)], 1)
+    keys = []
+    for a in range(width):
+        for b in range(width):
+            zr = ((t0[:, 0] + a) % g) * g + (t0[:, 1] + b) % g
+            for c in range(width):
+                first = np.all(chunks[:, :c] != chunks[:, c:c + 1], axis=1)
+                keys.append((zr * 64 + chunks[:, c])[first])
+    _, cnt = np.unique(np.concatenate(keys), return_counts=True)
+    return int(cnt.max()), int((cnt > capacity).sum())
+
+
 @pytest.mark.parametrize("n,g,width", [(16, 24, 4), (16, 32, 6)])
 def test_pipe_menon3_matches_fp64_oracle(native, cuda, orc, n, g, width):
     """3-D Pipe-Menon (the kooshball configuration's density weights) against
     the double-precision restatement, 10 iterations.  The oracle gets the
-    float32 kernel shape the GPU path uses."""
+    float32 kernel shape the GPU path uses.  The centre's lists exceed the
+    512-entry sort capacity, so their cells come from the long-list kernel
+    (32 segments added in segment order; the oracle sums in sample order, a
+    difference of ~1e-16)."""
     import torch
     from kspacejet_gb300 import gpu, synth
 
     tr = synth.kooshball(g, 300)
+    longest, over = _lists3_over(tr, g, width)
+    assert longest > 1024 and over > 10
     got = gpu.pipe_menon_dcf3(torch.from_numpy(tr).to(cuda), n, g, width=width).cpu().numpy()
     beta = float(np.float32(orc.kb_beta(width, g / n)))
     want = orc.pipe_menon_dcf3(tr, g, width, beta=beta)
