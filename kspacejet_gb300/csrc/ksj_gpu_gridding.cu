@@ -770,6 +770,72 @@ __device__ __forceinline__ void block_sort(uint32_t* buf, int n) {
   }
 }
 
+// Stages (k, j) for j = j0, j0 / 2, ..., 1 of that network on the chunk of
+// list elements [base, base + kLongSortSmem) held in buf (elements at or
+// beyond n are absent).  Every pair of these stages lies inside the chunk:
+// j < kLongSortSmem, and the mirrored partner of stage j = k / 2 only when
+// k <= kLongSortSmem.
+__device__ __forceinline__ void chunk_stages(uint32_t* buf, int base, int n, int k, int j0) {
+  for (int j = j0; j > 0; j >>= 1) {
+    for (int t = threadIdx.x; t < kLongSortSmem && base + t < n; t += blockDim.x) {
+      const int i = base + t;
+      const int partner = (j == (k >> 1)) ? (i ^ (k - 1)) : (i ^ j);
+      if (partner > i && partner < n) {
+        const uint32_t x = buf[t], y = buf[partner - base];
+        if (x > y) {
+          buf[t] = y;
+          buf[partner - base] = x;
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// The network of block_sort on a list longer than the shared buffer, in
+// place in global memory, with every stage whose pairs lie inside one
+// kLongSortSmem-entry chunk run on that chunk in shared memory: first each
+// chunk sorted whole (k up to the chunk size), then per larger k the stages
+// with j >= the chunk size over global memory and the rest chunk by chunk.
+// Same comparisons in the same stage order as block_sort: the same result.
+__device__ __forceinline__ void chunk_load(uint32_t* buf, const uint32_t* ent, int base, int n) {
+  for (int t = threadIdx.x; t < kLongSortSmem && base + t < n; t += blockDim.x) buf[t] = ent[base + t];
+  __syncthreads();
+}
+__device__ __forceinline__ void chunk_store(const uint32_t* buf, uint32_t* ent, int base, int n) {
+  for (int t = threadIdx.x; t < kLongSortSmem && base + t < n; t += blockDim.x) ent[base + t] = buf[t];
+  __syncthreads();
+}
+__device__ __forceinline__ void block_sort_chunked(uint32_t* ent, int n, uint32_t* buf) {
+  int p = 1;
+  while (p < n) p <<= 1;
+  for (int base = 0; base < n; base += kLongSortSmem) {
+    chunk_load(buf, ent, base, n);
+    for (int k = 2; k <= kLongSortSmem; k <<= 1) chunk_stages(buf, base, n, k, k >> 1);
+    chunk_store(buf, ent, base, n);
+  }
+  for (int k = 2 * kLongSortSmem; k <= p; k <<= 1) {
+    for (int j = k >> 1; j >= kLongSortSmem; j >>= 1) {
+      for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const int partner = (j == (k >> 1)) ? (i ^ (k - 1)) : (i ^ j);
+        if (partner > i && partner < n) {
+          const uint32_t x = ent[i], y = ent[partner];
+          if (x > y) {
+            ent[i] = y;
+            ent[partner] = x;
+          }
+        }
+      }
+      __syncthreads();
+    }
+    for (int base = 0; base < n; base += kLongSortSmem) {
+      chunk_load(buf, ent, base, n);
+      chunk_stages(buf, base, n, k, kLongSortSmem >> 1);
+      chunk_store(buf, ent, base, n);
+    }
+  }
+}
+
 template <int W>
 __device__ __forceinline__ void sort_long_list(const SortArgs& a, size_t gl, uint32_t* long_buf) {
   const int f = static_cast<int>(gl / a.lists_per_frame);
@@ -787,16 +853,17 @@ __device__ __forceinline__ void sort_long_list(const SortArgs& a, size_t gl, uin
       for (int i = threadIdx.x; i < n; i += blockDim.x) ent[i] = long_buf[i];
     sorted = long_buf;
   } else {
-    block_sort(ent, n);
+    block_sort_chunked(ent, n, long_buf);
   }
   __syncthreads();
   if (a.expanded != nullptr) expand_list<W>(a, f, l, begin, n, sorted, threadIdx.x, blockDim.x);
 }
 
 // Blocks take the queued long lists in turn: sort (in shared memory up to
-// kLongSortSmem entries, else in place) and expand.
+// kLongSortSmem entries, else in place with chunk-local stages in shared
+// memory) and expand.
 template <int W>
-__global__ void __launch_bounds__(kLongSortThreads) k_sort_long(SortArgs a) {
+__global__ void __launch_bounds__(kLongSortThreads, 1) k_sort_long(SortArgs a) {
   extern __shared__ uint32_t long_buf[];
   const uint32_t queued = *a.long_count;
   for (uint32_t q = blockIdx.x; q < queued; q += gridDim.x) {

@@ -121,6 +121,30 @@ def test_binning_permutation_is_bit_exact(native, cuda, kb, grid, width):
     np.testing.assert_array_equal(smp, ref_smp)
 
 
+def test_binning_of_lists_beyond_the_shared_sort_buffer(native, cuda):
+    """12 000 spokes through one 64-cell grid: the centre lists hold up to ~9e4
+    entries, beyond the long-list sort's 16 K-entry shared buffer, so they are
+    sorted in global memory with chunk-local stages in shared memory (several
+    merge levels above the chunk size).  The lists match the restatement
+    exactly: every entry present, in increasing sample order."""
+    import torch
+    from kspacejet_gb300 import gpu, synth
+
+    tr = synth.golden_angle_radial(64, 12000)[None]
+    g = gpu.kb_gridding(image=32, grid=64, channels=1, samples=tr.shape[1], width=4)
+    k = torch.from_numpy(synth.random_kspace(1, tr.shape[1], 5)).to(cuda)[None].contiguous()
+    ws = g.new_workspace(cuda)
+    g.run(k, torch.from_numpy(tr).to(cuda), g.new_output(cuda), ws)
+    torch.cuda.synchronize()
+    assert g.flags(ws) == 0
+    cw, off, smp = g.binning(ws)
+    ref_off, ref_smp = binning(tr, 64, 64, 4, True, chunk=cw)
+    lengths = np.diff(ref_off)
+    assert lengths.max() > 65536 and (lengths > 16384).sum() > 10
+    np.testing.assert_array_equal(off, ref_off)
+    np.testing.assert_array_equal(smp, ref_smp)
+
+
 def test_device_checks_flag_bad_inputs(native, cuda):
     import torch
     from kspacejet_gb300 import gpu, synth
