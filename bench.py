@@ -196,6 +196,18 @@ def dist_setup(n_gpus: int):
     return None, 0, 1, 0
 
 
+def max_over_ranks(dist, *values: float) -> tuple[float, ...]:
+    """The per-rank timings reduced to their maximum over all ranks (the
+    slowest replica sets the whole job's time); unchanged on one process."""
+    if dist is None:
+        return tuple(float(v) for v in values)
+    import torch
+
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return tuple(float(v) for v in t.tolist())
+
+
 def read_traffic() -> float | None:
     """dram__bytes_read.sum + dram__bytes_write.sum per launch of the dominant
     kernel from the committed ncu summary (profiles/)."""
@@ -372,10 +384,7 @@ def run_ours(args) -> dict | None:
     if not np.isfinite(oh.numpy()).all():
         raise RuntimeError("non-finite reconstruction")
 
-    if dist is not None:
-        tt = torch.tensor([ms, e2e_ms], dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms, e2e_ms = float(tt[0]), float(tt[1])
+    ms, e2e_ms = max_over_ranks(dist, ms, e2e_ms)
     if rank != 0:
         return None
 
