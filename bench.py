@@ -184,6 +184,134 @@ def cpu_reference_rate(traj: np.ndarray, ksp: np.ndarray, budget_s: float = 2.5,
                       f"direct-DFT fallback for a non-power-of-two axis), {cores} threads, {el:.2f} s wall"}
 
 
+def cpu_kb_rate(traj: np.ndarray, ksp: np.ndarray, budget_s: float = 3.0, width: int = WIDTH):
+    """Gridded samples/s of the same Kaiser-Bessel reconstruction as a
+    single-precision CPU program (the oracle's restatement with an FFT: float
+    gridding, mixed-radix FFT of the grid rows and of the kept columns, crop,
+    deapodisation), one (frame, coil) image per task on all host cores.  The
+    reference has no Kaiser-Bessel path, so this is a restatement, not the
+    reference."""
+    import oracle
+
+    impl = oracle.Oracle()
+    cores = os.cpu_count() or 1
+    rng = np.random.default_rng(1)
+    pairs = [(int(f), int(c)) for f, c in zip(rng.integers(0, FRAMES, 4096), rng.integers(0, COILS, 4096))]
+    dcfs = {}
+
+    def task(fc):
+        f, c = fc
+        d = dcfs.get(f)
+        if d is None:
+            d = np.hypot(traj[f, :, 0], traj[f, :, 1]).astype(np.float32)
+            dcfs[f] = d
+        impl.kb_gridding_f32(GRID, IMAGE, ksp[f, c], traj[f], d, width=width)
+        return traj.shape[1]
+
+    done = samples = 0
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=cores) as pool:
+        while True:
+            batch = pairs[done:done + cores]
+            samples += sum(pool.map(task, batch))
+            done += len(batch)
+            el = time.perf_counter() - t0
+            if el >= budget_s or done >= len(pairs):
+                break
+    el = time.perf_counter() - t0
+    return {"value": samples / el, "unit": METRIC, "cores": cores, "kind": "port",
+            "sample": f"restatement, not reference (the reference has no Kaiser-Bessel path): {done} (frame, coil) "
+                      f"images of the workload ({traj.shape[1]} samples each), KB W={width} gridding on the "
+                      f"{GRID}^2 grid, FFT of every grid row and of the {IMAGE} kept columns, crop and "
+                      f"deapodisation in float32, {cores} threads, {el:.2f} s wall"}
+
+
+def accuracy_check(rss: np.ndarray, traj: np.ndarray, ksp: np.ndarray, frames, width: int = WIDTH,
+                   pixels: int = 256) -> dict:
+    """Relative L2 error of RSS images the timed call wrote, against (a) the
+    RSS of the FP64 restatement of the same Kaiser-Bessel algorithm over every
+    coil and (b) the RSS of the exact FP64 direct NUDFT of the DCF-weighted
+    samples at `pixels` seeded pixels.  Outside every timed region."""
+    import oracle
+
+    orc = oracle.Oracle()
+    cores = os.cpu_count() or 1
+    rng = np.random.default_rng(17)
+    flat = rng.choice(IMAGE * IMAGE, size=pixels, replace=False)
+    pix = np.stack([flat // IMAGE, flat % IMAGE], axis=-1)
+    o = (IMAGE - 1) / 2.0
+    worst_same = worst_exact = 0.0
+    with ThreadPoolExecutor(max_workers=cores) as pool:
+        for f in frames:
+            t64 = traj[f].astype(np.float64)
+            d64 = np.hypot(t64[:, 0], t64[:, 1])
+            coils = list(pool.map(lambda c: orc.kb_gridding(GRID, IMAGE, ksp[f, c].astype(np.complex128), t64, d64,
+                                                            width=width), range(ksp.shape[1])))
+            ref = np.sqrt(sum(np.abs(x) ** 2 for x in coils))
+            exact = list(pool.map(lambda c: orc.direct_adjoint_at(pix, ksp[f, c].astype(np.complex128) * d64, t64, o, o),
+                                  range(ksp.shape[1])))
+            ref_exact = np.sqrt(sum(np.abs(x) ** 2 for x in exact))
+            worst_same = max(worst_same, oracle.rel_l2(rss[f], ref))
+            worst_exact = max(worst_exact, oracle.rel_l2(rss[f][pix[:, 0], pix[:, 1]], ref_exact))
+    return {"rel_l2_vs_fp64_same_algorithm": worst_same, "rel_l2_vs_exact_nudft": worst_exact,
+            "frames_checked": [int(f) for f in frames], "coils": int(ksp.shape[1]), "output": "rss",
+            "exact_nudft_pixels": pixels, "kernel_width": width,
+            "note": "max over the checked frames; FP64 Kaiser-Bessel restatement over all pixels, exact FP64 "
+                    "direct NUDFT of the DCF-weighted samples at seeded pixels"}
+
+
+def dropin_leg(steps: int, warmup: int) -> dict:
+    """The drop-in operator itself: radial_gridding_reconstruct (linear
+    gridding, sigma 1, ramp DCF) at the reference envelope's anchor shape
+    (256^2 image, 65 536 samples, 8 coils) fired through the GPU plug-in with
+    host buffers (every firing copies in, computes and copies out), next to the
+    reference's CPU path on the same shape over all host cores."""
+    import oracle
+    import kspacejet_gb300
+    from kspacejet_gb300 import host as H, synth
+
+    n, c = 256, 8
+    tr = synth.golden_angle_radial(512, 128)  # 65 536 samples, |k| <= pi
+    m = tr.shape[0]
+    ks = synth.multicoil_kspace(tr, n, c, seed=5)
+    mod = H.ProviderModule(kspacejet_gb300.NONCARTESIAN_PLUGIN)
+    try:
+        kin, tin = H.aligned_copy(ks), H.aligned_copy(tr.ravel())
+        out = H.aligned((n * n * c,), np.complex64)
+        with mod.instance("radial_gridding_reconstruct", H.radial_config(c, n, n, m)) as inst:
+            def fire():
+                r = inst.fire([(kin, H.TYPE_KSPACE, 0), (tin, H.TYPE_TRAJECTORY, 1)], out, H.TYPE_COIL_IMAGE,
+                              scratch_bytes=H.radial_scratch_bytes(n, n, m))
+                if r.status != 0:
+                    raise RuntimeError(f"plug-in firing failed: {r.status} {r.error}")
+            for _ in range(max(warmup, 3)):
+                fire()
+            t0 = time.perf_counter()
+            for _ in range(steps):
+                fire()
+            gpu_s = (time.perf_counter() - t0) / steps
+    finally:
+        mod.close()
+    try:
+        impl, kind = oracle.Reference(), "reference"
+    except FileNotFoundError:
+        impl, kind = oracle.Oracle(), "port"
+    cores = os.cpu_count() or 1
+    dcf = impl.ramp_dcf(tr)
+    reps = max(1, cores // c)
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=cores) as pool:
+        list(pool.map(lambda i: impl.linear_gridding(n, n, ks[i % c], tr, dcf), range(reps * c)))
+    cpu_s = (time.perf_counter() - t0) / reps
+    return {"operator": "radial_gridding_reconstruct", "shape": {"image": n, "samples": m, "channels": c},
+            "path": "GPU plug-in fired through the C-ABI firing host, pageable host payloads, copies inside",
+            "gpu_ms_per_firing": gpu_s * 1e3, "gpu_samples_per_s": c * m / gpu_s,
+            "cpu_ms_per_frame": cpu_s * 1e3, "cpu_samples_per_s": c * m / cpu_s,
+            "cpu": {"kind": kind, "cores": cores, "what": "ramp DCF + radial_linear_gridding2_adjoint per coil, "
+                                                           "one coil per thread"},
+            "speedup": cpu_s / gpu_s, "timing": "host wall clock per firing (the firing is synchronous)"}
+
+
 # ------------------------------------------------------------ GPU arm
 
 def dist_setup(n_gpus: int):
@@ -234,6 +362,39 @@ def kernel_bytes(g, entries: int) -> dict:
     }
 
 
+def width6_leg(g4_tuning_note: str, k, t, traj_h, ksp_h, dev, steps: int, warmup: int) -> dict:
+    """The same workload with Kaiser-Bessel width 6: the form whose
+    approximation error against the exact NUDFT is below 1e-5 (width 4 is
+    ~4e-4).  Device-resident inputs, tuned, CUDA events; accuracy of its
+    output on one frame."""
+    import torch
+    from kspacejet_gb300 import gpu
+
+    g = gpu.kb_gridding(image=IMAGE, grid=GRID, channels=COILS, samples=traj_h.shape[1], frames=FRAMES, width=6,
+                        output=gpu.OUTPUT_RSS)
+    out = g.new_output(dev)
+    ws = g.new_workspace(dev)
+    tuning = g.tune(k, t, out, ws)
+    for _ in range(warmup):
+        g.run(k, t, out, ws, tuning=tuning)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        g.run(k, t, out, ws, tuning=tuning)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    acc = accuracy_check(out.cpu().numpy(), traj_h, ksp_h, frames=(FRAMES // 3,), width=6)
+    del ws
+    return {"kernel_width": 6, "ms_per_step": ms, "value": FRAMES * COILS * traj_h.shape[1] / (ms / 1e3),
+            "unit": "samples/s", "accuracy": acc,
+            "tuning": {"coil_group": tuning.coil_group, "column_block": tuning.column_block,
+                       "frames_per_pass": tuning.frames_per_pass or FRAMES,
+                       "rows_blocks_per_sm": tuning.rows_blocks_per_sm}}
+
+
 def run_ours(args) -> dict | None:
     import torch
 
@@ -243,7 +404,8 @@ def run_ours(args) -> dict | None:
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
     traj_h, ksp_h = make_inputs(seed=7 + rank)
-    cpu = cpu_reference_rate(traj_h, ksp_h) if rank == 0 else None
+    cpu = cpu_kb_rate(traj_h, ksp_h) if rank == 0 else None
+    cpu_linear = cpu_reference_rate(traj_h, ksp_h) if rank == 0 else None
 
     g = gpu.kb_gridding(image=IMAGE, grid=GRID, channels=COILS, samples=traj_h.shape[1], frames=FRAMES, width=WIDTH,
                         output=gpu.OUTPUT_RSS)
@@ -384,6 +546,17 @@ def run_ours(args) -> dict | None:
     if not np.isfinite(oh.numpy()).all():
         raise RuntimeError("non-finite reconstruction")
 
+    # ---- outside every timed region: accuracy of the timed call's output,
+    # the width-6 form, and the drop-in operator through its plug-in
+    accuracy = width6 = dropin = None
+    if rank == 0:
+        step()
+        torch.cuda.synchronize()
+        accuracy = accuracy_check(out.cpu().numpy(), traj_h, ksp_h, frames=(0, FRAMES // 2))
+        if not args.skip_extra:
+            width6 = width6_leg("", k, t, traj_h, ksp_h, dev, args.steps, args.warmup)
+            dropin = dropin_leg(args.steps, args.warmup)
+
     ms, e2e_ms = max_over_ranks(dist, ms, e2e_ms)
     if rank != 0:
         return None
@@ -441,7 +614,11 @@ def run_ours(args) -> dict | None:
                 "speedup_vs_per_frame_loop": per_frame_ms / ms, "launches_per_call": per_call_launches},
         "roofline": roofline, "kernels": per_kernel,
         "clocks": clocks.summary(),
+        "accuracy": accuracy,
         "cpu_baseline": cpu,
+        "reference_cpu_linear": cpu_linear,
+        "width6": width6,
+        "dropin": dropin,
     }
 
 
@@ -776,6 +953,8 @@ def main() -> int:
     ap.add_argument("--serve", action="store_true", help="served-stream benchmark (separate JSON line)")
     ap.add_argument("--rows", action="store_true", help="the other hot-path rows (one JSON line each)")
     ap.add_argument("--spokes3", type=int, default=40000, help="--rows: spokes of the 3-D kooshball (0 skips it)")
+    ap.add_argument("--skip-extra", action="store_true",
+                    help="skip the width-6 and drop-in legs (small profiling runs)")
     ap.add_argument("--serve-requests", type=int, default=160)
     ap.add_argument("--serve-slots", type=int, default=4)
     ap.add_argument("--serve-cap-gib", type=int, default=24)

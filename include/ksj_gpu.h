@@ -112,6 +112,10 @@ typedef struct ksj_gpu_gridding_tuning {
   uint32_t frames_per_pass; /* frames per row/column pass (the row-transformed grid of one pass stays in L2) */
   uint32_t rows_blocks_per_sm; /* 1 or 2 resident row CTAs per SM (2 caps registers at 80 per thread) */
   uint32_t coil_parts;      /* 1 or 2: a row CTA's coil group is split into this many independent list tasks */
+  uint32_t wait_fault_polls; /* tests only; 0 in normal use.  Nonzero: every later segment of a long binning
+                                list waits for a count that never comes and gives up after this many polls,
+                                raising KSJ_GPU_FLAG_WAIT_TIMEOUT (the output is then invalid): exercises the
+                                bounded-wait path of the row pass without a fault */
 } ksj_gpu_gridding_tuning;
 
 /* Workspace bytes ksj_gpu_gridding_adjoint needs for `desc` (0 on a bad desc). */
@@ -240,7 +244,8 @@ KSJ_GPU_API ksj_gpu_status ksj_gpu_pipe_menon_dcf3(const ksj_gpu_gridding3_desc*
 /* Exact direct adjoint NUDFT, no DCF:
  *   img(c)(r, col) = sum_s y(c)(s) exp(i (k_row,s (r - row_origin) + k_col,s (col - col_origin)))
  * d_kspace [channel][sample] complex64, d_traj [sample][2], d_out coil-last
- * complex64 [row][col][channel].  Workspace: ksj_gpu_direct_workspace_bytes. */
+ * complex64 [row][col][channel].  channels <= 524,280 (KSJ_GPU_ERROR_UNSUPPORTED
+ * above).  Workspace: ksj_gpu_direct_workspace_bytes. */
 KSJ_GPU_API size_t ksj_gpu_direct_workspace_bytes(uint32_t rows, uint32_t cols, uint32_t channels);
 KSJ_GPU_API ksj_gpu_status ksj_gpu_direct_adjoint(uint32_t rows, uint32_t cols, double row_origin, double col_origin,
                                                   uint32_t channels, uint32_t samples, const void* d_kspace,
@@ -277,23 +282,24 @@ KSJ_GPU_API ksj_gpu_status ksj_gpu_direct_forward(uint32_t rows, uint32_t cols, 
                                                   const float* d_traj, void* d_out, void* stream);
 
 /* The direct NUDFT adjoint above without a caller workspace and without any
- * allocation.  No counterpart in the reference: its direct adjoint
- * (libs/numerics/kspacejet-nufft/src/eigen/eigen_nufft_direct_nudft.cpp:77-97)
- * is a CPU loop writing the image in place.  For callers that cannot allocate device memory at call
- * time: hosts that bind only this C ABI and own no device allocator, and
- * latency-bound loops where cudaMalloc/cudaFree would synchronise the device
- * and stall every other stream.  Same kernels and same output as
- * ksj_gpu_direct_adjoint.
+ * allocation.  No counterpart in the reference.  For callers that cannot
+ * allocate device memory at call time: hosts that bind only this C ABI and
+ * own no device allocator, and latency-bound loops where cudaMalloc/cudaFree
+ * would synchronise the device and stall every other stream.  Same kernels
+ * and same output as ksj_gpu_direct_adjoint.
  *   - The coil-major intermediate lives in a file-scope device array of
  *     ksj_gpu_direct_static_scratch_bytes() = 8 MiB per device, so
  *     rows * cols * channels <= 1,048,576 (e.g. 128 x 128 x 64, 256 x 256 x 16);
  *     larger requests return KSJ_GPU_ERROR_WORKSPACE before any device work.
+ *     channels <= 524,280 as for ksj_gpu_direct_adjoint (UNSUPPORTED above).
  *   - Nothing needs to start at zero: every scratch element the call reads
  *     was written earlier in the same call.
  *   - The first call on each device (with that device current) looks up the
  *     array's address, which may load the module; make that first call before
- *     any stream capture.  The device used is the current device; `stream`
- *     must belong to it.
+ *     any stream capture.  The address is kept with the CUDA context it was
+ *     taken in and looked up again when the current context changes (after a
+ *     cudaDeviceReset, for instance).  The device used is the current device;
+ *     `stream` must belong to it.
  *   - All calls on one device share the one array: calls that overlap in time
  *     (different streams, or host threads without ordering) race on it and
  *     give wrong results.  Serialise them, e.g. on one stream. */
@@ -443,6 +449,12 @@ KSJ_GPU_API ksj_gpu_status ksj_gpu_context_copy(ksj_gpu_context* context, void* 
 KSJ_GPU_API ksj_gpu_status ksj_gpu_context_sync(ksj_gpu_context* context);
 /* Total device bytes and streams the context holds (the Provider declares them). */
 KSJ_GPU_API uint64_t ksj_gpu_context_device_bytes(const ksj_gpu_context* context);
+/* Host-side fault injection for tests of the plug-ins' failure paths: the
+ * next `count` device allocations ksj_gpu_context_buffer would make return
+ * KSJ_GPU_ERROR_OUT_OF_MEMORY without calling cudaMalloc (0 clears).  The
+ * device is not touched.  No counterpart in the reference (its tests fake a
+ * misbehaving Provider instead). */
+KSJ_GPU_API void ksj_gpu_inject_allocation_failures(uint32_t count);
 
 /* Per-kernel timing for measurement.  While enabled, every kernel the
  * library launches is bracketed by CUDA events on the stream it is launched

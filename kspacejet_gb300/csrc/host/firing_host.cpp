@@ -384,6 +384,27 @@ KSJH_API void ksjh_destroy(ksjh_instance* inst) {
   delete inst;
 }
 
+// operator_on_cancel for a cancelled (kind 1) or failed (kind 2) scan: the
+// terminal protocol's cancellation path (provider.h:676-694): no lease, no
+// output grants.  Returns the provider's status; `error` (512 bytes) gets
+// its message.
+KSJH_API uint32_t ksjh_cancel(ksjh_instance* inst, uint32_t kind, char* error) {
+  if (inst == nullptr) return KSJ_STATUS_INVALID_ARGUMENT;
+  ksj_cancel_context cc{};
+  cc.abi = header(sizeof(cc));
+  cc.kind = kind;
+  cc.terminal_epoch = 89;
+  cc.cancellation_generation = 1;
+  cc.reason.abi = header(sizeof(cc.reason));
+  static const char kReason[] = "cancelled by the host";
+  cc.reason.data = kReason;
+  cc.reason.size = sizeof(kReason) - 1;
+  ksj_error_view e = empty_error();
+  const ksj_status st = inst->module->api.operator_on_cancel(inst->op, inst->context, inst->key, &cc, &e);
+  if (error) copy_error(e, error);
+  return st;
+}
+
 KSJH_API size_t ksjh_firing_size(void) { return sizeof(ksjh_firing); }
 
 KSJH_API uint32_t ksjh_fire(ksjh_instance* inst, ksjh_firing* f) {

@@ -117,6 +117,7 @@ struct Shape {
   float row_origin, col_origin;
   float phase_row, phase_col, phase_sign;  // origin-phase coefficients
   int coil_group, column_block, list_capacity, frames_per_pass, rows_blocks, coil_parts;
+  uint32_t wait_fault;  // tests only: segment waits that cannot succeed, given up after this many polls
   DifPlan plan_rows, plan_cols;
 };
 
@@ -265,6 +266,7 @@ ksj_gpu_status make_shape(const ksj_gpu_gridding_desc* d, const ksj_gpu_gridding
   if (parts == 0) parts = 1;
   if ((parts != 1 && parts != 2) || parts > cg) return KSJ_GPU_ERROR_INVALID_ARGUMENT;
   s->coil_parts = parts;
+  s->wait_fault = has(offsetof(ksj_gpu_gridding_tuning, wait_fault_polls) + 4) ? t->wait_fault_polls : 0u;
   return KSJ_GPU_OK;
 }
 
@@ -948,6 +950,8 @@ struct RowsArgs {
   int coil_group, coil_parts;
   int out_cols, cpitch;
   int col_shift;  // kept column of frequency k: (k + col_shift) mod grid_cols, when below out_cols
+  uint32_t wait_limit;   // polls before a segment wait gives up
+  int wait_beyond;       // added to every segment wait's target: 0, or unreachable in the wait-fault test mode
   DifPlan plan;
 };
 
@@ -1104,7 +1108,8 @@ __device__ __forceinline__ void grid_entries_regs(float2 (&r)[kChunk], const Row
 // itself in (the later segments do not wait out the limit as well) and
 // KSJ_GPU_FLAG_WAIT_TIMEOUT is raised.
 __device__ __forceinline__ void put_chunk(const float2 (&r)[kChunk], float2* dst, int stride, int width, bool live,
-                                          int seg, int* counter, uint32_t* flags) {
+                                          int seg, int* counter, uint32_t* flags, uint32_t wait_limit,
+                                          int wait_beyond) {
   if (counter == nullptr) {
     if (live) {
 #pragma unroll
@@ -1117,8 +1122,8 @@ __device__ __forceinline__ void put_chunk(const float2 (&r)[kChunk], float2* dst
   bool ok = true;
   if (seg > 0) {
     uint32_t polls = 0;
-    while (*reinterpret_cast<volatile int*>(counter) < 32 * seg) {
-      if (++polls >= kWaitLimit) {
+    while (*reinterpret_cast<volatile int*>(counter) < 32 * seg + wait_beyond) {
+      if (++polls >= wait_limit) {
         ok = false;
         atomicOr(flags, KSJ_GPU_FLAG_WAIT_TIMEOUT);
         break;
@@ -1195,7 +1200,8 @@ __device__ __forceinline__ void rows_grid_regs(const RowsArgs& a, int f, int cgi
     float2 r[kChunk];
     grid_entries_regs<W, kFormat, kWrap, kAR>(r, a, sample_base, coil_ok, lane, chunk * kChunk, xent, e1 - e0, meta);
     put_chunk(r, acc + static_cast<size_t>(chunk * kChunk) * 32 + lane, 32, min(kChunk, a.grid_cols - chunk * kChunk),
-              true, seg, list_segments(n) > 1 ? tasks.combined + chunk : nullptr, a.flags);
+              true, seg, list_segments(n) > 1 ? tasks.combined + chunk : nullptr, a.flags, a.wait_limit,
+              a.wait_beyond);
   }
 }
 
@@ -1338,7 +1344,7 @@ __global__ void __launch_bounds__(kThreads, kBlocks) k_rows(RowsArgs a) {
         grid_entries_regs<W, kFormat, true, kAheadRegs>(r, a, rbase, rok, lane, col_lo,
                                                         xent + static_cast<size_t>(e0) * kMV, e1 - e0, meta);
         put_chunk(r, acc + addr(rc, col_lo), cg, min(kChunk, a.grid_cols - col_lo), lane_coil, seg,
-                  tasks.combined + part * a.nchunks + chunk, a.flags);
+                  tasks.combined + part * a.nchunks + chunk, a.flags, a.wait_limit, a.wait_beyond);
         continue;
       }
       const int col_hi = min(col_lo + kChunk, a.grid_cols);
@@ -1863,6 +1869,8 @@ ksj_gpu_status launch_all(const Shape& s, const Layout& l, const ksj_gpu_griddin
   r.entries_per_frame = s.entries_per_frame;
   r.coil_group = s.coil_group;
   r.coil_parts = s.coil_parts;
+  r.wait_limit = s.wait_fault ? s.wait_fault : kWaitLimit;
+  r.wait_beyond = s.wait_fault ? (1 << 30) : 0;
   r.out_cols = s.out_cols;
   r.cpitch = s.cpitch;
   r.plan = s.plan_cols;
@@ -2485,6 +2493,8 @@ ksj_gpu_status launch_all3(const Shape& s, const Layout3& l, const ksj_gpu_gridd
   r.entries_per_frame = 0;
   r.coil_group = s.coil_group;
   r.coil_parts = s.coil_parts;
+  r.wait_limit = s.wait_fault ? s.wait_fault : kWaitLimit;
+  r.wait_beyond = s.wait_fault ? (1 << 30) : 0;
   r.out_cols = n;
   r.cpitch = s.cpitch;
   r.plan = s.plan_cols;
@@ -3134,7 +3144,9 @@ extern "C" ksj_gpu_status ksj_gpu_read_flags(const void* d_workspace, void* stre
 
 namespace {
 std::mutex g_tune_mutex;
-std::map<std::tuple<uint32_t, uint32_t, uint32_t, uint32_t, uint32_t, uint32_t, uint32_t, uint32_t, uint32_t,
+// keyed by the shape and the device: a tuning is chosen against one device's
+// shared-memory and SM limits
+std::map<std::tuple<int, uint32_t, uint32_t, uint32_t, uint32_t, uint32_t, uint32_t, uint32_t, uint32_t, uint32_t,
                     uint32_t, uint32_t>,
          ksj_gpu_gridding_tuning>
     g_tune_cache;
@@ -3145,7 +3157,9 @@ extern "C" ksj_gpu_status ksj_gpu_gridding_tune(const ksj_gpu_gridding_desc* des
                                                 void* d_workspace, size_t workspace_bytes, void* stream,
                                                 ksj_gpu_gridding_tuning* tuning) {
   if (desc == nullptr || tuning == nullptr) return KSJ_GPU_ERROR_INVALID_ARGUMENT;
-  const auto key = std::make_tuple(desc->kernel, desc->image_rows, desc->image_cols, desc->grid_rows,
+  int device = 0;
+  if (cudaGetDevice(&device) != cudaSuccess) return KSJ_GPU_ERROR_CUDA;
+  const auto key = std::make_tuple(device, desc->kernel, desc->image_rows, desc->image_cols, desc->grid_rows,
                                    desc->grid_cols, desc->kernel_width, desc->channels, desc->samples, desc->frames,
                                    desc->output, desc->sample_format);
   {

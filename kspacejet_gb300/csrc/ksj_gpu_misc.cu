@@ -89,6 +89,7 @@ namespace {
 constexpr int kDirectPixels = 128;  // threads (pixels) per block
 constexpr int kDirectTile = 256;    // samples staged per iteration
 constexpr int kDirectCoils = 8;     // accumulators per thread
+constexpr uint32_t kDirectChannelLimit = 65535u * kDirectCoils;  // grid.y of the launch
 
 // img[c][r][col] = sum_s y[c][s] exp(i (k_r,s (r - r0) + k_c,s (col - c0))),
 // summed in sample order in float; the phase of every (pixel, sample) pair
@@ -277,6 +278,7 @@ extern "C" ksj_gpu_status ksj_gpu_direct_adjoint(uint32_t rows, uint32_t cols, d
     return KSJ_GPU_ERROR_INVALID_ARGUMENT;
   if (rows > 8192 || cols > 8192 || static_cast<uint64_t>(rows) * cols > (1u << 26))
     return KSJ_GPU_ERROR_UNSUPPORTED;
+  if (channels > kDirectChannelLimit) return KSJ_GPU_ERROR_UNSUPPORTED;  // launch grid y = ceil(C / 8) <= 65535
   const float ro = static_cast<float>(row_origin), co = static_cast<float>(col_origin);
   if (static_cast<double>(ro) != row_origin || static_cast<double>(co) != col_origin)
     return KSJ_GPU_ERROR_UNSUPPORTED;
@@ -389,6 +391,23 @@ extern "C" ksj_gpu_status ksj_gpu_rss_coil_last(uint64_t pixels, uint32_t channe
 
 // ------------------------------------------------------------------ context
 
+namespace {
+// Host-side allocation fault injection (tests): the next N device
+// allocations of ksj_gpu_context_buffer report out-of-memory without calling
+// cudaMalloc.
+std::atomic<uint32_t> g_injected_allocation_failures{0};
+
+bool take_injected_allocation_failure() {
+  uint32_t n = g_injected_allocation_failures.load();
+  while (n > 0) {
+    if (g_injected_allocation_failures.compare_exchange_weak(n, n - 1)) return true;
+  }
+  return false;
+}
+}  // namespace
+
+extern "C" void ksj_gpu_inject_allocation_failures(uint32_t count) { g_injected_allocation_failures.store(count); }
+
 struct ksj_gpu_context {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -442,6 +461,7 @@ extern "C" ksj_gpu_status ksj_gpu_context_buffer(ksj_gpu_context* ctx, uint32_t 
       ctx->buffer_bytes[slot] = 0;
     }
     void* p = nullptr;
+    if (take_injected_allocation_failure()) return KSJ_GPU_ERROR_OUT_OF_MEMORY;
     if (cudaMalloc(&p, bytes) != cudaSuccess) {
       cudaGetLastError();
       return KSJ_GPU_ERROR_OUT_OF_MEMORY;
@@ -538,15 +558,40 @@ extern "C" uint32_t ksj_gpu_timing_read(uint32_t max_entries, char* names, uint6
 // ksj_gpu_direct_adjoint_static runs the kernels of ksj_gpu_direct_adjoint
 // with the coil-major intermediate in a file-scope device array instead of a
 // caller workspace, so the call itself allocates nothing.  The array's address
-// is looked up once per device (with that device current) and kept.
+// is looked up once per device context (with that device current) and kept
+// with the context it belongs to: after a cudaDeviceReset, or a primary
+// context released and created again, the module is loaded anew and the
+// array may move, so a changed current context looks the address up again.
 
 namespace ksj_gpu {
 namespace {
 constexpr size_t kDirectStaticScratchBytes = size_t(8) << 20;  // rows x cols x channels x 8 B at most
 __device__ __align__(256) unsigned char g_direct_scratch[kDirectStaticScratchBytes];
 constexpr int kStaticScratchDevices = 64;
+struct StaticScratch {
+  void* context = nullptr;  // the CUcontext the address was taken in
+  void* address = nullptr;
+};
 std::mutex g_direct_scratch_mutex;
-void* g_direct_scratch_ptr[kStaticScratchDevices] = {};
+StaticScratch g_direct_scratch_at[kStaticScratchDevices];
+
+using CtxGetCurrentFn = int (*)(void**);  // cuCtxGetCurrent(CUcontext*)
+
+CtxGetCurrentFn ctx_get_current() {
+  static CtxGetCurrentFn fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    return reinterpret_cast<CtxGetCurrentFn>(p);
+  }();
+  return fn;
+}
+
+// The direct adjoint's launch grid has ceil(channels / kDirectCoils) blocks
+// along y, at most 65 535.
+constexpr uint32_t kDirectMaxChannels = kDirectChannelLimit;
 }  // namespace
 }  // namespace ksj_gpu
 
@@ -567,18 +612,30 @@ extern "C" ksj_gpu_status ksj_gpu_direct_adjoint_static(uint32_t rows, uint32_t 
   // the intermediate must fit the static array: rejected before any device work
   if (static_cast<uint64_t>(rows) * cols * channels * sizeof(float2) > kDirectStaticScratchBytes)
     return KSJ_GPU_ERROR_WORKSPACE;
+  if (channels > kDirectMaxChannels) return KSJ_GPU_ERROR_UNSUPPORTED;
   int device = 0;
   if (cudaGetDevice(&device) != cudaSuccess) return KSJ_GPU_ERROR_CUDA;
   if (device < 0 || device >= kStaticScratchDevices) return KSJ_GPU_ERROR_UNSUPPORTED;
+  const CtxGetCurrentFn get_ctx = ctx_get_current();
+  if (get_ctx == nullptr) return KSJ_GPU_ERROR_CUDA;
   void* scratch = nullptr;
   {
     std::lock_guard<std::mutex> lock(g_direct_scratch_mutex);
-    if (g_direct_scratch_ptr[device] == nullptr) {
+    StaticScratch& at = g_direct_scratch_at[device];
+    void* ctx = nullptr;
+    // with no context current yet, the symbol lookup creates the primary one
+    if (get_ctx(&ctx) != 0) return KSJ_GPU_ERROR_CUDA;
+    if (at.address == nullptr || ctx == nullptr || ctx != at.context) {
       void* p = nullptr;
-      if (cudaGetSymbolAddress(&p, g_direct_scratch) != cudaSuccess || p == nullptr) return KSJ_GPU_ERROR_CUDA;
-      g_direct_scratch_ptr[device] = p;
+      if (cudaGetSymbolAddress(&p, g_direct_scratch) != cudaSuccess || p == nullptr) {
+        cudaGetLastError();
+        return KSJ_GPU_ERROR_CUDA;
+      }
+      if (get_ctx(&ctx) != 0 || ctx == nullptr) return KSJ_GPU_ERROR_CUDA;
+      at.context = ctx;
+      at.address = p;
     }
-    scratch = g_direct_scratch_ptr[device];
+    scratch = at.address;
   }
   cudaStream_t cs = static_cast<cudaStream_t>(stream);
   float2* tmp = static_cast<float2*>(scratch);

@@ -323,6 +323,14 @@ ksj_status on_cancel(ksj_provider_operator* o, ksj_execution_context* c, ksj_key
   if (!is_context(o, c) || !is_key_state(o, k) || !full_header(d) || d->reserved0 != 0 ||
       (d->kind != KSJ_PROVIDER_SCAN_END_CANCELLED && d->kind != KSJ_PROVIDER_SCAN_END_FAILED))
     return fail(err, KSJ_STATUS_INVALID_ARGUMENT, kErrInvalidArgument);
+  // cancellation emits nothing and only releases provider work
+  // (provider.h:676-694): firings finish their device work before they
+  // return, so nothing is in flight; the scan's device memory and stream are
+  // freed here (a later firing creates them again) -- no allocation, no throw
+  if (o->gpu != nullptr) {
+    ksj_gpu_context_destroy(o->gpu);
+    o->gpu = nullptr;
+  }
   return KSJ_STATUS_OK;
 }
 

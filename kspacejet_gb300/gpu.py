@@ -43,7 +43,7 @@ class GriddingTuning(ctypes.Structure):
     _fields_ = [("struct_size", ctypes.c_uint32), ("coil_group", ctypes.c_uint32),
                 ("column_block", ctypes.c_uint32), ("list_capacity", ctypes.c_uint32),
                 ("frames_per_pass", ctypes.c_uint32), ("rows_blocks_per_sm", ctypes.c_uint32),
-                ("coil_parts", ctypes.c_uint32)]
+                ("coil_parts", ctypes.c_uint32), ("wait_fault_polls", ctypes.c_uint32)]
 
 
 _lib = None
@@ -71,6 +71,8 @@ def lib() -> ctypes.CDLL:
                                                ctypes.POINTER(u32), ctypes.POINTER(u64), ctypes.POINTER(u64), vp, vp]
         L.ksj_gpu_read_flags.restype = ctypes.c_int32
         L.ksj_gpu_read_flags.argtypes = [vp, vp, ctypes.POINTER(u32)]
+        L.ksj_gpu_inject_allocation_failures.restype = None
+        L.ksj_gpu_inject_allocation_failures.argtypes = [u32]
         L.ksj_gpu_gridding_tune.restype = ctypes.c_int32
         L.ksj_gpu_gridding_tune.argtypes = [ctypes.POINTER(GriddingDesc), vp, vp, vp, vp, vp, sz, vp,
                                             ctypes.POINTER(GriddingTuning)]

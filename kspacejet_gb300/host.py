@@ -15,6 +15,8 @@ TYPE_KSPACE, TYPE_TRAJECTORY, TYPE_COIL_IMAGE, TYPE_IMAGE = 0, 1, 2, 3
 STATUS = {0: "OK", 1: "BAD_ABI", 2: "INVALID_ARGUMENT", 3: "UNSUPPORTED", 4: "RESOURCE_EXHAUSTED", 5: "CANCELLED",
           6: "FAILED_PRECONDITION", 7: "INTERNAL_ERROR", 8: "CONTRACT_VIOLATION"}
 OK, INVALID_ARGUMENT, UNSUPPORTED, INTERNAL_ERROR, CONTRACT_VIOLATION = 0, 2, 3, 7, 8
+RESOURCE_EXHAUSTED, FAILED_PRECONDITION = 4, 6
+SCAN_END_NORMAL, SCAN_END_CANCELLED, SCAN_END_FAILED = 0, 1, 2
 
 
 class Firing(ctypes.Structure):
@@ -64,6 +66,8 @@ def lib() -> ctypes.CDLL:
         L.ksjh_firing_size.restype = ctypes.c_size_t
         L.ksjh_fire.restype = ctypes.c_uint32
         L.ksjh_fire.argtypes = [vp, ctypes.POINTER(Firing)]
+        L.ksjh_cancel.restype = ctypes.c_uint32
+        L.ksjh_cancel.argtypes = [vp, ctypes.c_uint32, cp]
         if L.ksjh_firing_size() != ctypes.sizeof(Firing):
             raise RuntimeError("firing host struct layout mismatch")
         _lib = L
@@ -180,6 +184,12 @@ class Instance:
 
     def __exit__(self, *a):
         self.close()
+
+    def cancel(self, kind: int = SCAN_END_CANCELLED) -> tuple[int, str]:
+        """operator_on_cancel (no lease, no grants); returns (status, error message)."""
+        err = ctypes.create_string_buffer(512)
+        st = lib().ksjh_cancel(self._h, kind, err)
+        return int(st), err.value.decode(errors="replace")
 
     def fire(self, inputs: list[tuple[np.ndarray, int, int]], output: np.ndarray, output_type: int,
              scratch_bytes: int = 0, metadata: bytes = b"\x31\x32\x33", keys=(71, 73), input_keys=None,

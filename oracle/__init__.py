@@ -179,6 +179,17 @@ class Oracle(_Base):
         return self._fn("kb_deapod", ctypes.c_double,
                         [ctypes.c_double, ctypes.c_int, ctypes.c_double, _i64])(x, width, beta, g)
 
+    def direct_adjoint_at(self, pixels: np.ndarray, samples: np.ndarray, traj: np.ndarray, row_origin: float,
+                          col_origin: float) -> np.ndarray:
+        """The exact FP64 direct adjoint NUDFT at the (row, col) pairs `pixels` [P, 2] only."""
+        pixels = np.ascontiguousarray(pixels, dtype=np.int64).reshape(-1, 2)
+        samples = np.ascontiguousarray(samples, dtype=np.complex128)
+        traj = np.ascontiguousarray(traj, dtype=np.float64).reshape(-1, 2)
+        out = np.zeros(pixels.shape[0], dtype=np.complex128)
+        self._fn("direct_nudft2_adjoint_at_f64", None, [_i64, _ptr, _dbl, _dbl, _ptr, _ptr, _i64, _ptr])(
+            pixels.shape[0], _p(pixels), row_origin, col_origin, _p(samples), _p(traj), samples.shape[0], _p(out))
+        return out
+
     def kb_gridding(self, grid: int, n: int, samples: np.ndarray, traj: np.ndarray, dcf: np.ndarray | None,
                     width: int = 4, sigma: float | None = None, beta: float | None = None,
                     row_origin: float | None = None, col_origin: float | None = None) -> np.ndarray:
@@ -199,6 +210,24 @@ class Oracle(_Base):
             raise OracleError("KB gridding rejected its configuration")
         return out
 
+
+    def kb_gridding_f32(self, grid: int, n: int, samples: np.ndarray, traj: np.ndarray, dcf: np.ndarray | None,
+                        width: int = 4, sigma: float | None = None, beta: float | None = None) -> np.ndarray:
+        """The same Kaiser-Bessel reconstruction as a single-precision CPU program with an FFT (one coil,
+        origin (n-1)/2): the timed CPU baseline of the KB forms, not a parity target."""
+        samples = np.ascontiguousarray(samples, dtype=np.complex64)
+        traj = np.ascontiguousarray(traj, dtype=np.float32)
+        if beta is None:
+            beta = self.kb_beta(width, sigma if sigma is not None else grid / n)
+        d = None if dcf is None else np.ascontiguousarray(dcf, dtype=np.float32)
+        out = np.zeros((n, n), dtype=np.complex64)
+        fn = self._fn("kb_gridding2_adjoint_f32", ctypes.c_int,
+                      [_i64, _i64, ctypes.c_int, _dbl, _dbl, _dbl, _ptr, _ptr, _ptr, _i64, _ptr])
+        rc = fn(grid, n, width, beta, (n - 1) / 2.0, (n - 1) / 2.0, _p(samples), _p(traj),
+                None if d is None else _p(d), samples.shape[0], _p(out))
+        if rc != 0:
+            raise OracleError("single-precision KB gridding rejected its configuration")
+        return out
 
     def kb_forward(self, grid: int, n: int, image: np.ndarray, traj: np.ndarray, width: int = 4,
                    sigma: float | None = None, beta: float | None = None) -> np.ndarray:

@@ -394,6 +394,29 @@ KSJO_EXPORT void ksjo_direct_nudft2_adjoint_f64(int64_t rows, int64_t cols, doub
   }
 }
 
+/* direct_nudft2_adjoint at selected pixels only (FP64): out[i] is the value
+ * the full form above gives at (pixels[2i], pixels[2i+1]).  The sum over
+ * samples is the same, in the same order; only pixels nobody asked for are
+ * skipped, so the exact NUDFT stays affordable at large images and sample
+ * counts. */
+KSJO_EXPORT void ksjo_direct_nudft2_adjoint_at_f64(int64_t npix, const int64_t* pixels, double row_origin,
+                                                   double col_origin, const double* samples_in, const double* traj,
+                                                   int64_t m, double* out) {
+  const cf64* samples = (const cf64*)samples_in;
+  cf64* o = (cf64*)out;
+  for (int64_t i = 0; i < npix; ++i) {
+    const double rp = (double)pixels[2 * i] - row_origin;
+    const double cp = (double)pixels[2 * i + 1] - col_origin;
+    cf64 sum = {0.0, 0.0};
+    for (int64_t s = 0; s < m; ++s) {
+      const double phase = traj[2 * s] * rp + traj[2 * s + 1] * cp;
+      const cf64 e = {cos(phase), sin(phase)};
+      sum = cadd_d(sum, cmul_d(samples[s], e));
+    }
+    o[i] = sum;
+  }
+}
+
 KSJO_EXPORT void ksjo_direct_nudft2_adjoint_f32(int64_t rows, int64_t cols, double row_origin, double col_origin,
                                                 const float* samples_in, const float* traj, int64_t m,
                                                 float* image_out) {
@@ -567,6 +590,136 @@ KSJO_EXPORT int ksjo_kb_gridding2_adjoint_f64(int64_t g, int64_t n, int width, d
     }
   }
   free(grid);
+  return 0;
+}
+
+/* ---------------------------------------- Kaiser-Bessel, single precision CPU
+ *
+ * The same Kaiser-Bessel reconstruction as ksjo_kb_gridding2_adjoint_f64 as a
+ * practical single-precision CPU program: float gridding with tap weights
+ * from the double kernel rounded once, a mixed-radix (2, 3, 4) decimation-in-
+ * time FFT with a twiddle table computed in double, the row transforms over
+ * every grid row and the column transforms over the kept columns only, then
+ * crop and deapodisation.  It is the timed CPU baseline for the KB forms
+ * (which the reference does not have), not a parity target; the tests check
+ * it against the FP64 form. */
+typedef struct {
+  int64_t n;
+  cf32* tw; /* exp(2 pi i t / n), t < n */
+} fftplan_f;
+
+static int fft_plan_f(fftplan_f* p, int64_t n) {
+  int64_t m = n;
+  while (m % 4 == 0) m /= 4;
+  while (m % 2 == 0) m /= 2;
+  while (m % 3 == 0) m /= 3;
+  if (m != 1) return -1;
+  p->n = n;
+  p->tw = (cf32*)malloc((size_t)n * sizeof(cf32));
+  if (!p->tw) return -1;
+  for (int64_t t = 0; t < n; ++t) {
+    const double a = 2.0 * kPiD * (double)t / (double)n;
+    p->tw[t].re = (float)cos(a);
+    p->tw[t].im = (float)sin(a);
+  }
+  return 0;
+}
+
+/* y[k] = sum_j x[j stride] exp(2 pi i j k / len), len | plan n; scratch >= 2 len */
+static void fft_dit_f(const fftplan_f* p, const cf32* x, int64_t stride, cf32* y, int64_t len, cf32* scratch) {
+  if (len == 1) { y[0] = x[0]; return; }
+  const int64_t r = (len % 4 == 0) ? 4 : (len % 2 == 0) ? 2 : 3;
+  const int64_t m = len / r;
+  const int64_t step = p->n / len;
+  for (int64_t q = 0; q < r; ++q) fft_dit_f(p, x + q * stride, stride * r, scratch + q * m, m, scratch + len);
+  for (int64_t k = 0; k < m; ++k) {
+    cf32 v[4];
+    for (int64_t q = 0; q < r; ++q) {
+      const cf32 w = p->tw[(q * k * step) % p->n];
+      v[q] = q == 0 ? scratch[k] : cmul_f(scratch[q * m + k], w);
+    }
+    if (r == 2) {
+      y[k] = cadd_f(v[0], v[1]);
+      y[k + m] = csub_f(v[0], v[1]);
+    } else if (r == 4) {
+      const cf32 a = cadd_f(v[0], v[2]), b = csub_f(v[0], v[2]);
+      const cf32 c = cadd_f(v[1], v[3]), dd = csub_f(v[1], v[3]);
+      const cf32 d = {-dd.im, dd.re}; /* i (v1 - v3) */
+      y[k] = cadd_f(a, c);
+      y[k + m] = cadd_f(b, d);
+      y[k + 2 * m] = csub_f(a, c);
+      y[k + 3 * m] = csub_f(b, d);
+    } else {
+      const float s3 = 0.86602540378443865f;
+      const cf32 t1 = cadd_f(v[1], v[2]);
+      const cf32 t2 = {v[0].re - 0.5f * t1.re, v[0].im - 0.5f * t1.im};
+      const cf32 d = csub_f(v[1], v[2]);
+      const cf32 t3 = {-s3 * d.im, s3 * d.re}; /* i sin(2 pi / 3) (v1 - v2) */
+      y[k] = cadd_f(v[0], t1);
+      y[k + m] = cadd_f(t2, t3);
+      y[k + 2 * m] = csub_f(t2, t3);
+    }
+  }
+}
+
+KSJO_EXPORT int ksjo_kb_gridding2_adjoint_f32(int64_t g, int64_t n, int width, double beta, double row_origin,
+                                              double col_origin, const float* samples_in, const float* traj,
+                                              const float* dcf, int64_t m, float* image_out) {
+  if (g < n || g < width || (width % 2) != 0 || width > 8) return -1;
+  fftplan_f plan;
+  if (fft_plan_f(&plan, g) != 0) return -1;
+  const cf32* samples = (const cf32*)samples_in;
+  cf32* image = (cf32*)image_out;
+  cf32* grid = (cf32*)calloc((size_t)(g * g), sizeof(cf32));
+  cf32* line = (cf32*)malloc((size_t)g * sizeof(cf32));
+  cf32* out = (cf32*)malloc((size_t)g * sizeof(cf32));
+  cf32* scratch = (cf32*)malloc((size_t)(4 * g + 64) * sizeof(cf32));
+  float* inv_d = (float*)malloc((size_t)n * sizeof(float));
+  if (!grid || !line || !out || !scratch || !inv_d) {
+    free(grid); free(line); free(out); free(scratch); free(inv_d); free(plan.tw);
+    return -1;
+  }
+  const double half = (double)(n / 2);
+  const double dr = half - row_origin, dc = half - col_origin;
+  const double scale = (double)g / (2.0 * kPiD);
+  for (int64_t s = 0; s < m; ++s) {
+    /* coordinates and phase in double (a float grid coordinate moves the
+       taps' weights by ~1e-5 at g = 384), then the sample arithmetic in float */
+    const double kr = traj[2 * s], kc = traj[2 * s + 1];
+    const double ur = kr * scale, uc = kc * scale;
+    const double ph = kr * dr + kc * dc;
+    const cf32 e = {(float)cos(ph), (float)sin(ph)};
+    const cf32 v = cmul_f(cscale_f(samples[s], dcf ? dcf[s] : 1.0f), e);
+    const int64_t r0 = (int64_t)floor(ur) - width / 2 + 1;
+    const int64_t c0 = (int64_t)floor(uc) - width / 2 + 1;
+    float wr[8], wc[8];
+    for (int a = 0; a < width; ++a) {
+      wr[a] = (float)ksjo_kb_kernel((double)(r0 + a) - ur, width, beta);
+      wc[a] = (float)ksjo_kb_kernel((double)(c0 + a) - uc, width, beta);
+    }
+    for (int a = 0; a < width; ++a) {
+      const int64_t rr = (((r0 + a) % g) + g) % g;
+      const cf32 va = cscale_f(v, wr[a]);
+      for (int b = 0; b < width; ++b) {
+        const int64_t cc = (((c0 + b) % g) + g) % g;
+        grid[rr * g + cc] = cadd_f(grid[rr * g + cc], cscale_f(va, wc[b]));
+      }
+    }
+  }
+  /* rows: every grid row; keep the n columns of the image (frequency q mod g) */
+  for (int64_t r = 0; r < g; ++r) {
+    fft_dit_f(&plan, grid + r * g, 1, out, g, scratch);
+    for (int64_t pc = 0; pc < n; ++pc) grid[r * g + pc] = out[(((pc - n / 2) % g) + g) % g];
+  }
+  for (int64_t p = 0; p < n; ++p) inv_d[p] = (float)(1.0 / ksjo_kb_deapod((double)(p - n / 2), width, beta, g));
+  /* columns: the n kept ones only, cropped and deapodised */
+  for (int64_t pc = 0; pc < n; ++pc) {
+    for (int64_t r = 0; r < g; ++r) line[r] = grid[r * g + pc];
+    fft_dit_f(&plan, line, 1, out, g, scratch);
+    for (int64_t pr = 0; pr < n; ++pr)
+      image[pr * n + pc] = cscale_f(out[(((pr - n / 2) % g) + g) % g], inv_d[pr] * inv_d[pc]);
+  }
+  free(grid); free(line); free(out); free(scratch); free(inv_d); free(plan.tw);
   return 0;
 }
 

@@ -348,8 +348,10 @@ def test_long_lists_byte_identical(native, cuda, orc, channels, grid, spokes):
 
 
 def test_bf16_sample_storage_bound(native, cuda, orc):
-    """BF16 sample storage, FP32 arithmetic: stated bound 1e-2 rel L2 against
-    the FP32-storage result (bfloat16 keeps 8 mantissa bits: ~2e-3 per value)."""
+    """BF16 sample storage, FP32 arithmetic: within 2e-3 rel L2 of the
+    FP32-storage result (bfloat16 keeps 8 mantissa bits: ~1.6e-3 per sample);
+    the bound against the FP64 oracle is tested on the batched shape
+    (test_gpu_config_shapes.py)."""
     import torch
     from kspacejet_gb300 import gpu
 
@@ -365,7 +367,7 @@ def test_bf16_sample_storage_bound(native, cuda, orc):
         g.run(k, t, o, g.new_workspace(cuda))
         res[fmt] = o.cpu().numpy()
     err = oracle.rel_l2(res[gpu.SAMPLES_BF16], res[gpu.SAMPLES_CF32])
-    assert 1e-5 < err < 1e-2
+    assert 1e-5 < err < 2e-3
 
 
 def test_direct_adjoint_matches_fp64(native, cuda, orc, fixtures):

@@ -87,6 +87,26 @@ def test_static_scratch_matches_workspace_entry_point():
         assert err <= REL_L2_TOL, (rows, cols, channels, err)
 
 
+def test_static_scratch_call_allocates_no_device_memory():
+    """The property the entry point exists for: after a first call on the
+    device, a further call changes the device's free memory by nothing
+    (cudaMemGetInfo read around it, no torch allocation in between)."""
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    L = _lib()
+    stream = torch.cuda.current_stream().cuda_stream
+    ks, traj = _inputs(8, 512, 5)
+    out = torch.empty((64, 64, 8), dtype=torch.complex64, device="cuda")
+    assert _static_call(L, 64, 64, ks, traj, out, stream) == OK
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(3):
+        assert _static_call(L, 64, 64, ks, traj, out, stream) == OK
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, (free0, free1)
+
+
 def test_static_scratch_rejects_oversize():
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
