@@ -1464,6 +1464,10 @@ struct ColsArgs {
   int out_pitch;                        // COIL_LAST: elements between pixels of the output (>= channels)
   int row_shift;                        // kept row of frequency k: (k + row_shift) mod grid_rows, when below out_rows
   DifPlan plan;
+  // persistent form (k_cols_ring): tiles of tile_coils coils x (kRingLines /
+  // tile_coils) columns; a unit is (frame, column block), tiles_per_unit
+  // tiles of consecutive coils each; units = frames of the pass x col_blocks
+  int tile_coils, tiles_per_unit, units, col_blocks;
 };
 
 
@@ -1624,6 +1628,159 @@ __global__ void __launch_bounds__(kColsThreads) k_cols(const __grid_constant__ C
   }
 }
 
+// Persistent column pass for the two-step column lengths.  Each CTA walks
+// its share of the (frame, column block) units -- units blockIdx.x,
+// blockIdx.x + gridDim.x, ... -- one tile of kRingLines lines (tile_coils
+// coils x kRingLines / tile_coils columns, all grid rows) at a time, through
+// a two-stage ring of shared-memory tiles: while the block transforms tile i,
+// the TMA copy of tile i + 1 is in flight, and tile i + 2's copy is issued as
+// soon as tile i's stage is free.  Per line the arithmetic is the one-shot
+// k_cols's (the same transform, crop and deapodisation); the RSS sums a
+// pixel's coils in channel order across the unit's tiles (the accumulator
+// carries over from tile to tile), so the bytes equal k_cols's.
+constexpr int kRingLines = 16;
+constexpr int kRingLgLines = 4;
+
+template <int kN>
+struct RingCfg;  // block size (step A of the two-step transform has kN / 16 x 16 tasks) and CTAs per SM
+template <>
+struct RingCfg<128> { static constexpr int kThreads = 256, kBlocks = 2; };
+template <>
+struct RingCfg<192> { static constexpr int kThreads = 256, kBlocks = 2; };
+template <>
+struct RingCfg<256> { static constexpr int kThreads = 256, kBlocks = 2; };
+template <>
+struct RingCfg<384> { static constexpr int kThreads = 384, kBlocks = 2; };
+template <>
+struct RingCfg<512> { static constexpr int kThreads = 512, kBlocks = 1; };
+
+template <int kN>
+__global__ void __launch_bounds__(RingCfg<kN>::kThreads, RingCfg<kN>::kBlocks)
+    k_cols_ring(const __grid_constant__ CUtensorMap inter_map, ColsArgs a) {
+  constexpr int kT = RingCfg<kN>::kThreads;
+  constexpr int kL = kRingLines;
+  constexpr int kLgL = kRingLgLines;
+  extern __shared__ __align__(16) unsigned char smem_cols[];
+  unsigned char* smem_raw = smem_cols;
+  const int tc = a.tile_coils;
+  const int lg_tc = ilog2(tc);
+  const int cb = kL / tc;  // columns per tile
+  const int lg_cb = kLgL - lg_tc;
+  const int tid = threadIdx.x;
+  const int tpu = a.tiles_per_unit;
+  constexpr size_t kTileElems = static_cast<size_t>(kN) * kL;
+  float2* tiles = reinterpret_cast<float2*>(smem_raw + ((128u - (smem_addr(smem_raw) & 127u)) & 127u));
+  float2* tw = tiles + 2 * kTileElems;
+  float* rss = reinterpret_cast<float*>(tw + kN);
+  const int npix = a.out_rows * cb;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(rss + ((npix + 1) & ~1));
+  float* inv_dr = reinterpret_cast<float*>(bars + 2);
+  constexpr uint32_t kTileBytes = static_cast<uint32_t>(kTileElems * sizeof(float2));
+  if (tid == 0) {
+    mbar_init(&bars[0], 1);
+    mbar_init(&bars[1], 1);
+    mbar_init_fence();
+  }
+  for (int i = tid; i < kN; i += kT) tw[i] = a.tw_rows[i];
+  for (int i = tid; i < npix; i += kT) rss[i] = 0.0f;
+  if (a.kb)
+    for (int i = tid; i < a.out_rows; i += kT) inv_dr[i] = __ldg(a.inv_dr + i);
+  __syncthreads();
+  const int my_units = a.units > static_cast<int>(blockIdx.x)
+                           ? (a.units - 1 - static_cast<int>(blockIdx.x)) / static_cast<int>(gridDim.x) + 1
+                           : 0;
+  const int ntiles = my_units * tpu;
+  auto unit_of = [&](int i) { return static_cast<int>(blockIdx.x) + (i / tpu) * static_cast<int>(gridDim.x); };
+  auto issue = [&](int i) {
+    const int u = unit_of(i), h = i - (i / tpu) * tpu;
+    const int f = a.frame0 + u / a.col_blocks;
+    const int col0 = (u - (u / a.col_blocks) * a.col_blocks) * cb;
+    float2* dst = tiles + (i & 1) * kTileElems;
+    mbar_arrive_expect_tx(&bars[i & 1], kTileBytes);
+    for (int k = 0; k < a.boxes; ++k)
+      tma_load_3d(dst + static_cast<size_t>(k) * a.box_rows * kL, &inter_map, h * tc, col0,
+                  f * kN + k * a.box_rows, &bars[i & 1]);
+  };
+  if (tid == 0)
+    for (int i = 0; i < 2 && i < ntiles; ++i) issue(i);
+  int i = 0;
+  bool ok = true;
+  for (; i < ntiles; ++i) {
+    const int b = i & 1;
+    const bool mine = mbar_wait_bounded(&bars[b], static_cast<uint32_t>((i >> 1) & 1), kWaitLimit);
+    if (!__syncthreads_and(mine)) {
+      ok = false;
+      break;
+    }
+    const int u = unit_of(i), h = i - (i / tpu) * tpu;
+    const int fg = a.frame0 + u / a.col_blocks;
+    const int col0 = (u - (u / a.col_blocks) * a.col_blocks) * cb;
+    const int coil0 = h * tc;
+    const int live_coils = min(tc, a.channels - coil0);
+    float2* tile = tiles + b * kTileElems;
+    auto emit = [&](int k, int ln, float2 v) {
+      int pr = k + a.row_shift;
+      if (pr >= kN) pr -= kN;
+      const int lc = ln >> lg_tc;
+      if (pr >= a.out_rows || col0 + lc >= a.out_cols || (ln & (tc - 1)) >= live_coils) return;
+      if (a.kb) {
+        const float sc = inv_dr[pr] * __ldg(a.inv_dc + col0 + lc);
+        v.x *= sc;
+        v.y *= sc;
+      }
+      if (a.output == KSJ_GPU_OUTPUT_RSS) {
+        float2* e = tile + (two_step_slot(k, kN) << kLgL) + ln;
+        e->x = __fadd_rn(__fmul_rn(v.x, v.x), __fmul_rn(v.y, v.y));
+      } else {
+        float2* o = static_cast<float2*>(a.out);
+        o[((static_cast<size_t>(fg) * a.out_rows + pr) * a.out_cols + col0 + lc) * a.out_pitch + coil0 +
+          (ln & (tc - 1))] = v;
+      }
+    };
+    fft_two_step<16, kN / 16>(tile, kLgL, tw, tid, kT, emit);
+    if (a.output == KSJ_GPU_OUTPUT_RSS) {
+      __syncthreads();
+      // channel-order sum per pixel (reductions.hpp:972-982), continued from
+      // the unit's previous tiles; thread q owns pixel q in both loops below
+      const int lane = tid & 31;
+      for (int q0 = tid - lane; q0 < npix; q0 += kT) {
+        const int q = q0 + lane;
+        const bool live = q < npix && col0 + (q & (cb - 1)) < a.out_cols;
+        const int pr = q >> lg_cb;
+        const int base = live ? (__ldg(a.pos_rows + pr) << kLgL) + ((q & (cb - 1)) << lg_tc) : 0;
+        float total = live ? rss[q] : 0.0f;
+        for (int t = 0; t < live_coils + 31; ++t) {
+          const int c = t - lane;
+          if (live && c >= 0 && c < live_coils) total = __fadd_rn(total, tile[base + c].x);
+        }
+        if (live) rss[q] = total;
+      }
+      if (h == tpu - 1) {
+        float* o = static_cast<float*>(a.out);
+        for (int q = tid; q < npix; q += kT) {
+          const int pr = q >> lg_cb;
+          const int l = q & (cb - 1);
+          if (col0 + l < a.out_cols) o[(static_cast<size_t>(fg) * a.out_rows + pr) * a.out_cols + col0 + l] =
+              __fsqrt_rn(rss[q]);
+          rss[q] = 0.0f;
+        }
+      }
+    }
+    __syncthreads();  // every thread is done with stage b
+    if (tid == 0 && i + 2 < ntiles) {
+      fence_proxy_async_shared();  // the stage was last written by the generic proxy
+      issue(i + 2);
+    }
+  }
+  if (!ok && tid == 0) {
+    // a copy never completed: report, then give the copies still in flight
+    // (tiles i and i + 1) a bounded chance to land before the block exits
+    atomicOr(a.flags, KSJ_GPU_FLAG_WAIT_TIMEOUT);
+    for (int t = i; t < i + 2 && t < ntiles; ++t)
+      mbar_wait_bounded(&bars[t & 1], static_cast<uint32_t>((t >> 1) & 1), kWaitLimit);
+  }
+}
+
 // ------------------------------------------------------------------ driver
 
 // The row-pass kernel a shape selects (rows_blocks: k_rows with that many
@@ -1718,6 +1875,76 @@ bool make_inter_map(const Shape& s, void* inter, CUtensorMap* map, int* box_rows
              CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
+
+// Tensor map for the persistent column pass: box (tile_coils coils,
+// kRingLines / tile_coils columns, box_rows rows).
+bool make_ring_map(const Shape& s, void* inter, int tile_coils, CUtensorMap* map, int* box_rows, int* boxes) {
+  Shape t = s;
+  t.col_group = tile_coils;
+  t.column_block = kRingLines / tile_coils;
+  return make_inter_map(t, inter, map, box_rows, boxes);
+}
+
+using RingKernel = void (*)(const __grid_constant__ CUtensorMap, ColsArgs);
+
+// The column pass of one shape: the persistent ring kernel for the two-step
+// column lengths, else one k_cols CTA per (frame, column block).  Both give
+// the same bytes.
+struct ColsPass {
+  bool ring = false;
+  ColsKernel kernel = nullptr;
+  size_t smem = 0;
+  int threads = kColsThreads;
+  int ctas = 0;
+  int column_block = 1;
+  int out_cols = 0;
+  CUtensorMap map;
+
+  bool setup(const Shape& s, void* inter, ColsArgs* c) {
+    const int tc = std::min(s.col_group, kRingLines);
+    const int cb = kRingLines / tc;
+    out_cols = s.out_cols;
+    ring = has_two_step_rows(s.grid_rows) && tc >= 2 && cb <= s.out_cols;
+    if (!ring) {
+      column_block = s.column_block;
+      smem = cols_smem_bytes(s);
+      kernel = cols_kernel_for(s.grid_rows);
+      return cols_kernel_setup(kernel, smem) && make_inter_map(s, inter, &map, &c->box_rows, &c->boxes);
+    }
+    column_block = cb;
+    c->tile_coils = tc;
+    c->tiles_per_unit = s.cpitch / tc;
+    c->col_blocks = (s.out_cols + cb - 1) / cb;
+    int blocks = 2;
+    switch (s.grid_rows) {
+      case 128: kernel = k_cols_ring<128>; threads = RingCfg<128>::kThreads; blocks = RingCfg<128>::kBlocks; break;
+      case 192: kernel = k_cols_ring<192>; threads = RingCfg<192>::kThreads; blocks = RingCfg<192>::kBlocks; break;
+      case 256: kernel = k_cols_ring<256>; threads = RingCfg<256>::kThreads; blocks = RingCfg<256>::kBlocks; break;
+      case 384: kernel = k_cols_ring<384>; threads = RingCfg<384>::kThreads; blocks = RingCfg<384>::kBlocks; break;
+      default: kernel = k_cols_ring<512>; threads = RingCfg<512>::kThreads; blocks = RingCfg<512>::kBlocks; break;
+    }
+    const size_t npix = static_cast<size_t>(s.out_rows) * cb;
+    smem = 128 + 2 * static_cast<size_t>(s.grid_rows) * kRingLines * sizeof(float2) + s.grid_rows * sizeof(float2) +
+           ((npix + 1) & ~size_t{1}) * sizeof(float) + 2 * sizeof(uint64_t) + static_cast<size_t>(s.out_rows) * sizeof(float);
+    int device = 0, sms = 0;
+    if (cudaGetDevice(&device) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || sms <= 0)
+      return false;
+    ctas = sms * blocks;
+    return cols_kernel_setup(kernel, smem) && make_ring_map(s, inter, tc, &map, &c->box_rows, &c->boxes);
+  }
+
+  // The column pass over nf frames starting at c.frame0.
+  void launch(ColsArgs c, int nf, cudaStream_t stream, const char* name) const {
+    LaunchScope scope(name, stream);
+    if (ring) {
+      c.units = nf * c.col_blocks;
+      kernel<<<std::min(ctas, c.units), threads, smem, stream>>>(map, c);
+    } else {
+      kernel<<<dim3((out_cols + column_block - 1) / column_block, nf), kColsThreads, smem, stream>>>(map, c);
+    }
+  }
+};
 
 // The binning lists of one call: per-sample records, list counts, offsets,
 // the scattered entries and their sort (and, when `expanded` is given, the
@@ -1899,11 +2126,8 @@ ksj_gpu_status launch_all(const Shape& s, const Layout& l, const ksj_gpu_griddin
   c.output = d->output == KSJ_GPU_OUTPUT_RSS ? KSJ_GPU_OUTPUT_RSS : KSJ_GPU_OUTPUT_COIL_LAST;
   c.out = coil_major ? static_cast<void*>(ws + l.coil_last) : d_out;
   c.out_pitch = s.channels;
-  CUtensorMap map;
-  if (!make_inter_map(s, inter, &map, &c.box_rows, &c.boxes)) return KSJ_GPU_ERROR_CUDA;
-  const size_t cols_smem = cols_smem_bytes(s);
-  const ColsKernel cols_kernel = cols_kernel_for(s.grid_rows);
-  if (!cols_kernel_setup(cols_kernel, cols_smem)) return KSJ_GPU_ERROR_CUDA;
+  ColsPass cols_pass;
+  if (!cols_pass.setup(s, inter, &c)) return KSJ_GPU_ERROR_CUDA;
 
   // frames in passes sized so one pass's row-transformed grid stays in L2
   const int pixels = s.out_rows * s.out_cols;
@@ -1927,11 +2151,7 @@ ksj_gpu_status launch_all(const Shape& s, const Layout& l, const ksj_gpu_griddin
     r.frame0 = f0;
     c.frame0 = f0;
     rows_launch.launch(r, s.grid_rows, (s.channels + s.coil_group - 1) / s.coil_group, nf, ps);
-    {
-      LaunchScope scope("k_cols", ps);
-      const dim3 grid((s.out_cols + s.column_block - 1) / s.column_block, nf);
-      cols_kernel<<<grid, kColsThreads, cols_smem, ps>>>(map, c);
-    }
+    cols_pass.launch(c, nf, ps, "k_cols");
     if (coil_major) {
       // [frame][pixel][channel] -> [frame][channel][pixel], this pass's frames
       const size_t fe = static_cast<size_t>(pixels) * s.channels;
@@ -2501,9 +2721,6 @@ ksj_gpu_status launch_all3(const Shape& s, const Layout3& l, const ksj_gpu_gridd
   r.col_shift = n / 2;
   RowsLauncher rows_launch;
   if (!rows_launch.setup<W, kFormat>(s)) return KSJ_GPU_ERROR_CUDA;
-  const size_t cols_smem = cols_smem_bytes(s);
-  const ColsKernel cols_kernel = cols_kernel_for(s.grid_rows);
-  if (!cols_kernel_setup(cols_kernel, cols_smem)) return KSJ_GPU_ERROR_CUDA;
   // columns of every plane (y transformed, cropped, y/x deapodised): [plane][pixel][cpitch]
   ColsArgs c{};
   c.tw_rows = tw_rows;
@@ -2525,25 +2742,20 @@ ksj_gpu_status launch_all3(const Shape& s, const Layout3& l, const ksj_gpu_gridd
   c.output = KSJ_GPU_OUTPUT_COIL_LAST;
   c.out = inter2;
   c.out_pitch = s.cpitch;
-  CUtensorMap map;
-  if (!make_inter_map(s, inter, &map, &c.box_rows, &c.boxes)) return KSJ_GPU_ERROR_CUDA;
+  ColsPass cols_pass;
+  if (!cols_pass.setup(s, inter, &c)) return KSJ_GPU_ERROR_CUDA;
   for (int f0 = 0; f0 < g; f0 += s.frames_per_pass) {
     const int nf = std::min(s.frames_per_pass, g - f0);
     r.frame0 = f0;
     c.frame0 = f0;
     rows_launch.launch(r, g, (s.channels + s.coil_group - 1) / s.coil_group, nf, stream);
-    {
-      LaunchScope scope("k_cols", stream);
-      cols_kernel<<<dim3((n + s.column_block - 1) / s.column_block, nf), kColsThreads, cols_smem, stream>>>(map, c);
-    }
+    cols_pass.launch(c, nf, stream, "k_cols");
   }
   // z: the column pass over [plane][pixel][cpitch] with planes as rows and pixels as columns
   Shape z = s;
   z.frames = 1;
   z.out_cols = n * n;
-  CUtensorMap zmap;
   ColsArgs cz = c;
-  if (!make_inter_map(z, inter2, &zmap, &cz.box_rows, &cz.boxes)) return KSJ_GPU_ERROR_CUDA;
   cz.frame0 = 0;
   cz.frames = 1;
   cz.out_cols = n * n;
@@ -2551,10 +2763,9 @@ ksj_gpu_status launch_all3(const Shape& s, const Layout3& l, const ksj_gpu_gridd
   cz.output = d->output;
   cz.out = d_out;
   cz.out_pitch = s.channels;
-  {
-    LaunchScope scope("k_cols_z", stream);
-    cols_kernel<<<dim3((n * n + s.column_block - 1) / s.column_block, 1), kColsThreads, cols_smem, stream>>>(zmap, cz);
-  }
+  ColsPass z_pass;
+  if (!z_pass.setup(z, inter2, &cz)) return KSJ_GPU_ERROR_CUDA;
+  z_pass.launch(cz, 1, stream, "k_cols_z");
   return check_launch();
 }
 
@@ -3403,15 +3614,8 @@ extern "C" ksj_gpu_status ksj_gpu_cartesian_ifft2(uint32_t rows, uint32_t cols, 
   c.out = d_out;
   c.out_pitch = s.channels;
   c.frame0 = 0;
-  CUtensorMap map;
-  if (!make_inter_map(s, inter, &map, &c.box_rows, &c.boxes)) return KSJ_GPU_ERROR_CUDA;
-  const size_t cols_smem = cols_smem_bytes(s);
-  const ColsKernel cols_kernel = cols_kernel_for(s.grid_rows);
-  if (!cols_kernel_setup(cols_kernel, cols_smem)) return KSJ_GPU_ERROR_CUDA;
-  {
-    LaunchScope scope("k_cols", cstream);
-    cols_kernel<<<dim3((s.out_cols + s.column_block - 1) / s.column_block, s.frames), kColsThreads, cols_smem, cstream>>>(
-        map, c);
-  }
+  ColsPass cols_pass;
+  if (!cols_pass.setup(s, inter, &c)) return KSJ_GPU_ERROR_CUDA;
+  cols_pass.launch(c, s.frames, cstream, "k_cols");
   return check_launch();
 }
