@@ -418,8 +418,10 @@ def run_ours(args) -> dict | None:
     if args.tuning:
         # a fixed tuning (coil_group, column_block, frames_per_pass, rows_blocks_per_sm, coil_parts), e.g. to
         # profile the kernels the autotuner picks in a plain run (its candidate timings are not valid under ncu)
-        cg, cb, fpp, rb, parts = (int(v) for v in args.tuning.split(","))
-        tuning = gpu.GriddingTuning(ctypes.sizeof(gpu.GriddingTuning), cg, cb, 0, fpp, rb, parts)
+        vals = [int(v) for v in args.tuning.split(",")]
+        cg, cb, fpp, rb, parts = vals[:5]
+        colp = vals[5] if len(vals) > 5 else 0
+        tuning = gpu.GriddingTuning(ctypes.sizeof(gpu.GriddingTuning), cg, cb, 0, fpp, rb, parts, colp)
     else:
         tuning = g.tune(k, t, out, ws)
     for _ in range(args.warmup):
@@ -490,7 +492,8 @@ def run_ours(args) -> dict | None:
     # pass, so no two of its launches overlap and each launch's events time it alone
     # (the tuned call may run two passes concurrently on two streams)
     tuning_k = gpu.GriddingTuning(ctypes.sizeof(gpu.GriddingTuning), tuning.coil_group, tuning.column_block,
-                                  tuning.list_capacity, 0, tuning.rows_blocks_per_sm, tuning.coil_parts)
+                                  tuning.list_capacity, 0, tuning.rows_blocks_per_sm, tuning.coil_parts,
+                                  tuning.column_pass)
     for _ in range(2):
         g.run(k, t, out, ws, tuning=tuning_k)
     torch.cuda.synchronize()
@@ -556,6 +559,19 @@ def run_ours(args) -> dict | None:
         if not args.skip_extra:
             width6 = width6_leg("", k, t, traj_h, ksp_h, dev, args.steps, args.warmup)
             dropin = dropin_leg(args.steps, args.warmup)
+    served = None
+    if rank == 0 and not args.skip_extra:
+        del ws
+        torch.cuda.empty_cache()
+        srv = run_serve(args, n=64)
+        served = {k2: srv[k2] for k2 in ("value", "serial_value", "vs_serial", "p50_ms", "p99_ms", "serial_p50_ms",
+                                         "serial_p99_ms", "poisson_rate_per_s")}
+        served.update({"unit": "samples/s", "requests": srv["config"]["requests"],
+                       "batches": srv["results"]["served"]["burst"]["batches"],
+                       "workload": srv["config"]["workload"], "serial": srv["config"]["serial"],
+                       "served": srv["config"]["served"],
+                       "note": "value = burst throughput of the served loop; p50/p99 under Poisson arrivals at 90 % "
+                               "of the serial path's burst throughput; bench.py --serve runs 160 requests"})
 
     ms, e2e_ms = max_over_ranks(dist, ms, e2e_ms)
     if rank != 0:
@@ -604,7 +620,9 @@ def run_ours(args) -> dict | None:
                                    "tuning": {"coil_group": tuning.coil_group, "column_block": tuning.column_block,
                                               "frames_per_pass": tuning.frames_per_pass or FRAMES,
                                               "rows_blocks_per_sm": tuning.rows_blocks_per_sm,
-                                              "coil_parts": tuning.coil_parts or 1},
+                                              "coil_parts": tuning.coil_parts or 1,
+                                              "column_pass": "persistent ring" if tuning.column_pass == 2
+                                              else "one CTA per column"},
                                    "gridded_samples_per_step_per_gpu": per_step}),
         "e2e": {"value": e2e, "unit": "samples/s", "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": int(ksp_h.nbytes + traj_h.nbytes), "d2h_bytes_per_step": int(out.numel() * 4)},
@@ -619,6 +637,7 @@ def run_ours(args) -> dict | None:
         "reference_cpu_linear": cpu_linear,
         "width6": width6,
         "dropin": dropin,
+        "serve": served,
     }
 
 
@@ -701,39 +720,52 @@ def serve_pass(server, reqs, arrivals=None) -> dict:
     return st
 
 
-def run_serve(args) -> dict:
+def run_serve(args, n: int | None = None) -> dict:
+    """The served stream: `n` requests through the request loop, once as the
+    plain serial GPU path (one slot, batches of one request: each request is
+    its own one-frame call) and once served (slots, ragged batches of up to
+    --serve-batch requests), each as a burst (all submitted at once) and as
+    Poisson arrivals at 90 % of the serial path's burst throughput."""
     import torch
     from kspacejet_gb300 import serve
 
     torch.cuda.init()
-    n = args.serve_requests
+    n = n or args.serve_requests
     reqs, _base = serve_workload(n, seed=11)
     warm, _ = serve_workload(8, seed=12)
     samples = sum(r.kspace.size for r in reqs)
+    modes = (("serial", 1, 1), ("served", args.serve_slots, args.serve_batch))
     out = {"metric": "served gridded samples/s", "unit": "samples/s", "higher_is_better": True, "n_gpus": 1,
            "data": "synthetic", "dtype": "f32 (complex64 samples, float32 gridding/FFT)",
            "config": {"workload": "served stream of 2D radial slices (KB W=4, sigma=2, ramp DCF, RSS)",
                       "requests": n, "readout": list(SERVE_READOUTS), "spokes": [64, 805], "coils": [8, 32],
                       "gridded_samples": samples, "inputs": "pinned host memory, results to pinned host memory",
-                      "slots": args.serve_slots}}
+                      "serial": "1 slot, 1 request per call", "served": f"{args.serve_slots} slots, ragged batches "
+                                                                        f"of up to {args.serve_batch} requests",
+                      "device_memory_cap_gib": args.serve_cap_gib}}
     results = {}
-    for name, slots in (("serial", 1), ("served", args.serve_slots)):
-        with serve.Server(slots=slots, device_memory_cap=args.serve_cap_gib << 30) as s:
+    for name, slots, batch in modes:
+        with serve.Server(slots=slots, device_memory_cap=args.serve_cap_gib << 30, max_batch_frames=batch) as s:
             serve_pass(s, warm)
             serve_pass(s, reqs)  # first pass uploads and caches the trajectories
-            burst = serve_pass(s, reqs)
-            results[name] = {"burst": burst}
+            results[name] = {"burst": serve_pass(s, reqs)}
     # Poisson arrivals at 90% of the serial path's burst throughput
     rate = 0.9 * n / results["serial"]["burst"]["wall_seconds"]
     rng = np.random.default_rng(13)
     arrivals = np.cumsum(rng.exponential(1.0 / rate, size=n))
-    for name, slots in (("serial", 1), ("served", args.serve_slots)):
-        with serve.Server(slots=slots, device_memory_cap=args.serve_cap_gib << 30) as s:
+    for name, slots, batch in modes:
+        with serve.Server(slots=slots, device_memory_cap=args.serve_cap_gib << 30, max_batch_frames=batch) as s:
             serve_pass(s, warm)
             serve_pass(s, reqs)
             results[name]["poisson"] = serve_pass(s, reqs, arrivals)
-    out["value"] = results["served"]["burst"]["samples_per_s"]
-    out["serial_value"] = results["serial"]["burst"]["samples_per_s"]
+    ser, srv = results["serial"], results["served"]
+    out["value"] = srv["burst"]["samples_per_s"]
+    out["serial_value"] = ser["burst"]["samples_per_s"]
+    out["vs_serial"] = out["value"] / out["serial_value"]
+    out["p50_ms"] = srv["poisson"]["latency_p50_ms"]
+    out["p99_ms"] = srv["poisson"]["latency_p99_ms"]
+    out["serial_p50_ms"] = ser["poisson"]["latency_p50_ms"]
+    out["serial_p99_ms"] = ser["poisson"]["latency_p99_ms"]
     out["poisson_rate_per_s"] = rate
     out["results"] = results
     return out
@@ -949,15 +981,17 @@ def main() -> int:
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--frames", type=int, default=FRAMES,
                     help="frames per call (default: the 96-frame workload; fewer only for small profiling cases)")
-    ap.add_argument("--tuning", default="", help="fixed gridding tuning cg,cb,fpp,rb,parts instead of the autotuner")
+    ap.add_argument("--tuning", default="",
+                    help="fixed gridding tuning cg,cb,fpp,rb,parts[,column_pass] instead of the autotuner")
     ap.add_argument("--serve", action="store_true", help="served-stream benchmark (separate JSON line)")
     ap.add_argument("--rows", action="store_true", help="the other hot-path rows (one JSON line each)")
     ap.add_argument("--spokes3", type=int, default=40000, help="--rows: spokes of the 3-D kooshball (0 skips it)")
     ap.add_argument("--skip-extra", action="store_true",
                     help="skip the width-6 and drop-in legs (small profiling runs)")
     ap.add_argument("--serve-requests", type=int, default=160)
-    ap.add_argument("--serve-slots", type=int, default=4)
-    ap.add_argument("--serve-cap-gib", type=int, default=24)
+    ap.add_argument("--serve-slots", type=int, default=2)
+    ap.add_argument("--serve-batch", type=int, default=32, help="requests per ragged batch of the served path")
+    ap.add_argument("--serve-cap-gib", type=int, default=64)
     args = ap.parse_args()
     FRAMES = args.frames
     if args.warmup < 3 and args.impl == "ours":

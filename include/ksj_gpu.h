@@ -112,6 +112,8 @@ typedef struct ksj_gpu_gridding_tuning {
   uint32_t frames_per_pass; /* frames per row/column pass (the row-transformed grid of one pass stays in L2) */
   uint32_t rows_blocks_per_sm; /* 1 or 2 resident row CTAs per SM (2 caps registers at 80 per thread) */
   uint32_t coil_parts;      /* 1 or 2: a row CTA's coil group is split into this many independent list tasks */
+  uint32_t column_pass;     /* 0 heuristic, 1 one CTA per (frame, column block), 2 persistent CTAs with a
+                                two-stage TMA ring of 16-line tiles (two-step column lengths only) */
   uint32_t wait_fault_polls; /* tests only; 0 in normal use.  Nonzero: every later segment of a long binning
                                 list waits for a count that never comes and gives up after this many polls,
                                 raising KSJ_GPU_FLAG_WAIT_TIMEOUT (the output is then invalid): exercises the
@@ -135,6 +137,26 @@ KSJ_GPU_API ksj_gpu_status ksj_gpu_gridding_adjoint(const ksj_gpu_gridding_desc*
                                                     const ksj_gpu_gridding_tuning* tuning, const void* d_kspace,
                                                     const float* d_traj, const float* d_dcf, void* d_out,
                                                     void* d_workspace, size_t workspace_bytes, void* stream);
+
+/* A ragged batch: frames of different coil and sample counts (and the same
+ * grid, image, kernel and DCF mode) in one call.  desc->channels and
+ * desc->samples are the maxima and give the layouts' pitches: d_kspace
+ * [frame][desc->channels][desc->samples], d_traj [frame][desc->samples][2],
+ * d_out as for ksj_gpu_gridding_adjoint.  d_frame_channels[f] (1..channels)
+ * and d_frame_samples[f] (1..samples), device arrays of `frames` entries,
+ * give frame f's coils and samples; the padding of the k-space and of the
+ * trajectory is never read.  Frame f's output equals that of
+ * ksj_gpu_gridding_adjoint on the frame alone with its own coil and sample
+ * counts, byte for byte (coil outputs: its first d_frame_channels[f] coils,
+ * the others zero).  Kaiser-Bessel only.  Workspace:
+ * ksj_gpu_gridding_workspace_bytes(desc).  No counterpart in the reference
+ * (the batching behind the request loop of ksj_serve.h). */
+KSJ_GPU_API ksj_gpu_status ksj_gpu_gridding_adjoint_ragged(const ksj_gpu_gridding_desc* desc,
+                                                           const ksj_gpu_gridding_tuning* tuning,
+                                                           const uint32_t* d_frame_channels,
+                                                           const uint32_t* d_frame_samples, const void* d_kspace,
+                                                           const float* d_traj, const float* d_dcf, void* d_out,
+                                                           void* d_workspace, size_t workspace_bytes, void* stream);
 
 /* The same reconstruction from and to host memory: h_kspace, h_traj, h_dcf
  * and h_out have the layouts of the device form above and should be pinned
@@ -167,6 +189,13 @@ KSJ_GPU_API ksj_gpu_status ksj_gpu_gridding_binning(const ksj_gpu_gridding_desc*
                                                     uint32_t* out_chunk_width, uint64_t* out_list_count,
                                                     uint64_t* out_entry_count, uint64_t* out_offsets,
                                                     uint32_t* out_samples);
+
+/* Byte offset in the workspace of `desc`'s call of `frames` 32-bit words:
+ * frame f's own KSJ_GPU_FLAG_* bits (non-finite sample, bad trajectory, bad
+ * DCF) of the last ksj_gpu_gridding_adjoint / _ragged call that used the
+ * workspace, for callers that batch independent requests into one call and
+ * must fail only the offending one.  0 on a bad desc. */
+KSJ_GPU_API size_t ksj_gpu_gridding_frame_flags_offset(const ksj_gpu_gridding_desc* desc);
 
 /* Device-side check flags (KSJ_GPU_FLAG_*) of the last call that used
  * `d_workspace`.  Synchronises `stream`. */

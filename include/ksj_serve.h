@@ -1,21 +1,30 @@
 /*
- * ksj_serve.h -- a device-resident request loop for slice reconstructions of
- * uneven shape (readout, spokes, coils) arriving over time.
+ * ksj_serve.h -- a host-scheduled request loop with continuous batching for
+ * slice reconstructions of uneven shape (readout, spokes, coils) arriving
+ * over time, on one GPU.
  *
- * Requests are admitted in arrival order as soon as a slot (one CUDA stream
- * with its own grow-only device workspace) is free and the device bytes held
- * by admitted requests stay within the configured cap; admitted requests run
- * concurrently on their streams, so a request that arrives while others are
- * on the GPU starts as soon as capacity frees up (continuous batching, not a
- * queue in front of one GPU job).  Trajectories submitted with an id stay
- * resident on the device and are reused.  Per-request caps mirror the
- * reference's target envelope (config/target-envelope.json: max_frame_bytes,
- * max_image_bytes, max_channels_per_acquisition); the device cap plays the
- * role of the machine policy's memory limit for device bytes.
+ * A scheduler thread keeps up to `slots` batches in flight, each on its own
+ * CUDA stream with grow-only device buffers.  Whenever a slot is free, the
+ * oldest pending request opens a batch and the later pending requests of its
+ * class (grid, image, kernel width, DCF mode, output form) join it in
+ * arrival order, up to max_batch_frames requests and as long as the device
+ * bytes of everything in flight stay within the configured cap.  A batch is
+ * ONE ragged multi-frame reconstruction (ksj_gpu_gridding_adjoint_ragged:
+ * every request a frame with its own coil and sample counts), so small
+ * requests share one launch chain instead of paying for their own.  Requests
+ * that arrive while batches are on the GPU are admitted as slots and memory
+ * free up; batches on different slots overlap on the device.  Trajectories
+ * submitted with an id stay resident on the device and are reused.
+ * Per-request caps mirror the reference's target envelope
+ * (config/target-envelope.json: max_frame_bytes, max_image_bytes,
+ * max_channels_per_acquisition); the device cap plays the role of the machine
+ * policy's memory limit for device bytes.
  *
- * Each request is one ksj_gpu_gridding_adjoint call (Kaiser-Bessel, frames = 1)
- * whose result is byte-identical to the same call made alone: the kernels are
- * deterministic and requests share no device state but cached trajectories.
+ * Each result is byte-identical to the same ksj_gpu_gridding_adjoint call
+ * (Kaiser-Bessel, frames = 1) made alone: a ragged call's frames are
+ * independent and each equals its one-frame call.  A request whose own
+ * samples or trajectory fail the device checks fails alone.
+ * max_batch_frames = 1 with slots = 1 is the plain one-request-at-a-time path.
  *
  * No counterpart in the reference (its executor is synchronous,
  * max_in_flight = 1: libs/recon/kspacejet-recon-runtime/src/synchronous_firing_lease.cpp).
@@ -36,11 +45,13 @@ typedef struct ksj_serve ksj_serve;
 typedef struct ksj_serve_config {
   uint32_t struct_size;
   int32_t device;
-  uint32_t slots;              /* requests in flight on the device, >= 1 (1 = the serial path) */
+  uint32_t slots;              /* batches in flight on the device, >= 1 (1 with max_batch_frames 1: the serial path) */
   uint32_t max_channels;       /* per request (target envelope: 32) */
   uint64_t device_memory_cap;  /* bytes of device memory admitted requests may hold */
   uint64_t max_frame_bytes;    /* per-request k-space bytes (target envelope: 256 MiB) */
   uint64_t max_image_bytes;    /* per-request output bytes (target envelope: 128 MiB) */
+  uint32_t max_batch_frames;   /* requests per batch (one ragged call); 0 = 32, 1 = no batching */
+  uint32_t reserved0;
 } ksj_serve_config;
 
 #define KSJ_SERVE_OUTPUT_RSS 1u         /* float32 [image][image] */
@@ -72,8 +83,10 @@ typedef struct ksj_serve_stats {
   double latency_p99_ms;
   double latency_max_ms;
   uint64_t peak_device_bytes; /* high-water mark of admitted request bytes */
-  uint32_t peak_in_flight;
+  uint32_t peak_in_flight;    /* most requests on the device at once (over all batches) */
   uint32_t reserved0;
+  uint64_t batches;           /* ragged calls launched */
+  uint64_t batched_frames;    /* requests those calls carried */
 } ksj_serve_stats;
 
 KSJ_GPU_API ksj_gpu_status ksj_serve_create(const ksj_serve_config* config, ksj_serve** out);

@@ -118,12 +118,16 @@ struct Shape {
   float phase_row, phase_col, phase_sign;  // origin-phase coefficients
   int coil_group, column_block, list_capacity, frames_per_pass, rows_blocks, coil_parts;
   uint32_t wait_fault;  // tests only: segment waits that cannot succeed, given up after this many polls
+  int column_pass;      // 1 one CTA per tile (k_cols), 2 persistent ring (k_cols_ring)
   DifPlan plan_rows, plan_cols;
+  // ragged batches (device arrays, null otherwise): valid coils and samples of each frame
+  const uint32_t* frame_channels = nullptr;
+  const uint32_t* frame_samples = nullptr;
 };
 
 struct Layout {
-  size_t flags, records, counts, cursor, offsets, entries, expanded, long_lists, samples_t, inter, coil_last, tables,
-      total;
+  size_t flags, frame_flags, records, counts, cursor, offsets, entries, expanded, long_lists, samples_t, inter,
+      coil_last, tables, total;
 };
 
 size_t record_bytes(int width) {
@@ -267,6 +271,9 @@ ksj_gpu_status make_shape(const ksj_gpu_gridding_desc* d, const ksj_gpu_gridding
   if ((parts != 1 && parts != 2) || parts > cg) return KSJ_GPU_ERROR_INVALID_ARGUMENT;
   s->coil_parts = parts;
   s->wait_fault = has(offsetof(ksj_gpu_gridding_tuning, wait_fault_polls) + 4) ? t->wait_fault_polls : 0u;
+  int cp = has(offsetof(ksj_gpu_gridding_tuning, column_pass) + 4) ? static_cast<int>(t->column_pass) : 0;
+  if (cp < 0 || cp > 2) return KSJ_GPU_ERROR_INVALID_ARGUMENT;
+  s->column_pass = cp == 0 ? 1 : cp;  // one CTA per tile unless asked (measured faster on the 384 grid)
   return KSJ_GPU_OK;
 }
 
@@ -283,6 +290,7 @@ Layout make_layout(const Shape& s, const ksj_gpu_gridding_desc* d) {
   const size_t fm = static_cast<size_t>(s.frames) * s.samples;
   const size_t nl = static_cast<size_t>(s.frames) * s.lists_per_frame;
   l.flags = take(kFlagBytes);
+  l.frame_flags = take(static_cast<size_t>(s.frames) * 4);
   l.records = take(fm * record_bytes(s.width));
   l.counts = take(nl * 4);
   l.cursor = take(nl * 4);
@@ -339,6 +347,8 @@ __global__ void __launch_bounds__(256) k_fill(float* p, int n, float v) {
 struct PrepareArgs {
   const float* traj;
   const float* dcf;
+  const uint32_t* frame_samples;  // ragged batches: valid samples of each frame (null: all)
+  uint32_t* frame_flags;          // per-frame copy of the check flags (null: none)
   uint32_t dcf_mode;
   uint32_t require_nyquist;
   unsigned char* records;
@@ -363,6 +373,12 @@ __global__ void __launch_bounds__(256) k_prepare(PrepareArgs a) {
   const size_t total = static_cast<size_t>(a.frames) * a.samples;
   if (idx >= total) return;
   const int f = static_cast<int>(idx / a.samples);
+  if (a.frame_samples != nullptr &&
+      idx - static_cast<size_t>(f) * a.samples >= static_cast<size_t>(__ldg(a.frame_samples + f))) {
+    // a padding sample of a ragged batch: in no list (its trajectory is not read)
+    reinterpret_cast<SampleRecord<W>*>(a.records)[idx].r0 = -1;
+    return;
+  }
   const float2 k = __ldg(reinterpret_cast<const float2*>(a.traj) + idx);
   bool ok = isfinite(k.x) && isfinite(k.y);
   if (ok && a.require_nyquist) ok = k.x >= -kPiF && k.x <= kPiF && k.y >= -kPiF && k.y <= kPiF;
@@ -375,12 +391,14 @@ __global__ void __launch_bounds__(256) k_prepare(PrepareArgs a) {
     w = __ldg(a.dcf + idx);
     if (!(isfinite(w) && w >= 0.0f)) {
       atomicOr(a.flags, KSJ_GPU_FLAG_BAD_DCF);
+      if (a.frame_flags) atomicOr(a.frame_flags + f, KSJ_GPU_FLAG_BAD_DCF);
       w = 0.0f;
     }
   }
   SampleRecord<W> rec;
   if (!ok) {
     atomicOr(a.flags, KSJ_GPU_FLAG_BAD_TRAJECTORY);
+    if (a.frame_flags) atomicOr(a.frame_flags + f, KSJ_GPU_FLAG_BAD_TRAJECTORY);
     rec.r0 = 0;
     rec.c0 = 0;
     rec.scale = make_float2(0.0f, 0.0f);
@@ -486,7 +504,9 @@ __global__ void __launch_bounds__(256) k_scatter(const unsigned char* records, c
   const int f = static_cast<int>(idx / samples);
   const int s = static_cast<int>(idx - static_cast<size_t>(f) * samples);
   const SampleRecord<W>* rec = reinterpret_cast<const SampleRecord<W>*>(records) + idx;
-  const int r0 = rec->r0, c0 = rec->c0;
+  const int r0 = rec->r0;
+  if (r0 < 0) return;  // padding sample of a ragged batch
+  const int c0 = rec->c0;
   int k0, k1;
   list_chunks<W>(c0, grid_cols, &k0, &k1);
   const int lists = grid_rows * nchunks;
@@ -901,9 +921,16 @@ ksj_gpu_status launch_sort(SortArgs sa, size_t lists, size_t entries_total, int 
 // ceil(channels/32), frames)), checking every sample on the way: a
 // non-finite value (either component; bf16 exponent all ones) raises
 // KSJ_GPU_FLAG_NONFINITE_SAMPLE.
+//
+// Ragged batches (frame_channels / frame_samples non-null): frame f holds
+// frame_channels[f] coils of frame_samples[f] samples in the [channel][sample]
+// pitch of the call; the padding is not read and is written as zeros.
 template <uint32_t kFormat>
 __global__ void __launch_bounds__(256) k_samples_coil_last(const void* in_raw, void* out_raw, int channels,
-                                                           int samples, uint32_t* flags) {
+                                                           int samples, uint32_t* flags,
+                                                           const uint32_t* frame_channels,
+                                                           const uint32_t* frame_samples, int frame0,
+                                                           uint32_t* frame_flags) {
   using T = typename std::conditional<kFormat == KSJ_GPU_SAMPLES_BF16, uint32_t, unsigned long long>::type;
   __shared__ T t[32][33];
   const T* in = static_cast<const T*>(in_raw);
@@ -913,10 +940,16 @@ __global__ void __launch_bounds__(256) k_samples_coil_last(const void* in_raw, v
   const int c0 = blockIdx.y * 32;
   const T* src = in + static_cast<size_t>(f) * channels * samples;
   T* dst = out + static_cast<size_t>(f) * channels * samples;
+  const int live_c = frame_channels ? min(channels, static_cast<int>(__ldg(frame_channels + frame0 + f))) : channels;
+  const int live_s = frame_samples ? min(samples, static_cast<int>(__ldg(frame_samples + frame0 + f))) : samples;
   bool bad = false;
   for (int y = threadIdx.y; y < 32; y += blockDim.y) {
     const int c = c0 + y, sm = s0 + threadIdx.x;
     if (c < channels && sm < samples) {
+      if (c >= live_c || sm >= live_s) {
+        t[y][threadIdx.x] = T(0);
+        continue;
+      }
       const T v = src[static_cast<size_t>(c) * samples + sm];
       if (kFormat == KSJ_GPU_SAMPLES_BF16) {
         const uint32_t u = static_cast<uint32_t>(v);
@@ -928,7 +961,10 @@ __global__ void __launch_bounds__(256) k_samples_coil_last(const void* in_raw, v
       t[y][threadIdx.x] = v;
     }
   }
-  if (__syncthreads_or(bad) && threadIdx.x == 0 && threadIdx.y == 0) atomicOr(flags, KSJ_GPU_FLAG_NONFINITE_SAMPLE);
+  if (__syncthreads_or(bad) && threadIdx.x == 0 && threadIdx.y == 0) {
+    atomicOr(flags, KSJ_GPU_FLAG_NONFINITE_SAMPLE);
+    if (frame_flags) atomicOr(frame_flags + frame0 + f, KSJ_GPU_FLAG_NONFINITE_SAMPLE);
+  }
   for (int y = threadIdx.y; y < 32; y += blockDim.y) {
     const int sm = s0 + y, c = c0 + threadIdx.x;
     if (c < channels && sm < samples) dst[static_cast<size_t>(sm) * channels + c] = t[threadIdx.x][y];
@@ -1904,7 +1940,7 @@ struct ColsPass {
     const int tc = std::min(s.col_group, kRingLines);
     const int cb = kRingLines / tc;
     out_cols = s.out_cols;
-    ring = has_two_step_rows(s.grid_rows) && tc >= 2 && cb <= s.out_cols;
+    ring = s.column_pass == 2 && has_two_step_rows(s.grid_rows) && tc >= 2 && cb <= s.out_cols;
     if (!ring) {
       column_block = s.column_block;
       smem = cols_smem_bytes(s);
@@ -1953,7 +1989,7 @@ template <int W>
 ksj_gpu_status build_lists(const Shape& s, const ksj_gpu_gridding_desc* d, const float* d_traj, const float* d_dcf,
                            uint32_t* flags, unsigned char* records, uint32_t* counts, uint32_t* cursor,
                            uint32_t* offsets, uint32_t* entries, float4* expanded, uint32_t* long_lists,
-                           cudaStream_t stream) {
+                           cudaStream_t stream, uint32_t* frame_flags = nullptr) {
   const size_t nl = static_cast<size_t>(s.frames) * s.lists_per_frame;
   if (cudaMemsetAsync(counts, 0, nl * 4, stream) != cudaSuccess) return KSJ_GPU_ERROR_CUDA;
   if (cudaMemsetAsync(cursor, 0, nl * 4, stream) != cudaSuccess) return KSJ_GPU_ERROR_CUDA;
@@ -1962,6 +1998,8 @@ ksj_gpu_status build_lists(const Shape& s, const ksj_gpu_gridding_desc* d, const
     PrepareArgs p{};
     p.traj = d_traj;
     p.dcf = d_dcf;
+    p.frame_samples = s.frame_samples;
+    p.frame_flags = frame_flags;
     p.dcf_mode = d->dcf_mode;
     p.require_nyquist = d->require_nyquist;
     p.records = records;
@@ -2051,7 +2089,9 @@ ksj_gpu_status launch_all(const Shape& s, const Layout& l, const ksj_gpu_griddin
   int* pos_rows = reinterpret_cast<int*>(inv_dc + s.out_cols);
   int* pos_cols = pos_rows + s.out_rows;
 
-  if (cudaMemsetAsync(flags, 0, kFlagBytes, stream) != cudaSuccess) return KSJ_GPU_ERROR_CUDA;
+  if (cudaMemsetAsync(flags, 0, kFlagBytes, stream) != cudaSuccess ||
+      cudaMemsetAsync(ws + l.frame_flags, 0, static_cast<size_t>(s.frames) * 4, stream) != cudaSuccess)
+    return KSJ_GPU_ERROR_CUDA;
   {
     const int n = std::max(std::max(s.grid_rows, s.grid_cols), std::max(s.out_rows, s.out_cols));
     const double beta = s.beta;
@@ -2064,7 +2104,8 @@ ksj_gpu_status launch_all(const Shape& s, const Layout& l, const ksj_gpu_griddin
   {
     const ksj_gpu_status st = build_lists<W>(s, d, d_traj, d_dcf, flags, records, counts, cursor, offsets, entries,
                                              reinterpret_cast<float4*>(ws + l.expanded),
-                                             reinterpret_cast<uint32_t*>(ws + l.long_lists), stream);
+                                             reinterpret_cast<uint32_t*>(ws + l.long_lists), stream,
+                                             reinterpret_cast<uint32_t*>(ws + l.frame_flags));
     if (st != KSJ_GPU_OK) return st;
   }
   const size_t frame_samples = static_cast<size_t>(s.samples) * s.channels;  // elements per frame
@@ -2074,7 +2115,8 @@ ksj_gpu_status launch_all(const Shape& s, const Layout& l, const ksj_gpu_griddin
     LaunchScope scope("k_samples_coil_last", st);
     k_samples_coil_last<kFormat><<<tg, dim3(32, 8), 0, st>>>(
         static_cast<const unsigned char*>(d_kspace) + f0 * frame_samples * eb, ws + l.samples_t + f0 * frame_samples * eb,
-        s.channels, s.samples, flags);
+        s.channels, s.samples, flags, s.frame_channels, s.frame_samples, f0,
+        reinterpret_cast<uint32_t*>(ws + l.frame_flags));
   };
   if (io == nullptr || io->copy == nullptr) to_coil_last(0, s.frames, stream);
   RowsArgs r{};
@@ -2691,7 +2733,7 @@ ksj_gpu_status launch_all3(const Shape& s, const Layout3& l, const ksj_gpu_gridd
     const dim3 tg((s.samples + 31) / 32, (s.channels + 31) / 32, 1);
     LaunchScope scope("k_samples_coil_last", stream);
     k_samples_coil_last<kFormat><<<tg, dim3(32, 8), 0, stream>>>(d_kspace, ws + l.samples_t, s.channels, s.samples,
-                                                                 flags);
+                                                                 flags, nullptr, nullptr, 0, nullptr);
   }
   // rows of every plane (x transformed, kept columns, coil-last)
   RowsArgs r{};
@@ -3196,13 +3238,22 @@ extern "C" size_t ksj_gpu_gridding_workspace_bytes(const ksj_gpu_gridding_desc* 
   return make_layout(s, desc).total;
 }
 
-extern "C" ksj_gpu_status ksj_gpu_gridding_adjoint(const ksj_gpu_gridding_desc* desc,
-                                                   const ksj_gpu_gridding_tuning* tuning, const void* d_kspace,
-                                                   const float* d_traj, const float* d_dcf, void* d_out,
-                                                   void* d_workspace, size_t workspace_bytes, void* stream) {
+extern "C" size_t ksj_gpu_gridding_frame_flags_offset(const ksj_gpu_gridding_desc* desc) {
+  Shape s{};
+  if (make_shape(desc, nullptr, &s) != KSJ_GPU_OK) return 0;
+  return make_layout(s, desc).frame_flags;
+}
+
+namespace {
+ksj_gpu_status gridding_adjoint(const ksj_gpu_gridding_desc* desc, const ksj_gpu_gridding_tuning* tuning,
+                                const uint32_t* d_frame_channels, const uint32_t* d_frame_samples,
+                                const void* d_kspace, const float* d_traj, const float* d_dcf, void* d_out,
+                                void* d_workspace, size_t workspace_bytes, void* stream) {
   Shape s{};
   const ksj_gpu_status st = make_shape(desc, tuning, &s);
   if (st != KSJ_GPU_OK) return st;
+  s.frame_channels = d_frame_channels;
+  s.frame_samples = d_frame_samples;
   if (d_kspace == nullptr || d_traj == nullptr || d_out == nullptr) return KSJ_GPU_ERROR_INVALID_ARGUMENT;
   if (desc->dcf_mode == KSJ_GPU_DCF_EXTERNAL && d_dcf == nullptr) return KSJ_GPU_ERROR_INVALID_ARGUMENT;
   const Layout l = make_layout(s, desc);
@@ -3229,6 +3280,28 @@ extern "C" ksj_gpu_status ksj_gpu_gridding_adjoint(const ksj_gpu_gridding_desc* 
   cudaEventDestroy(ready);
   cudaEventDestroy(alt_done);
   return result;
+}
+}  // namespace
+
+extern "C" ksj_gpu_status ksj_gpu_gridding_adjoint(const ksj_gpu_gridding_desc* desc,
+                                                   const ksj_gpu_gridding_tuning* tuning, const void* d_kspace,
+                                                   const float* d_traj, const float* d_dcf, void* d_out,
+                                                   void* d_workspace, size_t workspace_bytes, void* stream) {
+  return gridding_adjoint(desc, tuning, nullptr, nullptr, d_kspace, d_traj, d_dcf, d_out, d_workspace,
+                          workspace_bytes, stream);
+}
+
+extern "C" ksj_gpu_status ksj_gpu_gridding_adjoint_ragged(const ksj_gpu_gridding_desc* desc,
+                                                          const ksj_gpu_gridding_tuning* tuning,
+                                                          const uint32_t* d_frame_channels,
+                                                          const uint32_t* d_frame_samples, const void* d_kspace,
+                                                          const float* d_traj, const float* d_dcf, void* d_out,
+                                                          void* d_workspace, size_t workspace_bytes, void* stream) {
+  if (d_frame_channels == nullptr || d_frame_samples == nullptr) return KSJ_GPU_ERROR_INVALID_ARGUMENT;
+  if (desc == nullptr || desc->struct_size < sizeof(ksj_gpu_gridding_desc) || desc->kernel != KSJ_GPU_KERNEL_KAISER_BESSEL)
+    return KSJ_GPU_ERROR_INVALID_ARGUMENT;
+  return gridding_adjoint(desc, tuning, d_frame_channels, d_frame_samples, d_kspace, d_traj, d_dcf, d_out,
+                          d_workspace, workspace_bytes, stream);
 }
 
 extern "C" size_t ksj_gpu_gridding_host_workspace_bytes(const ksj_gpu_gridding_desc* desc) {
@@ -3396,6 +3469,7 @@ extern "C" ksj_gpu_status ksj_gpu_gridding_tune(const ksj_gpu_gridding_desc* des
     for (uint32_t cbm : {1u, 2u})
     for (uint32_t fpp : {0u, 12u, 48u})
     for (uint32_t rb : {1u, 2u})
+    for (uint32_t colp : {1u, 2u})
     for (uint32_t parts : {1u, 2u}) {
       if (fpp >= desc->frames) continue;
       if (parts > 1 && cg < 16) continue;
@@ -3408,6 +3482,7 @@ extern "C" ksj_gpu_status ksj_gpu_gridding_tune(const ksj_gpu_gridding_desc* des
       t.frames_per_pass = fpp;
       t.rows_blocks_per_sm = rb;
       t.coil_parts = parts;
+      t.column_pass = colp;
       Shape s{};
       if (make_shape(desc, &t, &s) != KSJ_GPU_OK) continue;
       if (workspace_bytes < make_layout(s, desc).total) continue;

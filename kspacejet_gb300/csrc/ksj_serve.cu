@@ -1,16 +1,27 @@
 // ksj_serve.cu -- the request loop behind include/ksj_serve.h (host code).
 //
 // One scheduler thread owns every CUDA object.  Its loop:
-//   1. admit: while the oldest pending request fits (a free slot, and the
-//      device bytes of admitted requests plus its own <= the cap), stage its
-//      inputs through the slot's pinned buffer, enqueue copy-in, the
-//      ksj_gpu_gridding_adjoint call and copy-out on the slot's stream, and
-//      record the slot's completion event;
-//   2. retire: every slot whose event has completed copies its result to the
-//      caller's buffer, records the latency and frees its bytes and slot;
-//   3. otherwise sleep briefly on the submit condition variable.
-// Slots keep their device workspace, input, output and pinned staging
-// buffers between requests (grow-only), so steady state allocates nothing.
+//   1. retire: every slot whose completion event has fired hands each request
+//      of its batch its result (copied from staging when the caller's buffer
+//      is pageable) and its own check flags, records the latency and frees
+//      the slot and its bytes;
+//   2. admit: while a slot is free, the oldest pending request opens a batch
+//      and the pending requests of the same class (grid, image, kernel width,
+//      DCF mode, output form) join it in arrival order, up to the batch's
+//      frame limit and as long as the device bytes of everything in flight
+//      stay within the cap; the batch is copied in (each request's k-space
+//      into its frame of a padded [frame][channel][sample] block, cached
+//      trajectories device to device), reconstructed by ONE ragged call
+//      (ksj_gpu_gridding_adjoint_ragged: per-frame coil and sample counts,
+//      padding never read) and copied out, all on the slot's stream;
+//   3. otherwise wait briefly on the submit condition variable.
+// Requests that arrive while batches are on the GPU queue up and leave in
+// the next batch of their class as soon as a slot frees (continuous
+// batching); several slots keep several batches in flight.  Slots keep
+// their device and pinned buffers between batches (grow-only), so steady
+// state allocates nothing.  A request's frame of a ragged call is
+// byte-identical to the same reconstruction made alone, so a result does
+// not depend on its batch-mates.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -21,6 +32,7 @@
 #include <mutex>
 #include <new>
 #include <thread>
+#include <tuple>
 #include <unordered_map>
 #include <vector>
 
@@ -31,11 +43,13 @@ namespace {
 
 using Clock = std::chrono::steady_clock;
 
+constexpr uint32_t kDefaultBatchFrames = 32;
+
 struct Ticket {
   uint64_t id = 0;
   ksj_serve_request req{};
   Clock::time_point submitted;
-  uint64_t bytes = 0;
+  uint64_t bytes = 0;  // device bytes of this request alone (admission of a single request)
   ksj_gpu_status result = KSJ_GPU_OK;
   bool done = false;
 };
@@ -48,9 +62,12 @@ struct Buffer {
 struct Slot {
   cudaStream_t stream = nullptr;
   cudaEvent_t done = nullptr;
-  Buffer kspace, traj, out, workspace;  // device
-  Buffer pin_in, pin_out;               // pinned host staging
-  Ticket* busy = nullptr;
+  Buffer kspace, traj, out, workspace, counts;  // device
+  Buffer pin_in, pin_out, pin_meta;             // pinned host: pageable inputs, pageable outputs, counts + flags
+  std::vector<Ticket*> batch;                    // in frame order; empty = free
+  std::vector<size_t> out_staged;                // per request: offset in pin_out, or SIZE_MAX (direct)
+  uint64_t bytes = 0;
+  uint32_t frames = 0;
 };
 
 struct Trajectory {
@@ -85,7 +102,13 @@ bool ensure_pinned(Buffer& b, size_t bytes) {
   return true;
 }
 
-ksj_gpu_gridding_desc make_desc(const ksj_serve_request& r) {
+// Requests of one class share a ragged call.
+using ClassKey = std::tuple<uint32_t, uint32_t, uint32_t, uint32_t, uint32_t>;
+ClassKey class_of(const ksj_serve_request& r) {
+  return {r.grid, r.image, r.kernel_width, r.dcf_mode, r.output};
+}
+
+ksj_gpu_gridding_desc make_desc(const ksj_serve_request& r, uint32_t frames, uint32_t channels, uint32_t samples) {
   ksj_gpu_gridding_desc d{};
   d.struct_size = sizeof(d);
   d.kernel = KSJ_GPU_KERNEL_KAISER_BESSEL;
@@ -93,24 +116,40 @@ ksj_gpu_gridding_desc make_desc(const ksj_serve_request& r) {
   d.grid_rows = d.grid_cols = r.grid;
   d.kernel_width = r.kernel_width;
   d.row_origin = d.col_origin = (r.image - 1) / 2.0;
-  d.channels = r.channels;
-  d.samples = r.samples;
-  d.frames = 1;
+  d.channels = channels;
+  d.samples = samples;
+  d.frames = frames;
   d.dcf_mode = r.dcf_mode;
   d.output = r.output == KSJ_SERVE_OUTPUT_RSS ? KSJ_GPU_OUTPUT_RSS : KSJ_GPU_OUTPUT_COIL_MAJOR;
   d.sample_format = KSJ_GPU_SAMPLES_CF32;
   return d;
 }
 
-size_t out_bytes(const ksj_serve_request& r) {
-  const size_t px = static_cast<size_t>(r.image) * r.image;
-  return r.output == KSJ_SERVE_OUTPUT_RSS ? px * 4 : px * r.channels * 8;
+size_t pixels_of(const ksj_serve_request& r) { return static_cast<size_t>(r.image) * r.image; }
+
+// bytes of one frame of a call's output with `channels` coils
+size_t frame_out_bytes(const ksj_serve_request& r, uint32_t channels) {
+  return r.output == KSJ_SERVE_OUTPUT_RSS ? pixels_of(r) * 4 : pixels_of(r) * channels * 8;
+}
+
+// bytes the caller receives
+size_t out_bytes(const ksj_serve_request& r) { return frame_out_bytes(r, r.channels); }
+
+// Device bytes of a ragged call over `frames` frames of at most `channels`
+// coils and `samples` samples (0 on a bad shape).
+uint64_t batch_bytes(const ksj_serve_request& r, uint32_t frames, uint32_t channels, uint32_t samples) {
+  const ksj_gpu_gridding_desc d = make_desc(r, frames, channels, samples);
+  const size_t ws = ksj_gpu_gridding_workspace_bytes(&d);
+  if (ws == 0) return 0;
+  return ws + uint64_t{frames} * channels * samples * 8 + uint64_t{frames} * samples * 8 +
+         uint64_t{frames} * frame_out_bytes(r, channels) + uint64_t{frames} * 8;
 }
 
 }  // namespace
 
 struct ksj_serve {
   ksj_serve_config cfg{};
+  uint32_t max_batch = kDefaultBatchFrames;
   std::mutex mu;
   std::condition_variable work_cv, done_cv;
   std::deque<Ticket*> pending;
@@ -123,7 +162,7 @@ struct ksj_serve {
   bool init_ok = false;
   std::thread worker;
   // statistics (under mu)
-  uint64_t submitted = 0, completed = 0, rejected = 0, failed = 0, samples_done = 0;
+  uint64_t submitted = 0, completed = 0, rejected = 0, failed = 0, samples_done = 0, batches = 0, batched_frames = 0;
   std::vector<double> latencies_ms;
   Clock::time_point first_submit, last_done;
   bool any_submit = false;
@@ -131,94 +170,154 @@ struct ksj_serve {
   uint32_t peak_in_flight = 0;
 
   void run();
-  bool launch(Slot& slot, Ticket* t);
+  bool launch(Slot& slot, const std::vector<Ticket*>& batch, uint32_t channels, uint32_t samples);
   void retire(Slot& slot);
+  void fail_batch(const std::vector<Ticket*>& batch, ksj_gpu_status status);
 };
 
-bool ksj_serve::launch(Slot& slot, Ticket* t) {
-  const ksj_serve_request& r = t->req;
-  const ksj_gpu_gridding_desc d = make_desc(r);
+bool ksj_serve::launch(Slot& slot, const std::vector<Ticket*>& batch, uint32_t cmax, uint32_t mmax) {
+  const ksj_serve_request& r0 = batch.front()->req;
+  const uint32_t nf = static_cast<uint32_t>(batch.size());
+  const ksj_gpu_gridding_desc d = make_desc(r0, nf, cmax, mmax);
   const size_t ws = ksj_gpu_gridding_workspace_bytes(&d);
-  const size_t kb = static_cast<size_t>(r.channels) * r.samples * 8;
-  const size_t tb = static_cast<size_t>(r.samples) * 8;
-  const size_t ob = out_bytes(r);
-  if (ws == 0 || !ensure_device(slot.kspace, kb) || !ensure_device(slot.out, ob) ||
-      !ensure_device(slot.workspace, ws) ||
-      (!(r.flags & KSJ_SERVE_HOST_PINNED) && !ensure_pinned(slot.pin_in, kb + tb)) ||
-      !ensure_pinned(slot.pin_out, ob + 16))
-    return false;
-  // inputs: pinned callers are copied by DMA directly; pageable ones are
-  // staged through the slot's pinned buffer.  Trajectories with an id stay
-  // resident and later requests wait on their upload event.
-  const bool pinned = (r.flags & KSJ_SERVE_HOST_PINNED) != 0;
-  const void* k_src = r.kspace;
-  const void* t_src = r.trajectory;
-  if (!pinned) {
-    std::memcpy(slot.pin_in.p, r.kspace, kb);
-    k_src = slot.pin_in.p;
-    t_src = static_cast<char*>(slot.pin_in.p) + kb;
-  }
-  if (cudaMemcpyAsync(slot.kspace.p, k_src, kb, cudaMemcpyHostToDevice, slot.stream) != cudaSuccess) return false;
-  const float* d_traj = nullptr;
-  if (r.trajectory_id != 0) {
-    auto it = trajectories.find(r.trajectory_id);
-    if (it == trajectories.end()) {
-      Trajectory tr{};
-      tr.bytes = tb;
-      if (cudaMalloc(&tr.d, tb) != cudaSuccess ||
-          cudaEventCreateWithFlags(&tr.ready, cudaEventDisableTiming) != cudaSuccess) {
-        cudaGetLastError();
-        return false;
-      }
-      if (!pinned) std::memcpy(const_cast<void*>(t_src), r.trajectory, tb);
-      if (cudaMemcpyAsync(tr.d, t_src, tb, cudaMemcpyHostToDevice, slot.stream) != cudaSuccess ||
-          cudaEventRecord(tr.ready, slot.stream) != cudaSuccess)
-        return false;
-      it = trajectories.emplace(r.trajectory_id, tr).first;
-    } else if (it->second.bytes != tb || cudaStreamWaitEvent(slot.stream, it->second.ready, 0) != cudaSuccess) {
-      return false;  // an id names one trajectory: a different sample count is an error
+  const size_t flags_at = ksj_gpu_gridding_frame_flags_offset(&d);
+  const size_t frame_k = size_t{cmax} * mmax * 8;
+  const size_t frame_t = size_t{mmax} * 8;
+  const size_t frame_o = frame_out_bytes(r0, cmax);
+  size_t stage_in = 0, stage_out = 0;
+  for (const Ticket* t : batch) {
+    if (!(t->req.flags & KSJ_SERVE_HOST_PINNED)) {
+      stage_in += size_t{t->req.channels} * t->req.samples * 8 + size_t{t->req.samples} * 8;
+      stage_out += out_bytes(t->req);
     }
-    d_traj = static_cast<const float*>(it->second.d);
-  } else {
-    if (!ensure_device(slot.traj, tb)) return false;
-    if (!pinned) std::memcpy(const_cast<void*>(t_src), r.trajectory, tb);
-    if (cudaMemcpyAsync(slot.traj.p, t_src, tb, cudaMemcpyHostToDevice, slot.stream) != cudaSuccess) return false;
-    d_traj = static_cast<const float*>(slot.traj.p);
   }
-  if (ksj_gpu_gridding_adjoint(&d, nullptr, slot.kspace.p, d_traj, nullptr, slot.out.p, slot.workspace.p,
-                               slot.workspace.cap, slot.stream) != KSJ_GPU_OK)
+  if (ws == 0 || !ensure_device(slot.kspace, nf * frame_k) || !ensure_device(slot.traj, nf * frame_t) ||
+      !ensure_device(slot.out, nf * frame_o) || !ensure_device(slot.workspace, ws) ||
+      !ensure_device(slot.counts, size_t{nf} * 8) || !ensure_pinned(slot.pin_in, stage_in + 16) ||
+      !ensure_pinned(slot.pin_out, stage_out + 16) || !ensure_pinned(slot.pin_meta, size_t{nf} * 12))
     return false;
-  // result, then the device check flags (first word of the workspace) behind it
-  void* out_dst = pinned ? r.out : slot.pin_out.p;
-  if (cudaMemcpyAsync(out_dst, slot.out.p, ob, cudaMemcpyDeviceToHost, slot.stream) != cudaSuccess ||
-      cudaMemcpyAsync(static_cast<char*>(slot.pin_out.p) + ob, slot.workspace.p, 4, cudaMemcpyDeviceToHost,
-                      slot.stream) != cudaSuccess ||
+  // per-frame coil and sample counts, then (after the call) the frame flags
+  uint32_t* meta = static_cast<uint32_t*>(slot.pin_meta.p);
+  for (uint32_t f = 0; f < nf; ++f) {
+    meta[f] = batch[f]->req.channels;
+    meta[nf + f] = batch[f]->req.samples;
+  }
+  if (cudaMemcpyAsync(slot.counts.p, meta, size_t{nf} * 8, cudaMemcpyHostToDevice, slot.stream) != cudaSuccess)
+    return false;
+  char* stage = static_cast<char*>(slot.pin_in.p);
+  for (uint32_t f = 0; f < nf; ++f) {
+    const ksj_serve_request& r = batch[f]->req;
+    const bool pinned = (r.flags & KSJ_SERVE_HOST_PINNED) != 0;
+    const size_t kb = size_t{r.channels} * r.samples * 8, tb = size_t{r.samples} * 8;
+    const void* k_src = r.kspace;
+    const void* t_src = r.trajectory;
+    if (!pinned) {
+      std::memcpy(stage, r.kspace, kb);
+      std::memcpy(stage + kb, r.trajectory, tb);
+      k_src = stage;
+      t_src = stage + kb;
+      stage += kb + tb;
+    }
+    // k-space rows (channels) at the call's sample pitch
+    char* k_dst = static_cast<char*>(slot.kspace.p) + f * frame_k;
+    if (cudaMemcpy2DAsync(k_dst, size_t{mmax} * 8, k_src, size_t{r.samples} * 8, size_t{r.samples} * 8, r.channels,
+                          cudaMemcpyHostToDevice, slot.stream) != cudaSuccess)
+      return false;
+    char* t_dst = static_cast<char*>(slot.traj.p) + f * frame_t;
+    if (r.trajectory_id != 0) {
+      auto it = trajectories.find(r.trajectory_id);
+      if (it == trajectories.end()) {
+        Trajectory tr{};
+        tr.bytes = tb;
+        if (cudaMalloc(&tr.d, tb) != cudaSuccess ||
+            cudaEventCreateWithFlags(&tr.ready, cudaEventDisableTiming) != cudaSuccess) {
+          cudaGetLastError();
+          if (tr.d) cudaFree(tr.d);
+          return false;
+        }
+        if (cudaMemcpyAsync(tr.d, t_src, tb, cudaMemcpyHostToDevice, slot.stream) != cudaSuccess ||
+            cudaEventRecord(tr.ready, slot.stream) != cudaSuccess)
+          return false;
+        it = trajectories.emplace(r.trajectory_id, tr).first;
+      } else if (it->second.bytes != tb || cudaStreamWaitEvent(slot.stream, it->second.ready, 0) != cudaSuccess) {
+        return false;  // an id names one trajectory: a different sample count is an error
+      }
+      if (cudaMemcpyAsync(t_dst, it->second.d, tb, cudaMemcpyDeviceToDevice, slot.stream) != cudaSuccess) return false;
+    } else if (cudaMemcpyAsync(t_dst, t_src, tb, cudaMemcpyHostToDevice, slot.stream) != cudaSuccess) {
+      return false;
+    }
+  }
+  const uint32_t* counts = static_cast<const uint32_t*>(slot.counts.p);
+  if (ksj_gpu_gridding_adjoint_ragged(&d, nullptr, counts, counts + nf, slot.kspace.p,
+                                      static_cast<const float*>(slot.traj.p), nullptr, slot.out.p, slot.workspace.p,
+                                      slot.workspace.cap, slot.stream) != KSJ_GPU_OK)
+    return false;
+  // results (a coil-major frame's first `channels` coils are contiguous),
+  // then every frame's check flags
+  slot.out_staged.assign(nf, SIZE_MAX);
+  char* ostage = static_cast<char*>(slot.pin_out.p);
+  size_t ooff = 0;
+  for (uint32_t f = 0; f < nf; ++f) {
+    const ksj_serve_request& r = batch[f]->req;
+    const size_t ob = out_bytes(r);
+    void* dst = r.out;
+    if (!(r.flags & KSJ_SERVE_HOST_PINNED)) {
+      dst = ostage + ooff;
+      slot.out_staged[f] = ooff;
+      ooff += ob;
+    }
+    if (cudaMemcpyAsync(dst, static_cast<const char*>(slot.out.p) + f * frame_o, ob, cudaMemcpyDeviceToHost,
+                        slot.stream) != cudaSuccess)
+      return false;
+  }
+  if (cudaMemcpyAsync(meta + 2 * nf, static_cast<const char*>(slot.workspace.p) + flags_at, size_t{nf} * 4,
+                      cudaMemcpyDeviceToHost, slot.stream) != cudaSuccess ||
       cudaEventRecord(slot.done, slot.stream) != cudaSuccess)
     return false;
-  slot.busy = t;
+  slot.batch = batch;
+  slot.frames = nf;
   return true;
 }
 
-void ksj_serve::retire(Slot& slot) {
-  Ticket* t = slot.busy;
-  slot.busy = nullptr;
-  uint32_t flags = 0;
-  const size_t ob = out_bytes(t->req);
-  std::memcpy(&flags, static_cast<const char*>(slot.pin_out.p) + ob, sizeof(flags));
-  if (!(t->req.flags & KSJ_SERVE_HOST_PINNED)) std::memcpy(t->req.out, slot.pin_out.p, ob);
-  const auto now = Clock::now();
-  in_flight_bytes -= t->bytes;
+void ksj_serve::fail_batch(const std::vector<Ticket*>& batch, ksj_gpu_status status) {
   std::lock_guard<std::mutex> lock(mu);
-  t->result = flags == 0 ? KSJ_GPU_OK : KSJ_GPU_ERROR_NONFINITE_INPUT;
-  t->done = true;
-  if (t->result == KSJ_GPU_OK) {
-    ++completed;
-    samples_done += static_cast<uint64_t>(t->req.channels) * t->req.samples;
-  } else {
+  for (Ticket* t : batch) {
+    t->result = status;
+    t->done = true;
     ++failed;
   }
-  latencies_ms.push_back(std::chrono::duration<double, std::milli>(now - t->submitted).count());
+  done_cv.notify_all();
+}
+
+void ksj_serve::retire(Slot& slot) {
+  const uint32_t nf = slot.frames;
+  const uint32_t* meta = static_cast<const uint32_t*>(slot.pin_meta.p);
+  const auto now = Clock::now();
+  for (uint32_t f = 0; f < nf; ++f) {
+    Ticket* t = slot.batch[f];
+    if (slot.out_staged[f] != SIZE_MAX)
+      std::memcpy(t->req.out, static_cast<const char*>(slot.pin_out.p) + slot.out_staged[f], out_bytes(t->req));
+  }
+  in_flight_bytes -= slot.bytes;
+  std::lock_guard<std::mutex> lock(mu);
+  for (uint32_t f = 0; f < nf; ++f) {
+    Ticket* t = slot.batch[f];
+    t->result = meta[2 * nf + f] == 0 ? KSJ_GPU_OK : KSJ_GPU_ERROR_NONFINITE_INPUT;
+    t->done = true;
+    if (t->result == KSJ_GPU_OK) {
+      ++completed;
+      samples_done += static_cast<uint64_t>(t->req.channels) * t->req.samples;
+    } else {
+      ++failed;
+    }
+    latencies_ms.push_back(std::chrono::duration<double, std::milli>(now - t->submitted).count());
+  }
+  ++batches;
+  batched_frames += nf;
   last_done = now;
+  slot.batch.clear();
+  slot.bytes = 0;
+  slot.frames = 0;
   done_cv.notify_all();
 }
 
@@ -237,42 +336,59 @@ void ksj_serve::run() {
   done_cv.notify_all();
   for (;;) {
     bool progressed = false;
-    // retire finished slots
     for (Slot& s : slots) {
-      if (s.busy != nullptr && cudaEventQuery(s.done) == cudaSuccess) {
+      if (!s.batch.empty() && cudaEventQuery(s.done) == cudaSuccess) {
         retire(s);
         progressed = true;
       }
     }
-    // admit in arrival order
+    // admit: one batch per free slot
     for (;;) {
-      Ticket* t = nullptr;
       Slot* free_slot = nullptr;
       for (Slot& s : slots)
-        if (s.busy == nullptr) {
+        if (s.batch.empty()) {
           free_slot = &s;
           break;
         }
+      std::vector<Ticket*> batch;
+      uint32_t cmax = 0, mmax = 0;
+      uint64_t bytes = 0;
       {
         std::lock_guard<std::mutex> lock(mu);
         if (free_slot == nullptr || pending.empty()) break;
-        if (in_flight_bytes + pending.front()->bytes > cfg.device_memory_cap) break;
-        t = pending.front();
-        pending.pop_front();
+        const ksj_serve_request& head = pending.front()->req;
+        const ClassKey key = class_of(head);
+        // the head first, then its class's later requests in arrival order,
+        // while the batch stays within its frame limit and the device cap
+        for (auto it = pending.begin(); it != pending.end() && batch.size() < max_batch; ++it) {
+          const ksj_serve_request& r = (*it)->req;
+          if (class_of(r) != key) continue;
+          const uint32_t c = std::max(cmax, r.channels), m = std::max(mmax, r.samples);
+          const uint64_t b = batch_bytes(head, static_cast<uint32_t>(batch.size() + 1), c, m);
+          if (b == 0 || in_flight_bytes + b > cfg.device_memory_cap) {
+            if (batch.empty()) break;  // the head waits for bytes to free
+            continue;
+          }
+          batch.push_back(*it);
+          cmax = c;
+          mmax = m;
+          bytes = b;
+        }
+        if (batch.empty()) break;
+        for (Ticket* t : batch) pending.erase(std::find(pending.begin(), pending.end(), t));
       }
-      in_flight_bytes += t->bytes;
-      if (!launch(*free_slot, t)) {
-        free_slot->busy = nullptr;
-        in_flight_bytes -= t->bytes;
+      in_flight_bytes += bytes;
+      free_slot->bytes = bytes;
+      if (!launch(*free_slot, batch, cmax, mmax)) {
+        free_slot->batch.clear();
+        in_flight_bytes -= bytes;
+        free_slot->bytes = 0;
         cudaStreamSynchronize(free_slot->stream);
-        std::lock_guard<std::mutex> lock(mu);
-        t->result = KSJ_GPU_ERROR_CUDA;
-        t->done = true;
-        ++failed;
-        done_cv.notify_all();
+        cudaGetLastError();
+        fail_batch(batch, KSJ_GPU_ERROR_CUDA);
       } else {
         uint32_t n = 0;
-        for (Slot& s : slots) n += s.busy != nullptr;
+        for (Slot& s : slots) n += s.batch.empty() ? 0u : static_cast<uint32_t>(s.batch.size());
         std::lock_guard<std::mutex> lock(mu);
         peak_bytes = std::max(peak_bytes, in_flight_bytes);
         peak_in_flight = std::max(peak_in_flight, n);
@@ -280,16 +396,16 @@ void ksj_serve::run() {
       progressed = true;
     }
     bool busy = false;
-    for (Slot& s : slots) busy |= s.busy != nullptr;
+    for (Slot& s : slots) busy |= !s.batch.empty();
     std::unique_lock<std::mutex> lock(mu);
     if (stop && pending.empty() && !busy) break;
     if (!progressed) work_cv.wait_for(lock, std::chrono::microseconds(busy ? 20 : 2000));
   }
   for (Slot& s : slots) {
     if (s.stream) cudaStreamSynchronize(s.stream);
-    for (Buffer* b : {&s.kspace, &s.traj, &s.out, &s.workspace})
+    for (Buffer* b : {&s.kspace, &s.traj, &s.out, &s.workspace, &s.counts})
       if (b->p) cudaFree(b->p);
-    for (Buffer* b : {&s.pin_in, &s.pin_out})
+    for (Buffer* b : {&s.pin_in, &s.pin_out, &s.pin_meta})
       if (b->p) cudaFreeHost(b->p);
     if (s.done) cudaEventDestroy(s.done);
     if (s.stream) cudaStreamDestroy(s.stream);
@@ -301,13 +417,18 @@ void ksj_serve::run() {
 }
 
 extern "C" ksj_gpu_status ksj_serve_create(const ksj_serve_config* config, ksj_serve** out) {
-  if (config == nullptr || out == nullptr || config->struct_size < sizeof(ksj_serve_config) || config->slots == 0 ||
+  constexpr size_t kBaseConfig = offsetof(ksj_serve_config, max_batch_frames);
+  if (config == nullptr || out == nullptr || config->struct_size < kBaseConfig || config->slots == 0 ||
       config->slots > 64 || config->device_memory_cap == 0)
     return KSJ_GPU_ERROR_INVALID_ARGUMENT;
   *out = nullptr;
   auto* s = new (std::nothrow) ksj_serve{};
   if (s == nullptr) return KSJ_GPU_ERROR_OUT_OF_MEMORY;
-  s->cfg = *config;
+  std::memcpy(&s->cfg, config, std::min<size_t>(config->struct_size, sizeof(ksj_serve_config)));
+  s->cfg.struct_size = sizeof(ksj_serve_config);
+  if (config->struct_size >= offsetof(ksj_serve_config, max_batch_frames) + sizeof(uint32_t) &&
+      config->max_batch_frames != 0)
+    s->max_batch = std::min<uint32_t>(config->max_batch_frames, 1024);
   s->worker = std::thread([s] { s->run(); });
   {
     std::unique_lock<std::mutex> lock(s->mu);
@@ -328,12 +449,10 @@ extern "C" ksj_gpu_status ksj_serve_create(const ksj_serve_config* config, ksj_s
 extern "C" ksj_gpu_status ksj_serve_submit(ksj_serve* s, const ksj_serve_request* r, uint64_t* out_ticket) {
   if (s == nullptr || r == nullptr || out_ticket == nullptr || r->struct_size < sizeof(ksj_serve_request))
     return KSJ_GPU_ERROR_INVALID_ARGUMENT;
-  const ksj_gpu_gridding_desc d = make_desc(*r);
-  const size_t ws = ksj_gpu_gridding_workspace_bytes(&d);
   const uint64_t kb = uint64_t{r->channels} * r->samples * 8;
-  const uint64_t bytes = ws + kb + uint64_t{r->samples} * 8 + out_bytes(*r);
+  const uint64_t bytes = r->channels && r->samples ? batch_bytes(*r, 1, r->channels, r->samples) : 0;
   std::lock_guard<std::mutex> lock(s->mu);
-  if (ws == 0 || r->kspace == nullptr || r->trajectory == nullptr || r->out == nullptr ||
+  if (bytes == 0 || r->kspace == nullptr || r->trajectory == nullptr || r->out == nullptr ||
       (r->output != KSJ_SERVE_OUTPUT_RSS && r->output != KSJ_SERVE_OUTPUT_COIL_MAJOR) || r->channels > s->cfg.max_channels ||
       kb > s->cfg.max_frame_bytes || out_bytes(*r) > s->cfg.max_image_bytes || bytes > s->cfg.device_memory_cap) {
     ++s->rejected;
@@ -408,6 +527,8 @@ extern "C" ksj_gpu_status ksj_serve_get_stats(ksj_serve* s, ksj_serve_stats* out
   }
   out->peak_device_bytes = s->peak_bytes;
   out->peak_in_flight = s->peak_in_flight;
+  out->batches = s->batches;
+  out->batched_frames = s->batched_frames;
   return KSJ_GPU_OK;
 }
 
@@ -415,6 +536,7 @@ extern "C" void ksj_serve_reset_stats(ksj_serve* s) {
   if (s == nullptr) return;
   std::lock_guard<std::mutex> lock(s->mu);
   s->submitted = s->completed = s->rejected = s->failed = s->samples_done = 0;
+  s->batches = s->batched_frames = 0;
   s->latencies_ms.clear();
   s->any_submit = false;
   s->peak_bytes = 0;

@@ -43,7 +43,8 @@ class GriddingTuning(ctypes.Structure):
     _fields_ = [("struct_size", ctypes.c_uint32), ("coil_group", ctypes.c_uint32),
                 ("column_block", ctypes.c_uint32), ("list_capacity", ctypes.c_uint32),
                 ("frames_per_pass", ctypes.c_uint32), ("rows_blocks_per_sm", ctypes.c_uint32),
-                ("coil_parts", ctypes.c_uint32), ("wait_fault_polls", ctypes.c_uint32)]
+                ("coil_parts", ctypes.c_uint32), ("column_pass", ctypes.c_uint32),
+                ("wait_fault_polls", ctypes.c_uint32)]
 
 
 _lib = None

@@ -2,9 +2,11 @@
 
 A :class:`Server` owns a scheduler thread and ``slots`` CUDA streams on one
 device.  Requests (one Kaiser-Bessel slice reconstruction each, of any
-readout/spoke/coil shape within the caps) are queued with :meth:`Server.submit`
-and run concurrently as slots and the device-byte cap allow; each result is
-byte-identical to the same ``ksj_gpu_gridding_adjoint`` call made alone.
+readout/spoke/coil shape within the caps) are queued with :meth:`Server.submit`;
+pending requests of one class leave together as one ragged multi-frame call
+whenever a slot is free, and batches on different slots overlap, as slots and
+the device-byte cap allow.  Each result is byte-identical to the same
+``ksj_gpu_gridding_adjoint`` call made alone.
 """
 from __future__ import annotations
 
@@ -23,7 +25,8 @@ HOST_PINNED = 1
 class ServeConfig(ctypes.Structure):
     _fields_ = [("struct_size", ctypes.c_uint32), ("device", ctypes.c_int32), ("slots", ctypes.c_uint32),
                 ("max_channels", ctypes.c_uint32), ("device_memory_cap", ctypes.c_uint64),
-                ("max_frame_bytes", ctypes.c_uint64), ("max_image_bytes", ctypes.c_uint64)]
+                ("max_frame_bytes", ctypes.c_uint64), ("max_image_bytes", ctypes.c_uint64),
+                ("max_batch_frames", ctypes.c_uint32), ("reserved0", ctypes.c_uint32)]
 
 
 class ServeRequest(ctypes.Structure):
@@ -39,7 +42,8 @@ class ServeStats(ctypes.Structure):
                 ("failed", ctypes.c_uint64), ("gridded_samples", ctypes.c_uint64), ("wall_seconds", ctypes.c_double),
                 ("latency_p50_ms", ctypes.c_double), ("latency_p99_ms", ctypes.c_double),
                 ("latency_max_ms", ctypes.c_double), ("peak_device_bytes", ctypes.c_uint64),
-                ("peak_in_flight", ctypes.c_uint32), ("reserved0", ctypes.c_uint32)]
+                ("peak_in_flight", ctypes.c_uint32), ("reserved0", ctypes.c_uint32),
+                ("batches", ctypes.c_uint64), ("batched_frames", ctypes.c_uint64)]
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_ if name != "reserved0"}
@@ -94,10 +98,11 @@ class Request:
 
 class Server:
     def __init__(self, slots: int = 4, device_memory_cap: int = 16 << 30, max_channels: int = 32,
-                 max_frame_bytes: int = 256 << 20, max_image_bytes: int = 128 << 20, device: int = 0):
+                 max_frame_bytes: int = 256 << 20, max_image_bytes: int = 128 << 20, device: int = 0,
+                 max_batch_frames: int = 0):
         self._L = _lib()
         cfg = ServeConfig(ctypes.sizeof(ServeConfig), device, slots, max_channels, device_memory_cap,
-                          max_frame_bytes, max_image_bytes)
+                          max_frame_bytes, max_image_bytes, max_batch_frames, 0)
         h = ctypes.c_void_p()
         gpu._check(self._L.ksj_serve_create(ctypes.byref(cfg), ctypes.byref(h)), "serve_create")
         self._h = h

@@ -117,7 +117,7 @@ def test_segment_wait_runs_out_and_the_call_returns(native, cuda):
     g.run(k, t, want, ws)
     assert g.flags(ws) == 0
     for cg in (32, 16):  # the 32-coil register path and the shared-memory path
-        tun = gpu.GriddingTuning(ctypes.sizeof(gpu.GriddingTuning), cg, 0, 0, 0, 0, 0, 256)
+        tun = gpu.GriddingTuning(ctypes.sizeof(gpu.GriddingTuning), cg, 0, 0, 0, 0, 0, 0, 256)
         out = g.new_output(cuda)
         g.run(k, t, out, ws, tuning=tun)
         torch.cuda.synchronize()

@@ -290,13 +290,15 @@ def test_two_step_rows_byte_identical_across_row_kernels(native, cuda, orc, chan
         g.run(k, t, base, ws)
         want = base.cpu().numpy()
         ran = []
-        for cg, rb, fpp in ((32, 1, 0), (32, 2, 0), (32, 2, 1), (32, 1, 2), (16, 2, 0), (8, 1, 1)):
-            tun = gpu.GriddingTuning(ctypes.sizeof(gpu.GriddingTuning), cg, 0, 0, fpp, rb, 1)
+        # column pass 1: one CTA per (frame, column block); 2: the persistent ring
+        for cg, rb, fpp, colp in ((32, 1, 0, 1), (32, 2, 0, 2), (32, 2, 1, 1), (32, 1, 2, 2), (16, 2, 0, 1),
+                                  (8, 1, 1, 2), (32, 2, 0, 1)):
+            tun = gpu.GriddingTuning(ctypes.sizeof(gpu.GriddingTuning), cg, 0, 0, fpp, rb, 1, colp)
             o = g.new_output(cuda)
             o.fill_(float("nan")) if o.dtype == torch.float32 else o.real.fill_(float("nan"))
             g.run(k, t, o, ws, tuning=tun)
             assert g.flags(ws) == 0
-            assert o.cpu().numpy().tobytes() == want.tobytes(), (mode, cg, rb, fpp)
+            assert o.cpu().numpy().tobytes() == want.tobytes(), (mode, cg, rb, fpp, colp)
             ran.append((cg, rb, fpp))
         assert (32, 2, 1) in ran
         if mode == gpu.OUTPUT_COIL_LAST:
@@ -334,13 +336,14 @@ def test_long_lists_byte_identical(native, cuda, orc, channels, grid, spokes):
     g.run(k, t, base, ws)
     assert g.flags(ws) == 0
     want = base.cpu().numpy()
-    for cg, rb, fpp, parts in ((32, 1, 0, 1), (32, 2, 1, 1), (16, 2, 0, 1), (16, 1, 0, 2), (8, 2, 1, 2), (8, 1, 0, 1)):
-        tun = gpu.GriddingTuning(ctypes.sizeof(gpu.GriddingTuning), cg, 0, 0, fpp, rb, parts)
+    for cg, rb, fpp, parts, colp in ((32, 1, 0, 1, 1), (32, 2, 1, 1, 2), (16, 2, 0, 1, 1), (16, 1, 0, 2, 2),
+                                     (8, 2, 1, 2, 1), (8, 1, 0, 1, 2)):
+        tun = gpu.GriddingTuning(ctypes.sizeof(gpu.GriddingTuning), cg, 0, 0, fpp, rb, parts, colp)
         o = g.new_output(cuda)
         o.real.fill_(float("nan"))
         g.run(k, t, o, ws, tuning=tun)
         assert g.flags(ws) == 0
-        assert o.cpu().numpy().tobytes() == want.tobytes(), (cg, rb, fpp, parts)
+        assert o.cpu().numpy().tobytes() == want.tobytes(), (cg, rb, fpp, parts, colp)
     d64 = np.hypot(tr[:, 0].astype(np.float64), tr[:, 1].astype(np.float64))
     for c in (0, channels - 1):
         ref = orc.kb_gridding(grid, image, ks[c].astype(np.complex128), tr.astype(np.float64), d64, width=4)

@@ -1,7 +1,8 @@
-"""The request loop (include/ksj_serve.h): requests of uneven shape run
-concurrently and each result equals the same gridding call made alone,
-byte for byte; per-request caps reject; the device-byte cap limits how many
-requests are in flight."""
+"""The request loop (include/ksj_serve.h): requests of uneven shape are
+batched by class into ragged multi-frame calls that run concurrently, and
+each result equals the same gridding call made alone, byte for byte; a
+request with a bad input fails alone; per-request caps reject; the
+device-byte cap limits how many requests are in flight."""
 import numpy as np
 import pytest
 
@@ -96,3 +97,48 @@ def test_caps_reject_and_admission_limits_in_flight():
     assert st["peak_device_bytes"] <= one + one // 2
     for r, got in zip(reqs, outs):
         assert np.array_equal(got, _alone(r))
+
+
+def test_requests_batch_into_ragged_calls_and_equal_alone():
+    """A burst of one class (grid 256) with uneven spokes and coils leaves in
+    a few ragged calls, not one call per request; each result still equals
+    its own call made alone, byte for byte; the serial configuration
+    (one slot, batches of one) gives the same bytes."""
+    shapes = [(256, 64 + 37 * i, 4 + (5 * i) % 29) for i in range(12)]
+    reqs = [_request(ro, sp, co, seed=40 + i, output=serve.OUTPUT_COIL_MAJOR if i % 4 == 3 else serve.OUTPUT_RSS)
+            for i, (ro, sp, co) in enumerate(shapes)]
+    with serve.Server(slots=2, max_batch_frames=8) as s:
+        tickets = [s.submit(r) for r in reqs]
+        outs = [s.wait(t, timeout_ms=60000).copy() for t in tickets]
+        st = s.stats()
+    assert st["completed"] == len(reqs) and st["failed"] == 0
+    assert st["batched_frames"] == len(reqs)
+    assert st["batches"] < len(reqs), st
+    with serve.Server(slots=1, max_batch_frames=1) as s:
+        tickets = [s.submit(r) for r in reqs]
+        serial = [s.wait(t, timeout_ms=60000).copy() for t in tickets]
+        assert s.stats()["batches"] == len(reqs)
+    for r, got, one in zip(reqs, outs, serial):
+        want = _alone(r)
+        assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+        assert np.array_equal(one.view(np.uint32), want.view(np.uint32))
+
+
+def test_bad_request_fails_alone_in_its_batch():
+    """A non-finite sample in one request of a batch fails that request
+    (KSJ_GPU_ERROR_NONFINITE_INPUT) and no other."""
+    reqs = [_request(128, 64 + 8 * i, 8, seed=70 + i) for i in range(5)]
+    reqs[2].kspace[3, 17] = complex(float("nan"), 0.0)
+    with serve.Server(slots=1, max_batch_frames=8) as s:
+        tickets = [s.submit(r) for r in reqs]
+        results = []
+        for t in tickets:
+            try:
+                results.append(s.wait(t, timeout_ms=60000).copy())
+            except gpu.GpuError as e:
+                results.append(e)
+        st = s.stats()
+    assert st["failed"] == 1 and st["completed"] == 4
+    assert isinstance(results[2], gpu.GpuError)
+    for i in (0, 1, 3, 4):
+        assert np.array_equal(results[i].view(np.uint32), _alone(reqs[i]).view(np.uint32))
