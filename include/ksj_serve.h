@@ -87,6 +87,9 @@ typedef struct ksj_serve_stats {
   uint32_t reserved0;
   uint64_t batches;           /* ragged calls launched */
   uint64_t batched_frames;    /* requests those calls carried */
+  double copy_in_ms;          /* per batch, summed: stream time of the input copies */
+  double compute_ms;          /* the ragged reconstruction calls */
+  double copy_out_ms;         /* the result copies */
 } ksj_serve_stats;
 
 KSJ_GPU_API ksj_gpu_status ksj_serve_create(const ksj_serve_config* config, ksj_serve** out);

@@ -293,6 +293,67 @@ __device__ __forceinline__ void dft_inverse<6>(float2* v) {
   v[5] = o[2];
 }
 
+// exp(2 pi i t / 5) and exp(2 pi i t / 7), t = 1 .. R-1 (cos, sin), as
+// double literals.
+__host__ __device__ constexpr double omega_odd(int r, int t, int part) {
+  // r = 5: cos 72, 144 degrees, sin 72, 144; t > R/2 by symmetry
+  return r == 5 ? (t == 1   ? (part ? 0.9510565162951535 : 0.30901699437494745)
+                   : t == 2 ? (part ? 0.5877852522924731 : -0.8090169943749475)
+                   : t == 3 ? (part ? -0.5877852522924731 : -0.8090169943749475)
+                            : (part ? -0.9510565162951535 : 0.30901699437494745))
+                : (t == 1   ? (part ? 0.7818314824680298 : 0.6234898018587336)
+                   : t == 2 ? (part ? 0.9749279121818236 : -0.22252093395631434)
+                   : t == 3 ? (part ? 0.4338837391175582 : -0.9009688679024191)
+                   : t == 4 ? (part ? -0.4338837391175582 : -0.9009688679024191)
+                   : t == 5 ? (part ? -0.9749279121818236 : -0.22252093395631434)
+                            : (part ? -0.7818314824680298 : 0.6234898018587336));
+}
+
+// R-point inverse DFT for R = 5, 7 by its definition (R^2 complex
+// multiply-adds with constant twiddles; the inputs' pairwise sums and
+// differences halve the products).
+template <int R>
+__device__ __forceinline__ void dft_inverse_odd(float2* v) {
+  constexpr int H = R / 2;
+  float2 sum[H + 1], dif[H + 1];
+#pragma unroll
+  for (int j = 1; j <= H; ++j) {
+    sum[j] = cadd(v[j], v[R - j]);
+    dif[j] = csub(v[j], v[R - j]);
+  }
+  float2 out[R];
+  out[0] = v[0];
+#pragma unroll
+  for (int j = 1; j <= H; ++j) out[0] = cadd(out[0], sum[j]);
+#pragma unroll
+  for (int k = 1; k <= H; ++k) {
+    // X[k] = x0 + sum_j (cos(2 pi jk/R) sum_j + i sin(2 pi jk/R) dif_j); X[R-k] has -i
+    float2 re = v[0], im = make_float2(0.0f, 0.0f);
+#pragma unroll
+    for (int j = 1; j <= H; ++j) {
+      const float c = static_cast<float>(omega_odd(R, (j * k) % R, 0));
+      const float sn = static_cast<float>(omega_odd(R, (j * k) % R, 1));
+      re = make_float2(fmaf(c, sum[j].x, re.x), fmaf(c, sum[j].y, re.y));
+      im = make_float2(fmaf(sn, dif[j].x, im.x), fmaf(sn, dif[j].y, im.y));
+    }
+    // i * im = (-im.y, im.x)
+    out[k] = make_float2(re.x - im.y, re.y + im.x);
+    out[R - k] = make_float2(re.x + im.y, re.y - im.x);
+  }
+#pragma unroll
+  for (int k = 0; k < R; ++k) v[k] = out[k];
+}
+
+template <>
+__device__ __forceinline__ void dft_inverse<5>(float2* v) {
+  dft_inverse_odd<5>(v);
+}
+
+template <>
+__device__ __forceinline__ void dft_inverse<7>(float2* v) {
+  dft_inverse_odd<7>(v);
+}
+
 // cos(2 pi r / 96) for r in [0, 24] (a quarter turn), as double literals.
 __host__ __device__ constexpr double cos96(int r) {
   switch (r) {
@@ -453,39 +514,57 @@ __host__ __device__ constexpr bool has_two_step_rows(int n) {
 // columns it read): N2 * (k mod 16) + k / 16.
 __host__ __device__ constexpr int two_step_slot(int k, int n) { return (k & 15) * (n >> 4) + (k >> 4); }
 
-// In-place mixed-radix decimation-in-frequency plan for n = 2^a 3^b (b <= 1):
-// a factor 3 first (as radix 6 when n is even), then radix-8 stages, then a
-// final 4 or 2, so every block length after the first stage is a power of
-// two.  Stage s splits blocks of length m[s] * radix[s] into radix[s]
-// sub-blocks of length m[s] = 2^lg_m[s]; its twiddles are
-// exp(2 pi i (i * d * tw_stride[s]) / n).  The output X[k] ends at
-// dif_position(k) (digit reversal).
+// In-place mixed-radix decimation-in-frequency plan for n = 2^a 3^b 5^c 7^d
+// (n <= 4096).  For n = 2^a 3^b with b <= 1: a factor 3 first (as radix 6
+// when n is even), then radix-8 stages, then a final 4 or 2, so every block
+// length after the first stage is a power of two and all indexing is
+// shifts.  Otherwise the odd factors come first, one stage each (7s, 5s, 3s),
+// then the power of two as above; stages whose sub-block length is not a
+// power of two index with divisions (lg_m = -1).  Stage s splits blocks of
+// length m[s] * radix[s] into radix[s] sub-blocks of length m[s]; its
+// twiddles are exp(2 pi i (i * d * tw_stride[s]) / n).  The output X[k] ends
+// at dif_position(k) (digit reversal).
 struct DifPlan {
   int n;
   int stages;
-  int radix[12];
-  int lg_m[12];
-  int nbf[12];        // butterflies per line: n / radix
-  int tw_stride[12];  // n / block length
+  int radix[16];
+  int lg_m[16];       // log2 of the sub-block length, or -1 when it is not a power of two
+  int m[16];          // sub-block length
+  int nbf[16];        // butterflies per line: n / radix
+  int tw_stride[16];  // n / block length
 };
 
 inline bool make_dif_plan(int n, DifPlan* p) {
   if (n < 2 || n > 4096) return false;
-  int m = n, threes = 0;
+  int m = n, threes = 0, fives = 0, sevens = 0;
+  while (m % 7 == 0) {
+    m /= 7;
+    ++sevens;
+  }
+  while (m % 5 == 0) {
+    m /= 5;
+    ++fives;
+  }
   while (m % 3 == 0) {
     m /= 3;
     ++threes;
   }
-  if (threes > 1 || (m & (m - 1)) != 0) return false;
-  int rad[12];
+  if ((m & (m - 1)) != 0) return false;
+  int rad[16];
   int ns = 0;
-  if (threes) {
-    if (m >= 2) {
-      rad[ns++] = 6;
-      m /= 2;
-    } else {
-      rad[ns++] = 3;
+  if (threes <= 1 && fives == 0 && sevens == 0) {
+    if (threes) {
+      if (m >= 2) {
+        rad[ns++] = 6;
+        m /= 2;
+      } else {
+        rad[ns++] = 3;
+      }
     }
+  } else {
+    for (int i = 0; i < sevens; ++i) rad[ns++] = 7;
+    for (int i = 0; i < fives; ++i) rad[ns++] = 5;
+    for (int i = 0; i < threes; ++i) rad[ns++] = 3;
   }
   while (m >= 8) {
     rad[ns++] = 8;
@@ -501,7 +580,8 @@ inline bool make_dif_plan(int n, DifPlan* p) {
     int lg = 0;
     while ((1 << lg) < sub) ++lg;
     p->radix[s] = rad[s];
-    p->lg_m[s] = lg;
+    p->lg_m[s] = (1 << lg) == sub ? lg : -1;
+    p->m[s] = sub;
     p->nbf[s] = n / rad[s];
     p->tw_stride[s] = n / len;
     len = sub;
@@ -603,6 +683,30 @@ __device__ __forceinline__ void dif_stage_pairs(float2* smem, int lg_lines, int 
   }
 }
 
+// A DIF stage whose sub-block length m is not a power of two (plans with
+// several odd factors): the butterfly u of each line starts at
+// (u / m) * R * m + u mod m; one line per thread as in dif_stage.
+template <int R>
+__device__ __forceinline__ void dif_stage_any(float2* smem, int lg_lines, int nbf, int m, int tws,
+                                              const float2* __restrict__ tw, int tid, int nthreads) {
+  const int line = tid & ((1 << lg_lines) - 1);
+  const int step = nthreads >> lg_lines;
+  for (int u = tid >> lg_lines; u < nbf; u += step) {
+    const int blk = u / m, i = u - blk * m;
+    const int base = blk * R * m + i;
+    float2 v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = smem[((base + r * m) << lg_lines) + line];
+    dft_inverse<R>(v);
+    if (i != 0) {
+#pragma unroll
+      for (int d = 1; d < R; ++d) v[d] = cmul(v[d], tw[i * d * tws]);
+    }
+#pragma unroll
+    for (int d = 0; d < R; ++d) smem[((base + d * m) << lg_lines) + line] = v[d];
+  }
+}
+
 // Unnormalised inverse FFT (exp(+2 pi i n k / N)) of every line, in place,
 // output digit-reversed; tw[t] = exp(2 pi i t / n).  Requires nthreads to be
 // a multiple of the line count.  Synchronises the block after each stage.
@@ -610,6 +714,18 @@ __device__ __forceinline__ void dif_lines(float2* smem, int lg_lines, const DifP
                                           const float2* __restrict__ tw, int tid, int nthreads) {
   for (int s = 0; s < p.stages; ++s) {
     const int nbf = p.nbf[s], lg_m = p.lg_m[s], tws = p.tw_stride[s];
+    if (lg_m < 0 || p.radix[s] == 5 || p.radix[s] == 7) {
+      switch (p.radix[s]) {
+        case 8: dif_stage_any<8>(smem, lg_lines, nbf, p.m[s], tws, tw, tid, nthreads); break;
+        case 7: dif_stage_any<7>(smem, lg_lines, nbf, p.m[s], tws, tw, tid, nthreads); break;
+        case 5: dif_stage_any<5>(smem, lg_lines, nbf, p.m[s], tws, tw, tid, nthreads); break;
+        case 4: dif_stage_any<4>(smem, lg_lines, nbf, p.m[s], tws, tw, tid, nthreads); break;
+        case 3: dif_stage_any<3>(smem, lg_lines, nbf, p.m[s], tws, tw, tid, nthreads); break;
+        default: dif_stage_any<2>(smem, lg_lines, nbf, p.m[s], tws, tw, tid, nthreads); break;
+      }
+      __syncthreads();
+      continue;
+    }
     if (lg_lines >= 1) {
       switch (p.radix[s]) {
         case 8: dif_stage_pairs<8>(smem, lg_lines, nbf, lg_m, tws, tw, tid, nthreads); break;

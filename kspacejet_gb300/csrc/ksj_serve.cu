@@ -61,7 +61,7 @@ struct Buffer {
 
 struct Slot {
   cudaStream_t stream = nullptr;
-  cudaEvent_t done = nullptr;
+  cudaEvent_t start = nullptr, copied = nullptr, computed = nullptr, done = nullptr;  // timing events of a batch
   Buffer kspace, traj, out, workspace, counts;  // device
   Buffer pin_in, pin_out, pin_meta;             // pinned host: pageable inputs, pageable outputs, counts + flags
   std::vector<Ticket*> batch;                    // in frame order; empty = free
@@ -163,6 +163,7 @@ struct ksj_serve {
   std::thread worker;
   // statistics (under mu)
   uint64_t submitted = 0, completed = 0, rejected = 0, failed = 0, samples_done = 0, batches = 0, batched_frames = 0;
+  double copy_in_ms = 0.0, compute_ms = 0.0, copy_out_ms = 0.0;
   std::vector<double> latencies_ms;
   Clock::time_point first_submit, last_done;
   bool any_submit = false;
@@ -202,7 +203,8 @@ bool ksj_serve::launch(Slot& slot, const std::vector<Ticket*>& batch, uint32_t c
     meta[f] = batch[f]->req.channels;
     meta[nf + f] = batch[f]->req.samples;
   }
-  if (cudaMemcpyAsync(slot.counts.p, meta, size_t{nf} * 8, cudaMemcpyHostToDevice, slot.stream) != cudaSuccess)
+  if (cudaEventRecord(slot.start, slot.stream) != cudaSuccess ||
+      cudaMemcpyAsync(slot.counts.p, meta, size_t{nf} * 8, cudaMemcpyHostToDevice, slot.stream) != cudaSuccess)
     return false;
   char* stage = static_cast<char*>(slot.pin_in.p);
   for (uint32_t f = 0; f < nf; ++f) {
@@ -248,9 +250,11 @@ bool ksj_serve::launch(Slot& slot, const std::vector<Ticket*>& batch, uint32_t c
     }
   }
   const uint32_t* counts = static_cast<const uint32_t*>(slot.counts.p);
-  if (ksj_gpu_gridding_adjoint_ragged(&d, nullptr, counts, counts + nf, slot.kspace.p,
+  if (cudaEventRecord(slot.copied, slot.stream) != cudaSuccess ||
+      ksj_gpu_gridding_adjoint_ragged(&d, nullptr, counts, counts + nf, slot.kspace.p,
                                       static_cast<const float*>(slot.traj.p), nullptr, slot.out.p, slot.workspace.p,
-                                      slot.workspace.cap, slot.stream) != KSJ_GPU_OK)
+                                      slot.workspace.cap, slot.stream) != KSJ_GPU_OK ||
+      cudaEventRecord(slot.computed, slot.stream) != cudaSuccess)
     return false;
   // results (a coil-major frame's first `channels` coils are contiguous),
   // then every frame's check flags
@@ -299,7 +303,14 @@ void ksj_serve::retire(Slot& slot) {
       std::memcpy(t->req.out, static_cast<const char*>(slot.pin_out.p) + slot.out_staged[f], out_bytes(t->req));
   }
   in_flight_bytes -= slot.bytes;
+  float t_in = 0.0f, t_run = 0.0f, t_out = 0.0f;
+  cudaEventElapsedTime(&t_in, slot.start, slot.copied);
+  cudaEventElapsedTime(&t_run, slot.copied, slot.computed);
+  cudaEventElapsedTime(&t_out, slot.computed, slot.done);
   std::lock_guard<std::mutex> lock(mu);
+  copy_in_ms += t_in;
+  compute_ms += t_run;
+  copy_out_ms += t_out;
   for (uint32_t f = 0; f < nf; ++f) {
     Ticket* t = slot.batch[f];
     t->result = meta[2 * nf + f] == 0 ? KSJ_GPU_OK : KSJ_GPU_ERROR_NONFINITE_INPUT;
@@ -326,7 +337,8 @@ void ksj_serve::run() {
   slots.resize(cfg.slots);
   for (Slot& s : slots) {
     if (cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming) != cudaSuccess)
+        cudaEventCreate(&s.start) != cudaSuccess || cudaEventCreate(&s.copied) != cudaSuccess ||
+        cudaEventCreate(&s.computed) != cudaSuccess || cudaEventCreate(&s.done) != cudaSuccess)
       return;
   }
   {
@@ -407,7 +419,8 @@ void ksj_serve::run() {
       if (b->p) cudaFree(b->p);
     for (Buffer* b : {&s.pin_in, &s.pin_out, &s.pin_meta})
       if (b->p) cudaFreeHost(b->p);
-    if (s.done) cudaEventDestroy(s.done);
+    for (cudaEvent_t e : {s.start, s.copied, s.computed, s.done})
+      if (e) cudaEventDestroy(e);
     if (s.stream) cudaStreamDestroy(s.stream);
   }
   for (auto& kv : trajectories) {
@@ -529,6 +542,9 @@ extern "C" ksj_gpu_status ksj_serve_get_stats(ksj_serve* s, ksj_serve_stats* out
   out->peak_in_flight = s->peak_in_flight;
   out->batches = s->batches;
   out->batched_frames = s->batched_frames;
+  out->copy_in_ms = s->copy_in_ms;
+  out->compute_ms = s->compute_ms;
+  out->copy_out_ms = s->copy_out_ms;
   return KSJ_GPU_OK;
 }
 
@@ -537,6 +553,7 @@ extern "C" void ksj_serve_reset_stats(ksj_serve* s) {
   std::lock_guard<std::mutex> lock(s->mu);
   s->submitted = s->completed = s->rejected = s->failed = s->samples_done = 0;
   s->batches = s->batched_frames = 0;
+  s->copy_in_ms = s->compute_ms = s->copy_out_ms = 0.0;
   s->latencies_ms.clear();
   s->any_submit = false;
   s->peak_bytes = 0;

@@ -43,7 +43,8 @@ class ServeStats(ctypes.Structure):
                 ("latency_p50_ms", ctypes.c_double), ("latency_p99_ms", ctypes.c_double),
                 ("latency_max_ms", ctypes.c_double), ("peak_device_bytes", ctypes.c_uint64),
                 ("peak_in_flight", ctypes.c_uint32), ("reserved0", ctypes.c_uint32),
-                ("batches", ctypes.c_uint64), ("batched_frames", ctypes.c_uint64)]
+                ("batches", ctypes.c_uint64), ("batched_frames", ctypes.c_uint64),
+                ("copy_in_ms", ctypes.c_double), ("compute_ms", ctypes.c_double), ("copy_out_ms", ctypes.c_double)]
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_ if name != "reserved0"}

@@ -8,7 +8,7 @@ import oracle
 
 pytestmark = pytest.mark.gpu
 
-TOL = 2e-6  # rel L2 per coil against FP64 (float transforms of <= 512 points per axis)
+TOL = 3e-6  # rel L2 per coil against FP64 (float transforms of <= 512 points per axis)
 
 
 def test_cartesian_reference_known_answer(native, cuda):
@@ -23,7 +23,11 @@ def test_cartesian_reference_known_answer(native, cuda):
 
 
 @pytest.mark.parametrize("frames,channels,rows,cols", [(2, 8, 256, 256), (1, 32, 384, 192), (3, 5, 96, 64),
-                                                      (1, 40, 128, 512), (1, 64, 48, 24), (2, 1, 2, 12)])
+                                                      (1, 40, 128, 512), (1, 64, 48, 24), (2, 1, 2, 12),
+                                                      # lengths with factors 5, 7 and 3^2 (matrices such as
+                                                      # 160, 240, 320, 448 common in MRI)
+                                                      (1, 8, 160, 240), (1, 4, 320, 448), (2, 3, 100, 36),
+                                                      (1, 2, 210, 98), (1, 16, 7, 5), (1, 32, 288, 144)])
 def test_cartesian_matches_fp64(native, cuda, orc, frames, channels, rows, cols):
     import torch
     from kspacejet_gb300 import gpu
@@ -47,6 +51,7 @@ def test_cartesian_rejects(native, cuda):
     from kspacejet_gb300 import gpu
 
     with pytest.raises(gpu.GpuError):
-        gpu.cartesian_ifft2(torch.zeros((2, 100, 100), dtype=torch.complex64, device=cuda))  # 100: not 2^a 3^b
+        # 110 = 2 x 5 x 11: a prime factor above 7 (the reference's FFT takes it; here it is refused)
+        gpu.cartesian_ifft2(torch.zeros((2, 110, 110), dtype=torch.complex64, device=cuda))
     with pytest.raises(gpu.GpuError):
         gpu.cartesian_ifft2(torch.zeros((65, 8, 8), dtype=torch.complex64, device=cuda))

@@ -171,7 +171,9 @@ def _kb_case(orc, image, grid, width, channels, spokes, seed):
 
 
 @pytest.mark.parametrize("image,grid,width,first", [(64, 128, 4, 1), (48, 96, 4, 2), (32, 64, 6, 3), (64, 96, 4, 4),
-                                                    (32, 64, 4, 0), (32, 64, 2, 0), (64, 128, 8, 0)])
+                                                    (32, 64, 4, 0), (32, 64, 2, 0), (64, 128, 8, 0),
+                                                    # grids with factors 5 and 7 (mixed-radix stages of any length)
+                                                    (80, 160, 4, 5), (70, 140, 4, 6), (60, 90, 4, 7)])
 def test_kaiser_bessel_matches_fp64_oracle(native, cuda, orc, image, grid, width, first):
     """Same algorithm in FP64 (oracle) vs the FP32 GPU path: <= 1e-5; against
     the exact direct NUDFT of the DCF-weighted samples: the KB approximation
