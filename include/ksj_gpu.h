@@ -139,23 +139,30 @@ KSJ_GPU_API ksj_gpu_status ksj_gpu_gridding_adjoint(const ksj_gpu_gridding_desc*
                                                     void* d_workspace, size_t workspace_bytes, void* stream);
 
 /* A ragged batch: frames of different coil and sample counts (and the same
- * grid, image, kernel and DCF mode) in one call.  desc->channels and
- * desc->samples are the maxima and give the layouts' pitches: d_kspace
- * [frame][desc->channels][desc->samples], d_traj [frame][desc->samples][2],
- * d_out as for ksj_gpu_gridding_adjoint.  d_frame_channels[f] (1..channels)
- * and d_frame_samples[f] (1..samples), device arrays of `frames` entries,
- * give frame f's coils and samples; the padding of the k-space and of the
- * trajectory is never read.  Frame f's output equals that of
- * ksj_gpu_gridding_adjoint on the frame alone with its own coil and sample
- * counts, byte for byte (coil outputs: its first d_frame_channels[f] coils,
- * the others zero).  Kaiser-Bessel only.  Workspace:
- * ksj_gpu_gridding_workspace_bytes(desc).  No counterpart in the reference
- * (the batching behind the request loop of ksj_serve.h). */
+ * grid, image, kernel and DCF mode) in one call, each frame's inputs where
+ * they already are.  desc->channels and desc->samples are the maxima (they
+ * size the workspace); desc->dcf_mode is NONE or ANALYTIC_RAMP.  Device
+ * arrays of `frames` entries give frame f's coils d_frame_channels[f]
+ * (1..channels), samples d_frame_samples[f] (1..samples), and the addresses
+ * of its samples d_frame_kspace[f] (complex64 [channel][sample], packed at
+ * its own counts) and trajectory d_frame_traj[f] (float32 [sample][2]).  An
+ * address may be device memory or host memory the device reads in place
+ * (page-locked and mapped, e.g. cudaHostAlloc / cudaHostRegister on a
+ * unified-addressing system; check with cudaPointerGetAttributes): the
+ * samples are then read across the host link by the kernel that reorders
+ * them, with no separate copy.  d_out as for ksj_gpu_gridding_adjoint.
+ * Frame f's output equals that of ksj_gpu_gridding_adjoint on the frame
+ * alone with its own coil and sample counts, byte for byte (coil outputs:
+ * its first d_frame_channels[f] coils, the others zero).  Kaiser-Bessel
+ * only.  Workspace: ksj_gpu_gridding_workspace_bytes(desc); per-frame check
+ * flags at ksj_gpu_gridding_frame_flags_offset(desc).  No counterpart in the
+ * reference (the batching behind the request loop of ksj_serve.h). */
 KSJ_GPU_API ksj_gpu_status ksj_gpu_gridding_adjoint_ragged(const ksj_gpu_gridding_desc* desc,
                                                            const ksj_gpu_gridding_tuning* tuning,
                                                            const uint32_t* d_frame_channels,
-                                                           const uint32_t* d_frame_samples, const void* d_kspace,
-                                                           const float* d_traj, const float* d_dcf, void* d_out,
+                                                           const uint32_t* d_frame_samples,
+                                                           const uint64_t* d_frame_kspace,
+                                                           const uint64_t* d_frame_traj, void* d_out,
                                                            void* d_workspace, size_t workspace_bytes, void* stream);
 
 /* The same reconstruction from and to host memory: h_kspace, h_traj, h_dcf

@@ -51,7 +51,9 @@ typedef struct ksj_serve_config {
   uint64_t max_frame_bytes;    /* per-request k-space bytes (target envelope: 256 MiB) */
   uint64_t max_image_bytes;    /* per-request output bytes (target envelope: 128 MiB) */
   uint32_t max_batch_frames;   /* requests per batch (one ragged call); 0 = 32, 1 = no batching */
-  uint32_t reserved0;
+  uint32_t read_inputs_in_place; /* nonzero: page-locked, mapped inputs are read by the kernels across the
+                                    host link where they are, with no copy (pageable ones are staged in
+                                    page-locked memory first); 0: inputs are copied to the device */
 } ksj_serve_config;
 
 #define KSJ_SERVE_OUTPUT_RSS 1u         /* float32 [image][image] */

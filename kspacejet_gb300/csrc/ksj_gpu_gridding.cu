@@ -120,9 +120,13 @@ struct Shape {
   uint32_t wait_fault;  // tests only: segment waits that cannot succeed, given up after this many polls
   int column_pass;      // 1 one CTA per tile (k_cols), 2 persistent ring (k_cols_ring)
   DifPlan plan_rows, plan_cols;
-  // ragged batches (device arrays, null otherwise): valid coils and samples of each frame
+  // ragged batches (device arrays, null otherwise): valid coils and samples
+  // of each frame, and the addresses of its samples [C_f][M_f] and of its
+  // trajectory [M_f][2] (device memory or host memory the device reads)
   const uint32_t* frame_channels = nullptr;
   const uint32_t* frame_samples = nullptr;
+  const uint64_t* frame_kspace = nullptr;
+  const uint64_t* frame_traj = nullptr;
 };
 
 struct Layout {
@@ -348,6 +352,7 @@ struct PrepareArgs {
   const float* traj;
   const float* dcf;
   const uint32_t* frame_samples;  // ragged batches: valid samples of each frame (null: all)
+  const uint64_t* frame_traj;     // ragged batches: address of each frame's trajectory [M_f][2]
   uint32_t* frame_flags;          // per-frame copy of the check flags (null: none)
   uint32_t dcf_mode;
   uint32_t require_nyquist;
@@ -379,7 +384,10 @@ __global__ void __launch_bounds__(256) k_prepare(PrepareArgs a) {
     reinterpret_cast<SampleRecord<W>*>(a.records)[idx].r0 = -1;
     return;
   }
-  const float2 k = __ldg(reinterpret_cast<const float2*>(a.traj) + idx);
+  const float2 k =
+      a.frame_traj != nullptr
+          ? reinterpret_cast<const float2*>(__ldg(a.frame_traj + f))[idx - static_cast<size_t>(f) * a.samples]
+          : __ldg(reinterpret_cast<const float2*>(a.traj) + idx);
   bool ok = isfinite(k.x) && isfinite(k.y);
   if (ok && a.require_nyquist) ok = k.x >= -kPiF && k.x <= kPiF && k.y >= -kPiF && k.y <= kPiF;
   // a coordinate far outside the grid would overflow the int tap arithmetic
@@ -922,14 +930,17 @@ ksj_gpu_status launch_sort(SortArgs sa, size_t lists, size_t entries_total, int 
 // non-finite value (either component; bf16 exponent all ones) raises
 // KSJ_GPU_FLAG_NONFINITE_SAMPLE.
 //
-// Ragged batches (frame_channels / frame_samples non-null): frame f holds
-// frame_channels[f] coils of frame_samples[f] samples in the [channel][sample]
-// pitch of the call; the padding is not read and is written as zeros.
+// Ragged batches (frame_channels / frame_samples / frame_src non-null):
+// frame f holds frame_channels[f] coils of frame_samples[f] samples, packed
+// [channel][sample] at address frame_src[f] (device memory, or host memory
+// the device reads in place); the padding up to the call's channels and
+// samples is written as zeros.
 template <uint32_t kFormat>
 __global__ void __launch_bounds__(256) k_samples_coil_last(const void* in_raw, void* out_raw, int channels,
                                                            int samples, uint32_t* flags,
                                                            const uint32_t* frame_channels,
-                                                           const uint32_t* frame_samples, int frame0,
+                                                           const uint32_t* frame_samples,
+                                                           const uint64_t* frame_src, int frame0,
                                                            uint32_t* frame_flags) {
   using T = typename std::conditional<kFormat == KSJ_GPU_SAMPLES_BF16, uint32_t, unsigned long long>::type;
   __shared__ T t[32][33];
@@ -938,10 +949,13 @@ __global__ void __launch_bounds__(256) k_samples_coil_last(const void* in_raw, v
   const int f = blockIdx.z;
   const int s0 = blockIdx.x * 32;
   const int c0 = blockIdx.y * 32;
-  const T* src = in + static_cast<size_t>(f) * channels * samples;
   T* dst = out + static_cast<size_t>(f) * channels * samples;
   const int live_c = frame_channels ? min(channels, static_cast<int>(__ldg(frame_channels + frame0 + f))) : channels;
   const int live_s = frame_samples ? min(samples, static_cast<int>(__ldg(frame_samples + frame0 + f))) : samples;
+  // ragged frames are packed at their own sample count
+  const T* src = frame_src ? reinterpret_cast<const T*>(__ldg(frame_src + frame0 + f))
+                           : in + static_cast<size_t>(f) * channels * samples;
+  const int pitch = frame_src ? live_s : samples;
   bool bad = false;
   for (int y = threadIdx.y; y < 32; y += blockDim.y) {
     const int c = c0 + y, sm = s0 + threadIdx.x;
@@ -950,7 +964,7 @@ __global__ void __launch_bounds__(256) k_samples_coil_last(const void* in_raw, v
         t[y][threadIdx.x] = T(0);
         continue;
       }
-      const T v = src[static_cast<size_t>(c) * samples + sm];
+      const T v = src[static_cast<size_t>(c) * pitch + sm];
       if (kFormat == KSJ_GPU_SAMPLES_BF16) {
         const uint32_t u = static_cast<uint32_t>(v);
         bad |= (u & 0x7f80u) == 0x7f80u || (u & 0x7f800000u) == 0x7f800000u;
@@ -1246,7 +1260,10 @@ __device__ __forceinline__ void rows_grid_regs(const RowsArgs& a, int f, int cgi
 // kCG = 32 fixes a 32-coil group taken whole by one warp (coil_parts 1):
 // lane = coil, no tap groups, every tap offset a constant; kCG = 0 reads the
 // group and the split from the arguments.
-template <int W, uint32_t kFormat, int kThreads, int kBlocks, int kCG>
+// kHalf: the sigma = 2 crop form of the row transform (out_cols =
+// grid_cols / 2, col_shift = out_cols / 2), whose kept columns are known at
+// compile time (fft_two_step_half); the same bytes as the general form.
+template <int W, uint32_t kFormat, int kThreads, int kBlocks, int kCG, bool kHalf = false>
 __global__ void __launch_bounds__(kThreads, kBlocks) k_rows(RowsArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int row = blockIdx.x;
@@ -1473,6 +1490,22 @@ __global__ void __launch_bounds__(kThreads, kBlocks) k_rows(RowsArgs a) {
     if (pc >= a.grid_cols) pc -= a.grid_cols;
     if (pc < a.out_cols && line < live_lines) dst_row[static_cast<size_t>(pc) * a.cpitch + line] = v;
   };
+  if constexpr (kHalf) {
+    auto live = [&](int line) { return line < live_lines; };
+    auto emit_half = [&](int pc, int, int line, float2 v) { dst_row[static_cast<size_t>(pc) * a.cpitch + line] = v; };
+    switch (a.grid_cols) {
+      case 128: fft_two_step_half<16, 8>(acc, lg_cg, tw, tid, nthreads, live, emit_half); return;
+      case 192: fft_two_step_half<16, 12>(acc, lg_cg, tw, tid, nthreads, live, emit_half); return;
+      case 256: fft_two_step_half<16, 16>(acc, lg_cg, tw, tid, nthreads, live, emit_half); return;
+      case 384: fft_two_step_half<16, 24>(acc, lg_cg, tw, tid, nthreads, live, emit_half); return;
+      default:
+        if constexpr (kThreads >= 512) {
+          fft_two_step_half<16, 32>(acc, lg_cg, tw, tid, nthreads, live, emit_half);
+          return;
+        }
+        break;
+    }
+  }
   // (blocks of kThreads threads take rows of up to kThreads columns)
   if (fft_two_step_rows<kThreads>(a.grid_cols, acc, lg_cg, tw, tid, nthreads, emit)) return;
 
@@ -1523,14 +1556,19 @@ struct ColsArgs {
 // kN is the column length for the two-step transform (128 .. 512, see
 // has_two_step_rows), or 0 for the in-place mixed-radix form of any other
 // length; one instance per length keeps each kernel's code small.
-template <int kN>
+// kLgL (when nonzero) fixes log2 of the line count (column_block x
+// col_group) at compile time; kHalf selects the sigma = 2 crop form of the
+// two-step transform (out_rows = grid_rows / 2, row_shift = out_rows / 2,
+// Kaiser-Bessel deapodisation), whose kept rows are known at compile time.
+// Every form gives the same bytes.
+template <int kN, int kLgL = 0, bool kHalf = false>
 __global__ void __launch_bounds__(kColsThreads) k_cols(const __grid_constant__ CUtensorMap inter_map, ColsArgs a) {
   extern __shared__ __align__(16) unsigned char smem_cols[];
   unsigned char* smem_raw = smem_cols;
   const int cb = a.column_block;
   const int cgc = a.col_group;
-  const int lines = cb * cgc;
-  const int lg_lines = ilog2(lines);
+  const int lines = kLgL ? (1 << kLgL) : cb * cgc;
+  const int lg_lines = kLgL ? kLgL : ilog2(lines);
   const int lg_cgc = ilog2(cgc);
   const int lg_cb = ilog2(cb);
   const int col0 = blockIdx.x * cb;
@@ -1611,7 +1649,23 @@ __global__ void __launch_bounds__(kColsThreads) k_cols(const __grid_constant__ C
       if (pr >= a.out_rows || col0 + (ln >> lg_cgc) >= a.out_cols || (ln & (cgc - 1)) >= live_coils_g) return;
       emit_pixel(pr, ln, tile + (two_step_slot(k, a.grid_rows) << lg_lines) + ln, v);
     };
-    if constexpr (kN != 0) {
+    if constexpr (kN != 0 && kHalf) {
+      auto live = [&](int ln) { return col0 + (ln >> lg_cgc) < a.out_cols && (ln & (cgc - 1)) < live_coils_g; };
+      auto emit_half = [&](int pr, int slot, int ln, float2 v) {
+        const int lc = ln >> lg_cgc;
+        const float sc = inv_dr[pr] * __ldg(a.inv_dc + col0 + lc);
+        v.x *= sc;
+        v.y *= sc;
+        if (a.output == KSJ_GPU_OUTPUT_RSS) {
+          tile[(slot << lg_lines) + ln].x = __fadd_rn(__fmul_rn(v.x, v.x), __fmul_rn(v.y, v.y));
+        } else {
+          float2* o = static_cast<float2*>(a.out);
+          o[((static_cast<size_t>(fg) * a.out_rows + pr) * a.out_cols + col0 + lc) * a.out_pitch + g * cgc +
+            (ln & (cgc - 1))] = v;
+        }
+      };
+      fft_two_step_half<16, kN / 16>(tile, lg_lines, tw, tid, nthreads, live, emit_half);
+    } else if constexpr (kN != 0) {
       fft_two_step<16, kN / 16>(tile, lg_lines, tw, tid, nthreads, emit);
     } else {
       dif_lines(tile, lg_lines, a.plan, tw, tid, nthreads);
@@ -1831,9 +1885,14 @@ struct RowsLauncher {
     smem = rows_smem_for(s.grid_cols, s.coil_group, s.width, rows_threads_for(s.grid_cols));
     threads = rows_threads_for(s.grid_cols);
     const bool whole32 = s.coil_group == 32 && s.coil_parts == 1;
-    kernel = (threads <= 384 && s.rows_blocks == 2)
-                 ? (whole32 ? k_rows<W, kFormat, 384, 2, 32> : k_rows<W, kFormat, 384, 2, 0>)
-                 : (whole32 ? k_rows<W, kFormat, kMaxThreads, 1, 32> : k_rows<W, kFormat, kMaxThreads, 1, 0>);
+    // the sigma = 2 crop form for the 32-coil register path
+    const bool half = whole32 && s.kb && s.out_cols * 2 == s.grid_cols && has_two_step_rows(s.grid_cols);
+    if (threads <= 384 && s.rows_blocks == 2)
+      kernel = half ? k_rows<W, kFormat, 384, 2, 32, true>
+                    : (whole32 ? k_rows<W, kFormat, 384, 2, 32> : k_rows<W, kFormat, 384, 2, 0>);
+    else
+      kernel = half ? k_rows<W, kFormat, kMaxThreads, 1, 32, true>
+                    : (whole32 ? k_rows<W, kFormat, kMaxThreads, 1, 32> : k_rows<W, kFormat, kMaxThreads, 1, 0>);
     return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)) ==
                cudaSuccess &&
            cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100) == cudaSuccess;
@@ -1857,14 +1916,22 @@ size_t cols_smem_bytes(const Shape& s) {
 
 using ColsKernel = void (*)(const __grid_constant__ CUtensorMap, ColsArgs);
 
-// The k_cols instance for columns of n grid rows.
-ColsKernel cols_kernel_for(int n) {
+// The k_cols instance for columns of n grid rows; half: the sigma = 2 crop
+// (out_rows = n / 2, row_shift = n / 4, Kaiser-Bessel), lines32: 32 lines per
+// tile (the default column block).
+template <int kN>
+ColsKernel cols_kernel_two_step(bool half, bool lines32) {
+  if (half) return lines32 ? k_cols<kN, 5, true> : k_cols<kN, 0, true>;
+  return lines32 ? k_cols<kN, 5, false> : k_cols<kN, 0, false>;
+}
+
+ColsKernel cols_kernel_for(int n, bool half = false, bool lines32 = false) {
   switch (n) {
-    case 128: return k_cols<128>;
-    case 192: return k_cols<192>;
-    case 256: return k_cols<256>;
-    case 384: return k_cols<384>;
-    case 512: return k_cols<512>;
+    case 128: return cols_kernel_two_step<128>(half, lines32);
+    case 192: return cols_kernel_two_step<192>(half, lines32);
+    case 256: return cols_kernel_two_step<256>(half, lines32);
+    case 384: return cols_kernel_two_step<384>(half, lines32);
+    case 512: return cols_kernel_two_step<512>(half, lines32);
     default: return k_cols<0>;
   }
 }
@@ -1944,7 +2011,8 @@ struct ColsPass {
     if (!ring) {
       column_block = s.column_block;
       smem = cols_smem_bytes(s);
-      kernel = cols_kernel_for(s.grid_rows);
+      const bool half = c->kb && s.out_rows * 2 == s.grid_rows && c->row_shift == s.out_rows / 2;
+      kernel = cols_kernel_for(s.grid_rows, half, s.column_block * s.col_group == 32);
       return cols_kernel_setup(kernel, smem) && make_inter_map(s, inter, &map, &c->box_rows, &c->boxes);
     }
     column_block = cb;
@@ -1999,6 +2067,7 @@ ksj_gpu_status build_lists(const Shape& s, const ksj_gpu_gridding_desc* d, const
     p.traj = d_traj;
     p.dcf = d_dcf;
     p.frame_samples = s.frame_samples;
+    p.frame_traj = s.frame_traj;
     p.frame_flags = frame_flags;
     p.dcf_mode = d->dcf_mode;
     p.require_nyquist = d->require_nyquist;
@@ -2113,9 +2182,10 @@ ksj_gpu_status launch_all(const Shape& s, const Layout& l, const ksj_gpu_griddin
     const size_t eb = sample_bytes(d->sample_format);
     const dim3 tg((s.samples + 31) / 32, (s.channels + 31) / 32, nf);
     LaunchScope scope("k_samples_coil_last", st);
+    const unsigned char* in = s.frame_kspace ? nullptr : static_cast<const unsigned char*>(d_kspace) + f0 * frame_samples * eb;
     k_samples_coil_last<kFormat><<<tg, dim3(32, 8), 0, st>>>(
-        static_cast<const unsigned char*>(d_kspace) + f0 * frame_samples * eb, ws + l.samples_t + f0 * frame_samples * eb,
-        s.channels, s.samples, flags, s.frame_channels, s.frame_samples, f0,
+        in, ws + l.samples_t + f0 * frame_samples * eb,
+        s.channels, s.samples, flags, s.frame_channels, s.frame_samples, s.frame_kspace, f0,
         reinterpret_cast<uint32_t*>(ws + l.frame_flags));
   };
   if (io == nullptr || io->copy == nullptr) to_coil_last(0, s.frames, stream);
@@ -2733,7 +2803,7 @@ ksj_gpu_status launch_all3(const Shape& s, const Layout3& l, const ksj_gpu_gridd
     const dim3 tg((s.samples + 31) / 32, (s.channels + 31) / 32, 1);
     LaunchScope scope("k_samples_coil_last", stream);
     k_samples_coil_last<kFormat><<<tg, dim3(32, 8), 0, stream>>>(d_kspace, ws + l.samples_t, s.channels, s.samples,
-                                                                 flags, nullptr, nullptr, 0, nullptr);
+                                                                 flags, nullptr, nullptr, nullptr, 0, nullptr);
   }
   // rows of every plane (x transformed, kept columns, coil-last)
   RowsArgs r{};
@@ -3245,16 +3315,30 @@ extern "C" size_t ksj_gpu_gridding_frame_flags_offset(const ksj_gpu_gridding_des
 }
 
 namespace {
+// The adjoint of a uniform batch (ragged null) or a ragged one (per-frame
+// counts and input addresses; d_kspace and d_traj unused).
+struct Ragged {
+  const uint32_t* channels;
+  const uint32_t* samples;
+  const uint64_t* kspace;
+  const uint64_t* traj;
+};
+
 ksj_gpu_status gridding_adjoint(const ksj_gpu_gridding_desc* desc, const ksj_gpu_gridding_tuning* tuning,
-                                const uint32_t* d_frame_channels, const uint32_t* d_frame_samples,
-                                const void* d_kspace, const float* d_traj, const float* d_dcf, void* d_out,
-                                void* d_workspace, size_t workspace_bytes, void* stream) {
+                                const Ragged* ragged, const void* d_kspace, const float* d_traj, const float* d_dcf,
+                                void* d_out, void* d_workspace, size_t workspace_bytes, void* stream) {
   Shape s{};
   const ksj_gpu_status st = make_shape(desc, tuning, &s);
   if (st != KSJ_GPU_OK) return st;
-  s.frame_channels = d_frame_channels;
-  s.frame_samples = d_frame_samples;
-  if (d_kspace == nullptr || d_traj == nullptr || d_out == nullptr) return KSJ_GPU_ERROR_INVALID_ARGUMENT;
+  if (ragged != nullptr) {
+    s.frame_channels = ragged->channels;
+    s.frame_samples = ragged->samples;
+    s.frame_kspace = ragged->kspace;
+    s.frame_traj = ragged->traj;
+  } else if (d_kspace == nullptr || d_traj == nullptr) {
+    return KSJ_GPU_ERROR_INVALID_ARGUMENT;
+  }
+  if (d_out == nullptr) return KSJ_GPU_ERROR_INVALID_ARGUMENT;
   if (desc->dcf_mode == KSJ_GPU_DCF_EXTERNAL && d_dcf == nullptr) return KSJ_GPU_ERROR_INVALID_ARGUMENT;
   const Layout l = make_layout(s, desc);
   if (d_workspace == nullptr || (reinterpret_cast<uintptr_t>(d_workspace) & 255u) != 0 || workspace_bytes < l.total)
@@ -3287,21 +3371,24 @@ extern "C" ksj_gpu_status ksj_gpu_gridding_adjoint(const ksj_gpu_gridding_desc* 
                                                    const ksj_gpu_gridding_tuning* tuning, const void* d_kspace,
                                                    const float* d_traj, const float* d_dcf, void* d_out,
                                                    void* d_workspace, size_t workspace_bytes, void* stream) {
-  return gridding_adjoint(desc, tuning, nullptr, nullptr, d_kspace, d_traj, d_dcf, d_out, d_workspace,
-                          workspace_bytes, stream);
+  return gridding_adjoint(desc, tuning, nullptr, d_kspace, d_traj, d_dcf, d_out, d_workspace, workspace_bytes, stream);
 }
 
 extern "C" ksj_gpu_status ksj_gpu_gridding_adjoint_ragged(const ksj_gpu_gridding_desc* desc,
                                                           const ksj_gpu_gridding_tuning* tuning,
                                                           const uint32_t* d_frame_channels,
-                                                          const uint32_t* d_frame_samples, const void* d_kspace,
-                                                          const float* d_traj, const float* d_dcf, void* d_out,
+                                                          const uint32_t* d_frame_samples,
+                                                          const uint64_t* d_frame_kspace,
+                                                          const uint64_t* d_frame_traj, void* d_out,
                                                           void* d_workspace, size_t workspace_bytes, void* stream) {
-  if (d_frame_channels == nullptr || d_frame_samples == nullptr) return KSJ_GPU_ERROR_INVALID_ARGUMENT;
-  if (desc == nullptr || desc->struct_size < sizeof(ksj_gpu_gridding_desc) || desc->kernel != KSJ_GPU_KERNEL_KAISER_BESSEL)
+  if (d_frame_channels == nullptr || d_frame_samples == nullptr || d_frame_kspace == nullptr ||
+      d_frame_traj == nullptr)
     return KSJ_GPU_ERROR_INVALID_ARGUMENT;
-  return gridding_adjoint(desc, tuning, d_frame_channels, d_frame_samples, d_kspace, d_traj, d_dcf, d_out,
-                          d_workspace, workspace_bytes, stream);
+  if (desc == nullptr || desc->struct_size < sizeof(ksj_gpu_gridding_desc) ||
+      desc->kernel != KSJ_GPU_KERNEL_KAISER_BESSEL || desc->dcf_mode == KSJ_GPU_DCF_EXTERNAL)
+    return KSJ_GPU_ERROR_INVALID_ARGUMENT;
+  const Ragged r{d_frame_channels, d_frame_samples, d_frame_kspace, d_frame_traj};
+  return gridding_adjoint(desc, tuning, &r, nullptr, nullptr, nullptr, d_out, d_workspace, workspace_bytes, stream);
 }
 
 extern "C" size_t ksj_gpu_gridding_host_workspace_bytes(const ksj_gpu_gridding_desc* desc) {

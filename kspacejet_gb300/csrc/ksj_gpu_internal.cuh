@@ -489,6 +489,56 @@ __device__ __forceinline__ void fft_two_step(float2* smem, int lg_lines, const f
   }
 }
 
+// The two-step transform above for the sigma = 2 crop: of the N = N1 * N2
+// outputs only the N/2 frequencies k in [-N/4, N/4) are kept, i.e. k2 <
+// N2/4 (k = k1 + N1 k2 < N/4) and k2 >= 3 N2/4 (k >= 3N/4), which the kept
+// index p = (k + N/4) mod N places at k + N/4 and k - 3N/4.  With k2
+// unrolled, both the kept set and p are known at compile time: no per-output
+// range checks, and the outputs nobody uses are never computed.  live(line)
+// false skips a line in both steps (padded coils, columns past the image).
+// emit(p, slot, line, v): slot = N2 k1 + k2 is the column step B read the
+// output's inputs from (the caller may overwrite it).
+template <int N1, int N2, int kBarId = 0, typename Live, typename Emit>
+__device__ __forceinline__ void fft_two_step_half(float2* smem, int lg_lines, const float2* __restrict__ tw, int tid,
+                                                  int nthreads, Live&& live, Emit&& emit) {
+  static_assert(N2 % 4 == 0, "the kept quarter-bands split on k2");
+  constexpr int kN = N1 * N2;
+  const int lines = 1 << lg_lines;
+  for (int u = tid; u < N2 * lines; u += nthreads) {
+    const int line = u & (lines - 1), n2 = u >> lg_lines;
+    if (!live(line)) continue;
+    float2* e = smem + (n2 << lg_lines) + line;
+    float2 v[N1];
+#pragma unroll
+    for (int n1 = 0; n1 < N1; ++n1) v[n1] = e[(N2 * n1) << lg_lines];
+    dft_reg<N1>(v);
+#pragma unroll
+    for (int k1 = 1; k1 < N1; ++k1) v[k1] = cmul(v[k1], tw[n2 * k1]);
+#pragma unroll
+    for (int k1 = 0; k1 < N1; ++k1) e[(N2 * k1) << lg_lines] = v[k1];
+  }
+  if constexpr (kBarId == 0)
+    __syncthreads();
+  else
+    asm volatile("bar.sync %0, %1;" ::"n"(kBarId), "r"(nthreads) : "memory");
+  for (int u = tid; u < N1 * lines; u += nthreads) {
+    const int line = u & (lines - 1), k1 = u >> lg_lines;
+    if (!live(line)) continue;
+    const float2* e = smem + ((N2 * k1) << lg_lines) + line;
+    float2 v[N2];
+#pragma unroll
+    for (int n2 = 0; n2 < N2; ++n2) v[n2] = e[n2 << lg_lines];
+    dft_reg<N2>(v);
+#pragma unroll
+    for (int k2 = 0; k2 < N2; ++k2) {
+      if (k2 < N2 / 4)
+        emit(k1 + N1 * k2 + kN / 4, N2 * k1 + k2, line, v[k2]);
+      else if (k2 >= 3 * N2 / 4)
+        emit(k1 + N1 * k2 - 3 * kN / 4, N2 * k1 + k2, line, v[k2]);
+    }
+  }
+}
+
 // Row lengths up to kMaxN with a two-step form (N1 = 16): false for any other n.
 template <int kMaxN, int kBarId = 0, typename Emit>
 __device__ __forceinline__ bool fft_two_step_rows(int n, float2* smem, int lg_lines, const float2* tw, int tid,

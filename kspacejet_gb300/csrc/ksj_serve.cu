@@ -62,10 +62,11 @@ struct Buffer {
 struct Slot {
   cudaStream_t stream = nullptr;
   cudaEvent_t start = nullptr, copied = nullptr, computed = nullptr, done = nullptr;  // timing events of a batch
-  Buffer kspace, traj, out, workspace, counts;  // device
+  Buffer kspace, out, workspace, counts;  // device: copied inputs (packed), images, workspace, per-frame table
   Buffer pin_in, pin_out, pin_meta;             // pinned host: pageable inputs, pageable outputs, counts + flags
   std::vector<Ticket*> batch;                    // in frame order; empty = free
   std::vector<size_t> out_staged;                // per request: offset in pin_out, or SIZE_MAX (direct)
+  const uint32_t* flags = nullptr;               // per-frame check flags, in pin_meta
   uint64_t bytes = 0;
   uint32_t frames = 0;
 };
@@ -142,7 +143,7 @@ uint64_t batch_bytes(const ksj_serve_request& r, uint32_t frames, uint32_t chann
   const size_t ws = ksj_gpu_gridding_workspace_bytes(&d);
   if (ws == 0) return 0;
   return ws + uint64_t{frames} * channels * samples * 8 + uint64_t{frames} * samples * 8 +
-         uint64_t{frames} * frame_out_bytes(r, channels) + uint64_t{frames} * 8;
+         uint64_t{frames} * frame_out_bytes(r, channels) + uint64_t{frames} * 28;
 }
 
 }  // namespace
@@ -150,6 +151,7 @@ uint64_t batch_bytes(const ksj_serve_request& r, uint32_t frames, uint32_t chann
 struct ksj_serve {
   ksj_serve_config cfg{};
   uint32_t max_batch = kDefaultBatchFrames;
+  bool in_place = false;  // read page-locked inputs in place instead of copying them
   std::mutex mu;
   std::condition_variable work_cv, done_cv;
   std::deque<Ticket*> pending;
@@ -176,56 +178,81 @@ struct ksj_serve {
   void fail_batch(const std::vector<Ticket*>& batch, ksj_gpu_status status);
 };
 
+// The device-readable address of host or device memory `p` (page-locked,
+// mapped host memory or device memory), or null when the device cannot read
+// it (pageable host memory).
+const void* device_address(const void* p) {
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) return p;
+  if (a.type == cudaMemoryTypeHost && a.devicePointer != nullptr) return a.devicePointer;
+  return nullptr;
+}
+
 bool ksj_serve::launch(Slot& slot, const std::vector<Ticket*>& batch, uint32_t cmax, uint32_t mmax) {
   const ksj_serve_request& r0 = batch.front()->req;
   const uint32_t nf = static_cast<uint32_t>(batch.size());
   const ksj_gpu_gridding_desc d = make_desc(r0, nf, cmax, mmax);
   const size_t ws = ksj_gpu_gridding_workspace_bytes(&d);
   const size_t flags_at = ksj_gpu_gridding_frame_flags_offset(&d);
-  const size_t frame_k = size_t{cmax} * mmax * 8;
-  const size_t frame_t = size_t{mmax} * 8;
   const size_t frame_o = frame_out_bytes(r0, cmax);
-  size_t stage_in = 0, stage_out = 0;
-  for (const Ticket* t : batch) {
-    if (!(t->req.flags & KSJ_SERVE_HOST_PINNED)) {
-      stage_in += size_t{t->req.channels} * t->req.samples * 8 + size_t{t->req.samples} * 8;
-      stage_out += out_bytes(t->req);
-    }
-  }
-  if (ws == 0 || !ensure_device(slot.kspace, nf * frame_k) || !ensure_device(slot.traj, nf * frame_t) ||
-      !ensure_device(slot.out, nf * frame_o) || !ensure_device(slot.workspace, ws) ||
-      !ensure_device(slot.counts, size_t{nf} * 8) || !ensure_pinned(slot.pin_in, stage_in + 16) ||
-      !ensure_pinned(slot.pin_out, stage_out + 16) || !ensure_pinned(slot.pin_meta, size_t{nf} * 12))
-    return false;
-  // per-frame coil and sample counts, then (after the call) the frame flags
-  uint32_t* meta = static_cast<uint32_t*>(slot.pin_meta.p);
-  for (uint32_t f = 0; f < nf; ++f) {
-    meta[f] = batch[f]->req.channels;
-    meta[nf + f] = batch[f]->req.samples;
-  }
-  if (cudaEventRecord(slot.start, slot.stream) != cudaSuccess ||
-      cudaMemcpyAsync(slot.counts.p, meta, size_t{nf} * 8, cudaMemcpyHostToDevice, slot.stream) != cudaSuccess)
-    return false;
-  char* stage = static_cast<char*>(slot.pin_in.p);
+  // where each request's inputs are read from: in place (mapped page-locked
+  // memory, when the loop reads inputs in place), through the slot's
+  // page-locked staging (pageable memory), and copied to the slot's device
+  // buffer unless read in place
+  std::vector<const void*> k_dev(nf, nullptr), t_dev(nf, nullptr);
+  size_t stage_in = 0, stage_out = 0, packed = 0;
   for (uint32_t f = 0; f < nf; ++f) {
     const ksj_serve_request& r = batch[f]->req;
-    const bool pinned = (r.flags & KSJ_SERVE_HOST_PINNED) != 0;
     const size_t kb = size_t{r.channels} * r.samples * 8, tb = size_t{r.samples} * 8;
-    const void* k_src = r.kspace;
-    const void* t_src = r.trajectory;
-    if (!pinned) {
-      std::memcpy(stage, r.kspace, kb);
-      std::memcpy(stage + kb, r.trajectory, tb);
-      k_src = stage;
-      t_src = stage + kb;
-      stage += kb + tb;
+    if (in_place) {
+      k_dev[f] = device_address(r.kspace);
+      if (r.trajectory_id == 0) t_dev[f] = device_address(r.trajectory);
     }
-    // k-space rows (channels) at the call's sample pitch
-    char* k_dst = static_cast<char*>(slot.kspace.p) + f * frame_k;
-    if (cudaMemcpy2DAsync(k_dst, size_t{mmax} * 8, k_src, size_t{r.samples} * 8, size_t{r.samples} * 8, r.channels,
-                          cudaMemcpyHostToDevice, slot.stream) != cudaSuccess)
-      return false;
-    char* t_dst = static_cast<char*>(slot.traj.p) + f * frame_t;
+    if (k_dev[f] == nullptr) stage_in += kb;
+    if (r.trajectory_id == 0 && t_dev[f] == nullptr) stage_in += tb;
+    if (!in_place) packed += kb + tb;
+    if (!(r.flags & KSJ_SERVE_HOST_PINNED)) stage_out += out_bytes(r);
+  }
+  const size_t meta_bytes = size_t{nf} * (4 + 4 + 8 + 8 + 4) + 16;
+  if (ws == 0 || !ensure_device(slot.kspace, packed + 16) || !ensure_device(slot.out, nf * frame_o) ||
+      !ensure_device(slot.workspace, ws) || !ensure_device(slot.counts, meta_bytes) ||
+      !ensure_pinned(slot.pin_in, stage_in + 16) || !ensure_pinned(slot.pin_out, stage_out + 16) ||
+      !ensure_pinned(slot.pin_meta, meta_bytes))
+    return false;
+  // per frame: coils, samples, k-space address, trajectory address (then,
+  // after the call, the frame's check flags)
+  uint32_t* counts = static_cast<uint32_t*>(slot.pin_meta.p);
+  uint64_t* addr = reinterpret_cast<uint64_t*>(static_cast<char*>(slot.pin_meta.p) + ((size_t{nf} * 8 + 15) & ~size_t{15}));
+  uint32_t* flags = reinterpret_cast<uint32_t*>(addr + 2 * nf);
+  if (cudaEventRecord(slot.start, slot.stream) != cudaSuccess) return false;
+  char* stage = static_cast<char*>(slot.pin_in.p);
+  char* dev = static_cast<char*>(slot.kspace.p);
+  auto place = [&](const void* src, size_t bytes, const void* in_place_addr) -> const void* {
+    if (in_place_addr != nullptr) return in_place_addr;
+    const void* from = src;
+    if (device_address(src) == nullptr) {  // pageable: through the page-locked staging
+      std::memcpy(stage, src, bytes);
+      from = stage;
+      stage += (bytes + 15) & ~size_t{15};
+      if (in_place) return device_address(from);
+    }
+    if (cudaMemcpyAsync(dev, from, bytes, cudaMemcpyHostToDevice, slot.stream) != cudaSuccess) return nullptr;
+    const void* at = dev;
+    dev += (bytes + 255) & ~size_t{255};
+    return at;
+  };
+  for (uint32_t f = 0; f < nf; ++f) {
+    const ksj_serve_request& r = batch[f]->req;
+    const size_t kb = size_t{r.channels} * r.samples * 8, tb = size_t{r.samples} * 8;
+    counts[f] = r.channels;
+    counts[nf + f] = r.samples;
+    const void* k_at = place(r.kspace, kb, k_dev[f]);
+    if (k_at == nullptr) return false;
+    const void* t_at = nullptr;
     if (r.trajectory_id != 0) {
       auto it = trajectories.find(r.trajectory_id);
       if (it == trajectories.end()) {
@@ -237,23 +264,30 @@ bool ksj_serve::launch(Slot& slot, const std::vector<Ticket*>& batch, uint32_t c
           if (tr.d) cudaFree(tr.d);
           return false;
         }
-        if (cudaMemcpyAsync(tr.d, t_src, tb, cudaMemcpyHostToDevice, slot.stream) != cudaSuccess ||
+        if (cudaMemcpyAsync(tr.d, r.trajectory, tb, cudaMemcpyHostToDevice, slot.stream) != cudaSuccess ||
             cudaEventRecord(tr.ready, slot.stream) != cudaSuccess)
           return false;
         it = trajectories.emplace(r.trajectory_id, tr).first;
       } else if (it->second.bytes != tb || cudaStreamWaitEvent(slot.stream, it->second.ready, 0) != cudaSuccess) {
         return false;  // an id names one trajectory: a different sample count is an error
       }
-      if (cudaMemcpyAsync(t_dst, it->second.d, tb, cudaMemcpyDeviceToDevice, slot.stream) != cudaSuccess) return false;
-    } else if (cudaMemcpyAsync(t_dst, t_src, tb, cudaMemcpyHostToDevice, slot.stream) != cudaSuccess) {
-      return false;
+      t_at = it->second.d;
+    } else {
+      t_at = place(r.trajectory, tb, t_dev[f]);
     }
+    if (t_at == nullptr) return false;
+    addr[f] = reinterpret_cast<uint64_t>(k_at);
+    addr[nf + f] = reinterpret_cast<uint64_t>(t_at);
   }
-  const uint32_t* counts = static_cast<const uint32_t*>(slot.counts.p);
+  const size_t addr_off = reinterpret_cast<char*>(addr) - static_cast<char*>(slot.pin_meta.p);
+  if (cudaMemcpyAsync(slot.counts.p, slot.pin_meta.p, addr_off + size_t{nf} * 16, cudaMemcpyHostToDevice,
+                      slot.stream) != cudaSuccess)
+    return false;
+  const uint32_t* d_counts = static_cast<const uint32_t*>(slot.counts.p);
+  const uint64_t* d_addr = reinterpret_cast<const uint64_t*>(static_cast<const char*>(slot.counts.p) + addr_off);
   if (cudaEventRecord(slot.copied, slot.stream) != cudaSuccess ||
-      ksj_gpu_gridding_adjoint_ragged(&d, nullptr, counts, counts + nf, slot.kspace.p,
-                                      static_cast<const float*>(slot.traj.p), nullptr, slot.out.p, slot.workspace.p,
-                                      slot.workspace.cap, slot.stream) != KSJ_GPU_OK ||
+      ksj_gpu_gridding_adjoint_ragged(&d, nullptr, d_counts, d_counts + nf, d_addr, d_addr + nf, slot.out.p,
+                                      slot.workspace.p, slot.workspace.cap, slot.stream) != KSJ_GPU_OK ||
       cudaEventRecord(slot.computed, slot.stream) != cudaSuccess)
     return false;
   // results (a coil-major frame's first `channels` coils are contiguous),
@@ -274,10 +308,11 @@ bool ksj_serve::launch(Slot& slot, const std::vector<Ticket*>& batch, uint32_t c
                         slot.stream) != cudaSuccess)
       return false;
   }
-  if (cudaMemcpyAsync(meta + 2 * nf, static_cast<const char*>(slot.workspace.p) + flags_at, size_t{nf} * 4,
+  if (cudaMemcpyAsync(flags, static_cast<const char*>(slot.workspace.p) + flags_at, size_t{nf} * 4,
                       cudaMemcpyDeviceToHost, slot.stream) != cudaSuccess ||
       cudaEventRecord(slot.done, slot.stream) != cudaSuccess)
     return false;
+  slot.flags = flags;
   slot.batch = batch;
   slot.frames = nf;
   return true;
@@ -295,7 +330,6 @@ void ksj_serve::fail_batch(const std::vector<Ticket*>& batch, ksj_gpu_status sta
 
 void ksj_serve::retire(Slot& slot) {
   const uint32_t nf = slot.frames;
-  const uint32_t* meta = static_cast<const uint32_t*>(slot.pin_meta.p);
   const auto now = Clock::now();
   for (uint32_t f = 0; f < nf; ++f) {
     Ticket* t = slot.batch[f];
@@ -313,7 +347,7 @@ void ksj_serve::retire(Slot& slot) {
   copy_out_ms += t_out;
   for (uint32_t f = 0; f < nf; ++f) {
     Ticket* t = slot.batch[f];
-    t->result = meta[2 * nf + f] == 0 ? KSJ_GPU_OK : KSJ_GPU_ERROR_NONFINITE_INPUT;
+    t->result = slot.flags[f] == 0 ? KSJ_GPU_OK : KSJ_GPU_ERROR_NONFINITE_INPUT;
     t->done = true;
     if (t->result == KSJ_GPU_OK) {
       ++completed;
@@ -415,7 +449,7 @@ void ksj_serve::run() {
   }
   for (Slot& s : slots) {
     if (s.stream) cudaStreamSynchronize(s.stream);
-    for (Buffer* b : {&s.kspace, &s.traj, &s.out, &s.workspace, &s.counts})
+    for (Buffer* b : {&s.kspace, &s.out, &s.workspace, &s.counts})
       if (b->p) cudaFree(b->p);
     for (Buffer* b : {&s.pin_in, &s.pin_out, &s.pin_meta})
       if (b->p) cudaFreeHost(b->p);
@@ -442,6 +476,8 @@ extern "C" ksj_gpu_status ksj_serve_create(const ksj_serve_config* config, ksj_s
   if (config->struct_size >= offsetof(ksj_serve_config, max_batch_frames) + sizeof(uint32_t) &&
       config->max_batch_frames != 0)
     s->max_batch = std::min<uint32_t>(config->max_batch_frames, 1024);
+  if (config->struct_size >= offsetof(ksj_serve_config, read_inputs_in_place) + sizeof(uint32_t))
+    s->in_place = config->read_inputs_in_place != 0;
   s->worker = std::thread([s] { s->run(); });
   {
     std::unique_lock<std::mutex> lock(s->mu);

@@ -114,14 +114,33 @@ def test_requests_batch_into_ragged_calls_and_equal_alone():
     assert st["completed"] == len(reqs) and st["failed"] == 0
     assert st["batched_frames"] == len(reqs)
     assert st["batches"] < len(reqs), st
+    # the same with page-locked inputs read in place by the kernels (and the
+    # pageable ones staged in page-locked memory first)
+    pinned = []
+    for r in reqs:
+        ks = torch.from_numpy(r.kspace).pin_memory()
+        tr = torch.from_numpy(r.trajectory).pin_memory()
+        dt = torch.float32 if r.output == serve.OUTPUT_RSS else torch.complex64
+        out = torch.empty(r.output_shape(), dtype=dt).pin_memory()
+        q = serve.Request(image=r.image, grid=r.grid, kspace=ks.numpy(), trajectory=tr.numpy(), output=r.output,
+                          pinned=True, out=out.numpy())
+        q._keep = (ks, tr, out)
+        pinned.append(q)
+    with serve.Server(slots=2, max_batch_frames=8, read_inputs_in_place=True) as s:
+        tickets = [s.submit(r) for r in pinned + reqs[:3]]
+        in_place = [s.wait(t, timeout_ms=60000).copy() for t in tickets]
+        assert s.stats()["failed"] == 0
     with serve.Server(slots=1, max_batch_frames=1) as s:
         tickets = [s.submit(r) for r in reqs]
         serial = [s.wait(t, timeout_ms=60000).copy() for t in tickets]
         assert s.stats()["batches"] == len(reqs)
-    for r, got, one in zip(reqs, outs, serial):
+    for i, (r, got, one) in enumerate(zip(reqs, outs, serial)):
         want = _alone(r)
         assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
         assert np.array_equal(one.view(np.uint32), want.view(np.uint32))
+        assert np.array_equal(in_place[i].view(np.uint32), want.view(np.uint32))
+        if i < 3:
+            assert np.array_equal(in_place[len(reqs) + i].view(np.uint32), want.view(np.uint32))
 
 
 def test_bad_request_fails_alone_in_its_batch():
