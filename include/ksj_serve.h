@@ -6,7 +6,8 @@
  * A scheduler thread keeps up to `slots` batches in flight, each on its own
  * CUDA stream with grow-only device buffers.  Whenever a slot is free, the
  * oldest pending request opens a batch and the later pending requests of its
- * class (grid, image, kernel width, DCF mode, output form) join it in
+ * class (grid, image, kernel width, DCF mode, output form, and optionally
+ * whether it has at most coil_split coils) join it in
  * arrival order, up to max_batch_frames requests and as long as the device
  * bytes of everything in flight stay within the configured cap.  A batch is
  * ONE ragged multi-frame reconstruction (ksj_gpu_gridding_adjoint_ragged:
@@ -54,6 +55,8 @@ typedef struct ksj_serve_config {
   uint32_t read_inputs_in_place; /* nonzero: page-locked, mapped inputs are read by the kernels across the
                                     host link where they are, with no copy (pageable ones are staged in
                                     page-locked memory first); 0: inputs are copied to the device */
+  uint32_t coil_split;         /* nonzero: requests of at most this many coils form their own batches */
+  uint32_t reserved0;
 } ksj_serve_config;
 
 #define KSJ_SERVE_OUTPUT_RSS 1u         /* float32 [image][image] */

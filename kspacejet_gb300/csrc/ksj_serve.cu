@@ -103,10 +103,13 @@ bool ensure_pinned(Buffer& b, size_t bytes) {
   return true;
 }
 
-// Requests of one class share a ragged call.
-using ClassKey = std::tuple<uint32_t, uint32_t, uint32_t, uint32_t, uint32_t>;
-ClassKey class_of(const ksj_serve_request& r) {
-  return {r.grid, r.image, r.kernel_width, r.dcf_mode, r.output};
+// Requests of one class share a ragged call.  With a coil split, requests
+// of at most `split` coils batch apart from larger ones: a ragged call's
+// per-frame work (the coil lines of the transforms, the lanes of the
+// gridding) follows its largest coil count.
+using ClassKey = std::tuple<uint32_t, uint32_t, uint32_t, uint32_t, uint32_t, bool>;
+ClassKey class_of(const ksj_serve_request& r, uint32_t split) {
+  return {r.grid, r.image, r.kernel_width, r.dcf_mode, r.output, split != 0 && r.channels <= split};
 }
 
 ksj_gpu_gridding_desc make_desc(const ksj_serve_request& r, uint32_t frames, uint32_t channels, uint32_t samples) {
@@ -152,6 +155,7 @@ struct ksj_serve {
   ksj_serve_config cfg{};
   uint32_t max_batch = kDefaultBatchFrames;
   bool in_place = false;  // read page-locked inputs in place instead of copying them
+  uint32_t coil_split = 0;  // requests of at most this many coils batch apart (0: no split)
   std::mutex mu;
   std::condition_variable work_cv, done_cv;
   std::deque<Ticket*> pending;
@@ -403,12 +407,12 @@ void ksj_serve::run() {
         std::lock_guard<std::mutex> lock(mu);
         if (free_slot == nullptr || pending.empty()) break;
         const ksj_serve_request& head = pending.front()->req;
-        const ClassKey key = class_of(head);
+        const ClassKey key = class_of(head, coil_split);
         // the head first, then its class's later requests in arrival order,
         // while the batch stays within its frame limit and the device cap
         for (auto it = pending.begin(); it != pending.end() && batch.size() < max_batch; ++it) {
           const ksj_serve_request& r = (*it)->req;
-          if (class_of(r) != key) continue;
+          if (class_of(r, coil_split) != key) continue;
           const uint32_t c = std::max(cmax, r.channels), m = std::max(mmax, r.samples);
           const uint64_t b = batch_bytes(head, static_cast<uint32_t>(batch.size() + 1), c, m);
           if (b == 0 || in_flight_bytes + b > cfg.device_memory_cap) {
@@ -478,6 +482,8 @@ extern "C" ksj_gpu_status ksj_serve_create(const ksj_serve_config* config, ksj_s
     s->max_batch = std::min<uint32_t>(config->max_batch_frames, 1024);
   if (config->struct_size >= offsetof(ksj_serve_config, read_inputs_in_place) + sizeof(uint32_t))
     s->in_place = config->read_inputs_in_place != 0;
+  if (config->struct_size >= offsetof(ksj_serve_config, coil_split) + sizeof(uint32_t))
+    s->coil_split = config->coil_split;
   s->worker = std::thread([s] { s->run(); });
   {
     std::unique_lock<std::mutex> lock(s->mu);

@@ -26,7 +26,8 @@ class ServeConfig(ctypes.Structure):
     _fields_ = [("struct_size", ctypes.c_uint32), ("device", ctypes.c_int32), ("slots", ctypes.c_uint32),
                 ("max_channels", ctypes.c_uint32), ("device_memory_cap", ctypes.c_uint64),
                 ("max_frame_bytes", ctypes.c_uint64), ("max_image_bytes", ctypes.c_uint64),
-                ("max_batch_frames", ctypes.c_uint32), ("read_inputs_in_place", ctypes.c_uint32)]
+                ("max_batch_frames", ctypes.c_uint32), ("read_inputs_in_place", ctypes.c_uint32),
+                ("coil_split", ctypes.c_uint32), ("reserved0", ctypes.c_uint32)]
 
 
 class ServeRequest(ctypes.Structure):
@@ -100,10 +101,11 @@ class Request:
 class Server:
     def __init__(self, slots: int = 4, device_memory_cap: int = 16 << 30, max_channels: int = 32,
                  max_frame_bytes: int = 256 << 20, max_image_bytes: int = 128 << 20, device: int = 0,
-                 max_batch_frames: int = 0, read_inputs_in_place: bool = False):
+                 max_batch_frames: int = 0, read_inputs_in_place: bool = False, coil_split: int = 0):
         self._L = _lib()
         cfg = ServeConfig(ctypes.sizeof(ServeConfig), device, slots, max_channels, device_memory_cap,
-                          max_frame_bytes, max_image_bytes, max_batch_frames, int(read_inputs_in_place))
+                          max_frame_bytes, max_image_bytes, max_batch_frames, int(read_inputs_in_place),
+                          coil_split, 0)
         h = ctypes.c_void_p()
         gpu._check(self._L.ksj_serve_create(ctypes.byref(cfg), ctypes.byref(h)), "serve_create")
         self._h = h
