@@ -808,172 +808,189 @@ def run_rows(args) -> list[dict]:
     w, s = max(args.warmup, 3), args.steps
     lines = []
 
-    # Pipe-Menon density weights: the batched workload's trajectories (96 x 34 x 384, grid 384, W=4)
-    traj = np.stack([synth.golden_angle_radial(READOUT, SPOKES, first_spoke=SPOKES * f) for f in range(FRAMES)])
-    t = torch.from_numpy(traj).to(dev)
-    ms = _time_gpu(lambda: gpu.pipe_menon_dcf(t, IMAGE, GRID, width=WIDTH, iterations=10), w, s)
-    m = traj.shape[0] * traj.shape[1]
-    lines.append({"metric": "Pipe-Menon weights: sample-iterations/s", "value": m * 10 / (ms / 1e3),
-                  "unit": "sample-iterations/s", "ms_per_call": ms, "dtype": "f64",
-                  "config": {"workload": f"{FRAMES} frames x {SPOKES} spokes x {READOUT}, grid {GRID}, KB W={WIDTH}, "
-                                         "10 iterations", "samples": m}})
+    only = set(filter(None, (args.only or "").split(",")))
 
-    # coil covariance and compression: config 4 shape, 512 readout x 805 spokes, 32 -> 8 channels
+    def want(name: str) -> bool:
+        return not only or name in only
+
     mm = 512 * 805
     rng = np.random.default_rng(3)
-    x = torch.from_numpy((rng.standard_normal((32, mm)) + 1j * rng.standard_normal((32, mm))).astype(np.complex64)).to(dev)
-    ws = torch.empty(gpu.lib().ksj_gpu_coil_covariance_workspace_bytes(32, mm), dtype=torch.uint8, device=dev)
-    cov = torch.empty((32, 32), dtype=torch.complex64, device=dev)
     L = gpu.lib()
+    x = None
+    if want("coil") or want("noise"):
+        x = torch.from_numpy((rng.standard_normal((32, mm)) + 1j * rng.standard_normal((32, mm))).astype(np.complex64)).to(dev)
+    g3, n3 = args.grid3, args.grid3 * 2 // 3
 
-    def covariance():
-        gpu._check(L.ksj_gpu_coil_covariance(32, mm, x.data_ptr(), cov.data_ptr(), ws.data_ptr(), ws.numel(),
-                                             torch.cuda.current_stream().cuda_stream), "coil_covariance")
-
-    gpu.timing_reset()
-    gpu.timing_enable(True)
-    ms = _time_gpu(covariance, w, s)
-    kern = {n: (c, t_) for n, c, t_ in gpu.timing_read()}
-    gpu.timing_enable(False)
-    mma_ms = kern["k_cov_mma"][1] / kern["k_cov_mma"][0]
-    kpad = (mm + 63) // 64 * 64
-    tensor_flops = 2.0 * 128 * 64 * kpad  # one M=128 N=64 contraction over the padded samples
-    lines.append({"metric": "coil covariance (tcgen05 split-BF16): samples/s", "value": mm / (ms / 1e3),
-                  "unit": "samples/s", "ms_per_call": ms, "dtype": "bf16 x3 split, f32 accumulate",
-                  "config": {"workload": "32 coils x 512 x 805 samples (complex64)"},
-                  "kernels_ms": {k: round(v[1] / v[0], 4) for k, v in kern.items()},
-                  "roofline": {"bound": "tensor", "kernel": "k_cov_mma",
-                               "achieved": round(tensor_flops / (mma_ms / 1e3) / 1e12, 2),
-                               "peak": bf16, "unit": "TFLOP/s", "frac": round(tensor_flops / (mma_ms / 1e3) / 1e12 / bf16, 4),
-                               "note": "the contraction is HBM-bound: 128 x 64 outputs per 64-sample tile"},
-                  "hbm": {"bytes": 3 * 32 * mm * 8, "GBps": round(3 * 32 * mm * 8 / (ms / 1e3) / 1e9, 1),
-                          "frac": round(3 * 32 * mm * 8 / (ms / 1e3) / 1e9 / hbm, 4)}})
-    basis, _ = gpu.compression_basis(cov.cpu().numpy(), 8)
-    bd = torch.from_numpy(basis).to(dev)
-    y = torch.empty((8, mm), dtype=torch.complex64, device=dev)
-
-    def compress():
-        gpu._check(L.ksj_gpu_coil_compress(32, 8, mm, bd.data_ptr(), x.data_ptr(), y.data_ptr(),
-                                           torch.cuda.current_stream().cuda_stream), "coil_compress")
-
-    ms = _time_gpu(compress, w, s)
-    byts = (32 + 8) * mm * 8
-    lines.append({"metric": "coil compression 32->8: samples/s", "value": mm / (ms / 1e3), "unit": "samples/s",
-                  "ms_per_call": ms, "dtype": "f32",
-                  "roofline": {"bound": "hbm", "achieved": round(byts / (ms / 1e3) / 1e9, 1), "peak": hbm,
-                               "unit": "GB/s", "frac": round(byts / (ms / 1e3) / 1e9 / hbm, 4)}})
-
-    # noise model from 32 x 65536 noise samples (covariance on the tensor cores, eigensolve on the
-    # host) and prewhitening Y = W X of the same 32 x 412 160 k-space
-    mn = 65536
-    noise = torch.from_numpy((rng.standard_normal((32, mn)) + 1j * rng.standard_normal((32, mn))).astype(np.complex64)).to(dev)
-    ms = _time_gpu(lambda: gpu.noise_model(noise), w, s)
-    lines.append({"metric": "noise model estimate: noise samples/s", "value": mn / (ms / 1e3), "unit": "samples/s",
-                  "ms_per_call": ms, "dtype": "bf16 x3 split covariance, f64 host eigensolve",
-                  "config": {"workload": "32 coils x 65536 noise samples, whitening matrix to the device"}})
-    wd = gpu.noise_model(noise)
-    yw = torch.empty((32, mm), dtype=torch.complex64, device=dev)
-
-    def prewhiten():
-        gpu._check(L.ksj_gpu_noise_prewhiten(32, mm, wd.data_ptr(), x.data_ptr(), yw.data_ptr(),
-                                             torch.cuda.current_stream().cuda_stream), "noise_prewhiten")
-
-    ms = _time_gpu(prewhiten, w, s)
-    byts = 2 * 32 * mm * 8
-    lines.append({"metric": "noise prewhitening 32x32: samples/s", "value": mm / (ms / 1e3), "unit": "samples/s",
-                  "ms_per_call": ms, "dtype": "f32",
-                  "config": {"workload": "32 coils x 512 x 805 samples (complex64)"},
-                  "roofline": {"bound": "hbm", "achieved": round(byts / (ms / 1e3) / 1e9, 1), "peak": hbm,
-                               "unit": "GB/s", "frac": round(byts / (ms / 1e3) / 1e9 / hbm, 4)}})
-
-    # 3-D kooshball: 256 readout x `spokes3` Fibonacci spokes, 20 coils, grid 384^3 (sigma 1.5), KB W=4,
-    # |k|^2 density weights, RSS; complex64 and bf16 sample storage
-    if args.spokes3 > 0:
-        tr3 = torch.from_numpy(synth.kooshball(256, args.spokes3)).to(dev)
-        m3 = tr3.shape[0]
-        gen = torch.Generator(device=dev).manual_seed(5)
-        k3 = torch.randn((20, m3), dtype=torch.complex64, device=dev, generator=gen)
-        for fmt, name in ((gpu.SAMPLES_CF32, "complex64"), (gpu.SAMPLES_BF16, "bf16")):
-            g3 = gpu.Gridding3(image=256, grid=384, channels=20, samples=m3, width=4, dcf=gpu.DCF_ANALYTIC_RAMP,
-                               output=gpu.OUTPUT_RSS, sample_format=fmt)
-            kin = k3 if fmt == gpu.SAMPLES_CF32 else torch.stack([k3.real.to(torch.bfloat16),
-                                                                  k3.imag.to(torch.bfloat16)], dim=-1).contiguous()
-            ws3 = g3.new_workspace(dev)
-            o3 = g3.new_output(dev)
-            gpu.timing_reset()
-            gpu.timing_enable(True)
-            ms = _time_gpu(lambda: g3.run(kin, tr3, o3, ws3), 1, max(1, min(s, 3)))
-            kern = {n_: round(t_ / c_, 3) for n_, c_, t_ in gpu.timing_read()}
-            gpu.timing_enable(False)
-            lines.append({"metric": "3-D kooshball gridded samples/s", "value": 20 * m3 / (ms / 1e3),
-                          "unit": "samples/s", "ms_per_call": ms, "dtype": f"f32 ({name} sample storage)",
-                          "config": {"workload": f"256 x {args.spokes3} spokes kooshball, 20 coils, grid 384^3, "
-                                                 "KB W=4, sigma 1.5, |k|^2 DCF, RSS", "gridded_samples": 20 * m3,
-                                     "workspace_bytes": ws3.numel()},
-                          "kernels_ms": kern})
-            del ws3, o3
-        # 3-D Pipe-Menon weights for the same trajectory (FP64, 10 iterations)
-        ms = _time_gpu(lambda: gpu.pipe_menon_dcf3(tr3, 256, 384, width=4, iterations=10), 1, max(1, min(s, 3)))
-        lines.append({"metric": "3-D Pipe-Menon weights: sample-iterations/s", "value": m3 * 10 / (ms / 1e3),
+    if want("pipe_menon"):
+        # Pipe-Menon density weights: the batched workload's trajectories (96 x 34 x 384, grid 384, W=4)
+        traj = np.stack([synth.golden_angle_radial(READOUT, SPOKES, first_spoke=SPOKES * f) for f in range(FRAMES)])
+        t = torch.from_numpy(traj).to(dev)
+        ms = _time_gpu(lambda: gpu.pipe_menon_dcf(t, IMAGE, GRID, width=WIDTH, iterations=10), w, s)
+        m = traj.shape[0] * traj.shape[1]
+        lines.append({"metric": "Pipe-Menon weights: sample-iterations/s", "value": m * 10 / (ms / 1e3),
                       "unit": "sample-iterations/s", "ms_per_call": ms, "dtype": "f64",
-                      "config": {"workload": f"256 x {args.spokes3} spokes kooshball, grid 384^3, KB W=4, "
-                                             "10 iterations", "samples": m3}})
+                      "config": {"workload": f"{FRAMES} frames x {SPOKES} spokes x {READOUT}, grid {GRID}, KB W={WIDTH}, "
+                                             "10 iterations", "samples": m}})
 
-    # exact direct forward NUDFT (the reference's nufft2_forward on its Eigen backend): 128^2 image,
-    # 8 coils, 34 spokes x 256 readout
-    imf = torch.from_numpy((rng.standard_normal((128, 128, 8)) + 1j * rng.standard_normal((128, 128, 8))).astype(np.complex64)).to(dev)
-    trf = torch.from_numpy(synth.golden_angle_radial(256, 34)).to(dev)
-    ms = _time_gpu(lambda: gpu.direct_forward(imf, trf), 1, max(1, min(s, 5)))
-    pairs = 128 * 128 * trf.shape[0]
-    lines.append({"metric": "direct forward NUDFT: (sample, pixel) pairs/s", "value": pairs / (ms / 1e3),
-                  "unit": "pairs/s", "ms_per_call": ms, "dtype": "f32 (exact phase per pair)",
-                  "config": {"workload": "128 x 128 image, 8 coils, 34 x 256 golden-angle samples",
-                             "complex_macs": pairs * 8}})
+    if want("coil"):
+        # coil covariance and compression: config 4 shape, 512 readout x 805 spokes, 32 -> 8 channels
+        ws = torch.empty(gpu.lib().ksj_gpu_coil_covariance_workspace_bytes(32, mm), dtype=torch.uint8, device=dev)
+        cov = torch.empty((32, 32), dtype=torch.complex64, device=dev)
 
-    # Kaiser-Bessel forward NUFFT on the batched shape: 96 frames of 192^2 x 32 coil images -> 34 x 384 samples
-    trh, _ = make_inputs()
-    trk = torch.from_numpy(trh).to(dev)
-    fop = gpu.kb_gridding(image=IMAGE, grid=GRID, channels=COILS, samples=trh.shape[1], frames=FRAMES, width=WIDTH,
-                          dcf=gpu.DCF_NONE, output=gpu.OUTPUT_COIL_LAST)
-    fimg = torch.randn((FRAMES, IMAGE, IMAGE, COILS), dtype=torch.complex64, device=dev)
-    fws = torch.empty(fop.forward_workspace_bytes(), dtype=torch.uint8, device=dev)
-    gpu.timing_reset()
-    gpu.timing_enable(True)
-    ms = _time_gpu(lambda: fop.forward(fimg, trk, fws), w, s)
-    kern = {n_: round(t_ / c_, 4) for n_, c_, t_ in gpu.timing_read()}
-    gpu.timing_enable(False)
-    lines.append({"metric": "Kaiser-Bessel forward NUFFT: samples/s", "value": FRAMES * COILS * trh.shape[1] / (ms / 1e3),
-                  "unit": "samples/s", "ms_per_call": ms, "dtype": "f32",
-                  "config": {"workload": f"{FRAMES} frames x {COILS} coils, {IMAGE}^2 images -> {SPOKES} x {READOUT} "
-                                         f"samples per frame, KB W={WIDTH}, grid {GRID}"},
-                  "kernels_ms": kern})
-    del fimg, fws
+        def covariance():
+            gpu._check(L.ksj_gpu_coil_covariance(32, mm, x.data_ptr(), cov.data_ptr(), ws.data_ptr(), ws.numel(),
+                                                 torch.cuda.current_stream().cuda_stream), "coil_covariance")
 
-    # Cartesian coil images: 8 frames x 32 coils x 256 x 256, coil-last output
-    kc = torch.from_numpy((rng.standard_normal((8, 32, 256, 256)) + 1j * rng.standard_normal((8, 32, 256, 256))).astype(np.complex64)).to(dev)
-    ms = _time_gpu(lambda: gpu.cartesian_ifft2(kc), w, s)
-    byts = 2 * kc.numel() * 8  # k-space read, coil-last images written
-    lines.append({"metric": "Cartesian coil images: images/s", "value": 8 * 32 / (ms / 1e3), "unit": "images/s",
-                  "ms_per_call": ms, "dtype": "f32",
-                  "config": {"workload": "8 frames x 32 coils x 256 x 256, inverse 2-D DFT, coil-last"},
-                  "roofline": {"bound": "hbm", "achieved": round(byts / (ms / 1e3) / 1e9, 1), "peak": hbm,
-                               "unit": "GB/s", "frac": round(byts / (ms / 1e3) / 1e9 / hbm, 4),
-                               "note": "algorithmic bytes = k-space in + images out; the transpose and the "
-                                       "row-transformed intermediate add 4 more passes"}})
-    del kc
+        gpu.timing_reset()
+        gpu.timing_enable(True)
+        ms = _time_gpu(covariance, w, s)
+        kern = {n: (c, t_) for n, c, t_ in gpu.timing_read()}
+        gpu.timing_enable(False)
+        mma_ms = kern["k_cov_mma"][1] / kern["k_cov_mma"][0]
+        kpad = (mm + 63) // 64 * 64
+        tensor_flops = 2.0 * 128 * 64 * kpad  # one M=128 N=64 contraction over the padded samples
+        lines.append({"metric": "coil covariance (tcgen05 split-BF16): samples/s", "value": mm / (ms / 1e3),
+                      "unit": "samples/s", "ms_per_call": ms, "dtype": "bf16 x3 split, f32 accumulate",
+                      "config": {"workload": "32 coils x 512 x 805 samples (complex64)"},
+                      "kernels_ms": {k: round(v[1] / v[0], 4) for k, v in kern.items()},
+                      "roofline": {"bound": "tensor", "kernel": "k_cov_mma",
+                                   "achieved": round(tensor_flops / (mma_ms / 1e3) / 1e12, 2),
+                                   "peak": bf16, "unit": "TFLOP/s", "frac": round(tensor_flops / (mma_ms / 1e3) / 1e12 / bf16, 4),
+                                   "note": "the contraction is HBM-bound: 128 x 64 outputs per 64-sample tile"},
+                      "hbm": {"bytes": 3 * 32 * mm * 8, "GBps": round(3 * 32 * mm * 8 / (ms / 1e3) / 1e9, 1),
+                              "frac": round(3 * 32 * mm * 8 / (ms / 1e3) / 1e9 / hbm, 4)}})
+        basis, _ = gpu.compression_basis(cov.cpu().numpy(), 8)
+        bd = torch.from_numpy(basis).to(dev)
+        y = torch.empty((8, mm), dtype=torch.complex64, device=dev)
 
-    # Walsh 7x7 on the compressed 8-coil image (256 x 256), and RSS of 32 coils
-    img = torch.from_numpy((rng.standard_normal((256, 256, 8)) + 1j * rng.standard_normal((256, 256, 8))).astype(np.complex64)).to(dev)
-    ms = _time_gpu(lambda: gpu.walsh_combine(img, window=7, iterations=24), w, s)
-    lines.append({"metric": "Walsh 7x7 combine: pixels/s", "value": 256 * 256 / (ms / 1e3), "unit": "pixels/s",
-                  "ms_per_call": ms, "dtype": "f32", "config": {"workload": "256 x 256 x 8 coils, 24 power iterations"}})
-    img32 = torch.from_numpy((rng.standard_normal((256, 256, 32)) + 1j * rng.standard_normal((256, 256, 32))).astype(np.complex64)).to(dev)
-    ms = _time_gpu(lambda: gpu.rss_coil_last(img32), w, s)
-    byts = 256 * 256 * (32 * 8 + 4)
-    lines.append({"metric": "RSS combine: pixels/s", "value": 256 * 256 / (ms / 1e3), "unit": "pixels/s",
-                  "ms_per_call": ms, "dtype": "f32",
-                  "roofline": {"bound": "hbm", "achieved": round(byts / (ms / 1e3) / 1e9, 1), "peak": hbm,
-                               "unit": "GB/s", "frac": round(byts / (ms / 1e3) / 1e9 / hbm, 4)}})
+        def compress():
+            gpu._check(L.ksj_gpu_coil_compress(32, 8, mm, bd.data_ptr(), x.data_ptr(), y.data_ptr(),
+                                               torch.cuda.current_stream().cuda_stream), "coil_compress")
+
+        ms = _time_gpu(compress, w, s)
+        byts = (32 + 8) * mm * 8
+        lines.append({"metric": "coil compression 32->8: samples/s", "value": mm / (ms / 1e3), "unit": "samples/s",
+                      "ms_per_call": ms, "dtype": "f32",
+                      "roofline": {"bound": "hbm", "achieved": round(byts / (ms / 1e3) / 1e9, 1), "peak": hbm,
+                                   "unit": "GB/s", "frac": round(byts / (ms / 1e3) / 1e9 / hbm, 4)}})
+
+    if want("noise"):
+        # noise model from 32 x 65536 noise samples (covariance on the tensor cores, eigensolve on the
+        # host) and prewhitening Y = W X of the same 32 x 412 160 k-space
+        mn = 65536
+        noise = torch.from_numpy((rng.standard_normal((32, mn)) + 1j * rng.standard_normal((32, mn))).astype(np.complex64)).to(dev)
+        ms = _time_gpu(lambda: gpu.noise_model(noise), w, s)
+        lines.append({"metric": "noise model estimate: noise samples/s", "value": mn / (ms / 1e3), "unit": "samples/s",
+                      "ms_per_call": ms, "dtype": "bf16 x3 split covariance, f64 host eigensolve",
+                      "config": {"workload": "32 coils x 65536 noise samples, whitening matrix to the device"}})
+        wd = gpu.noise_model(noise)
+        yw = torch.empty((32, mm), dtype=torch.complex64, device=dev)
+
+        def prewhiten():
+            gpu._check(L.ksj_gpu_noise_prewhiten(32, mm, wd.data_ptr(), x.data_ptr(), yw.data_ptr(),
+                                                 torch.cuda.current_stream().cuda_stream), "noise_prewhiten")
+
+        ms = _time_gpu(prewhiten, w, s)
+        byts = 2 * 32 * mm * 8
+        lines.append({"metric": "noise prewhitening 32x32: samples/s", "value": mm / (ms / 1e3), "unit": "samples/s",
+                      "ms_per_call": ms, "dtype": "f32",
+                      "config": {"workload": "32 coils x 512 x 805 samples (complex64)"},
+                      "roofline": {"bound": "hbm", "achieved": round(byts / (ms / 1e3) / 1e9, 1), "peak": hbm,
+                                   "unit": "GB/s", "frac": round(byts / (ms / 1e3) / 1e9 / hbm, 4)}})
+
+    if want("kooshball") and args.spokes3 > 0:
+        # 3-D kooshball: 256 readout x `spokes3` Fibonacci spokes, 20 coils, grid 384^3 (sigma 1.5), KB W=4,
+        # |k|^2 density weights, RSS; complex64 and bf16 sample storage
+        if args.spokes3 > 0:
+            tr3 = torch.from_numpy(synth.kooshball(256, args.spokes3)).to(dev)
+            m3 = tr3.shape[0]
+            gen = torch.Generator(device=dev).manual_seed(5)
+            k3 = torch.randn((20, m3), dtype=torch.complex64, device=dev, generator=gen)
+            for fmt, name in ((gpu.SAMPLES_CF32, "complex64"), (gpu.SAMPLES_BF16, "bf16")):
+                op3 = gpu.Gridding3(image=n3, grid=g3, channels=20, samples=m3, width=4, dcf=gpu.DCF_ANALYTIC_RAMP,
+                                   output=gpu.OUTPUT_RSS, sample_format=fmt)
+                kin = k3 if fmt == gpu.SAMPLES_CF32 else torch.stack([k3.real.to(torch.bfloat16),
+                                                                      k3.imag.to(torch.bfloat16)], dim=-1).contiguous()
+                ws3 = op3.new_workspace(dev)
+                o3 = op3.new_output(dev)
+                gpu.timing_reset()
+                gpu.timing_enable(True)
+                ms = _time_gpu(lambda: op3.run(kin, tr3, o3, ws3), 1, max(1, min(s, 3)))
+                kern = {n_: round(t_ / c_, 3) for n_, c_, t_ in gpu.timing_read()}
+                gpu.timing_enable(False)
+                lines.append({"metric": "3-D kooshball gridded samples/s", "value": 20 * m3 / (ms / 1e3),
+                              "unit": "samples/s", "ms_per_call": ms, "dtype": f"f32 ({name} sample storage)",
+                              "config": {"workload": f"256 x {args.spokes3} spokes kooshball, 20 coils, grid {g3}^3, "
+                                                     "KB W=4, sigma 1.5, |k|^2 DCF, RSS", "gridded_samples": 20 * m3,
+                                         "workspace_bytes": ws3.numel()},
+                              "kernels_ms": kern})
+                del ws3, o3
+            # 3-D Pipe-Menon weights for the same trajectory (FP64, 10 iterations)
+            ms = _time_gpu(lambda: gpu.pipe_menon_dcf3(tr3, n3, g3, width=4, iterations=10), 1, max(1, min(s, 3)))
+            lines.append({"metric": "3-D Pipe-Menon weights: sample-iterations/s", "value": m3 * 10 / (ms / 1e3),
+                          "unit": "sample-iterations/s", "ms_per_call": ms, "dtype": "f64",
+                          "config": {"workload": f"256 x {args.spokes3} spokes kooshball, grid {g3}^3, KB W=4, "
+                                                 "10 iterations", "samples": m3}})
+
+    if want("direct_forward"):
+        # exact direct forward NUDFT (the reference's nufft2_forward on its Eigen backend): 128^2 image,
+        # 8 coils, 34 spokes x 256 readout
+        imf = torch.from_numpy((rng.standard_normal((128, 128, 8)) + 1j * rng.standard_normal((128, 128, 8))).astype(np.complex64)).to(dev)
+        trf = torch.from_numpy(synth.golden_angle_radial(256, 34)).to(dev)
+        ms = _time_gpu(lambda: gpu.direct_forward(imf, trf), 1, max(1, min(s, 5)))
+        pairs = 128 * 128 * trf.shape[0]
+        lines.append({"metric": "direct forward NUDFT: (sample, pixel) pairs/s", "value": pairs / (ms / 1e3),
+                      "unit": "pairs/s", "ms_per_call": ms, "dtype": "f32 (exact phase per pair)",
+                      "config": {"workload": "128 x 128 image, 8 coils, 34 x 256 golden-angle samples",
+                                 "complex_macs": pairs * 8}})
+
+    if want("kb_forward"):
+        # Kaiser-Bessel forward NUFFT on the batched shape: 96 frames of 192^2 x 32 coil images -> 34 x 384 samples
+        trh, _ = make_inputs()
+        trk = torch.from_numpy(trh).to(dev)
+        fop = gpu.kb_gridding(image=IMAGE, grid=GRID, channels=COILS, samples=trh.shape[1], frames=FRAMES, width=WIDTH,
+                              dcf=gpu.DCF_NONE, output=gpu.OUTPUT_COIL_LAST)
+        fimg = torch.randn((FRAMES, IMAGE, IMAGE, COILS), dtype=torch.complex64, device=dev)
+        fws = torch.empty(fop.forward_workspace_bytes(), dtype=torch.uint8, device=dev)
+        gpu.timing_reset()
+        gpu.timing_enable(True)
+        ms = _time_gpu(lambda: fop.forward(fimg, trk, fws), w, s)
+        kern = {n_: round(t_ / c_, 4) for n_, c_, t_ in gpu.timing_read()}
+        gpu.timing_enable(False)
+        lines.append({"metric": "Kaiser-Bessel forward NUFFT: samples/s", "value": FRAMES * COILS * trh.shape[1] / (ms / 1e3),
+                      "unit": "samples/s", "ms_per_call": ms, "dtype": "f32",
+                      "config": {"workload": f"{FRAMES} frames x {COILS} coils, {IMAGE}^2 images -> {SPOKES} x {READOUT} "
+                                             f"samples per frame, KB W={WIDTH}, grid {GRID}"},
+                      "kernels_ms": kern})
+        del fimg, fws
+
+    if want("cartesian"):
+        # Cartesian coil images: 8 frames x 32 coils x 256 x 256, coil-last output
+        kc = torch.from_numpy((rng.standard_normal((8, 32, 256, 256)) + 1j * rng.standard_normal((8, 32, 256, 256))).astype(np.complex64)).to(dev)
+        ms = _time_gpu(lambda: gpu.cartesian_ifft2(kc), w, s)
+        byts = 2 * kc.numel() * 8  # k-space read, coil-last images written
+        lines.append({"metric": "Cartesian coil images: images/s", "value": 8 * 32 / (ms / 1e3), "unit": "images/s",
+                      "ms_per_call": ms, "dtype": "f32",
+                      "config": {"workload": "8 frames x 32 coils x 256 x 256, inverse 2-D DFT, coil-last"},
+                      "roofline": {"bound": "hbm", "achieved": round(byts / (ms / 1e3) / 1e9, 1), "peak": hbm,
+                                   "unit": "GB/s", "frac": round(byts / (ms / 1e3) / 1e9 / hbm, 4),
+                                   "note": "algorithmic bytes = k-space in + images out; the transpose and the "
+                                           "row-transformed intermediate add 4 more passes"}})
+        del kc
+
+    if want("combine"):
+        # Walsh 7x7 on the compressed 8-coil image (256 x 256), and RSS of 32 coils
+        img = torch.from_numpy((rng.standard_normal((256, 256, 8)) + 1j * rng.standard_normal((256, 256, 8))).astype(np.complex64)).to(dev)
+        ms = _time_gpu(lambda: gpu.walsh_combine(img, window=7, iterations=24), w, s)
+        lines.append({"metric": "Walsh 7x7 combine: pixels/s", "value": 256 * 256 / (ms / 1e3), "unit": "pixels/s",
+                      "ms_per_call": ms, "dtype": "f32", "config": {"workload": "256 x 256 x 8 coils, 24 power iterations"}})
+        img32 = torch.from_numpy((rng.standard_normal((256, 256, 32)) + 1j * rng.standard_normal((256, 256, 32))).astype(np.complex64)).to(dev)
+        ms = _time_gpu(lambda: gpu.rss_coil_last(img32), w, s)
+        byts = 256 * 256 * (32 * 8 + 4)
+        lines.append({"metric": "RSS combine: pixels/s", "value": 256 * 256 / (ms / 1e3), "unit": "pixels/s",
+                      "ms_per_call": ms, "dtype": "f32",
+                      "roofline": {"bound": "hbm", "achieved": round(byts / (ms / 1e3) / 1e9, 1), "peak": hbm,
+                                   "unit": "GB/s", "frac": round(byts / (ms / 1e3) / 1e9 / hbm, 4)}})
     return lines
 
 
@@ -991,6 +1008,9 @@ def main() -> int:
     ap.add_argument("--serve", action="store_true", help="served-stream benchmark (separate JSON line)")
     ap.add_argument("--rows", action="store_true", help="the other hot-path rows (one JSON line each)")
     ap.add_argument("--spokes3", type=int, default=40000, help="--rows: spokes of the 3-D kooshball (0 skips it)")
+    ap.add_argument("--grid3", type=int, default=384, help="--rows: grid of the 3-D kooshball (image = 2/3 of it)")
+    ap.add_argument("--only", default="", help="--rows: a comma list of rows to run (pipe_menon, coil, noise, "
+                                               "kooshball, direct_forward, kb_forward, cartesian, combine)")
     ap.add_argument("--skip-extra", action="store_true",
                     help="skip the width-6 and drop-in legs (small profiling runs)")
     ap.add_argument("--serve-requests", type=int, default=160)

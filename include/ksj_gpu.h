@@ -109,7 +109,8 @@ typedef struct ksj_gpu_gridding_tuning {
   uint32_t coil_group;      /* channels accumulated per row CTA: 1, 2, 4, 8, 16 or 32 */
   uint32_t column_block;    /* columns per column-pass tile: a power of two (1..32) */
   uint32_t list_capacity;   /* per-warp sorted-list buffer, entries (power of two, 64..2048) */
-  uint32_t frames_per_pass; /* frames per row/column pass (the row-transformed grid of one pass stays in L2) */
+  uint32_t frames_per_pass; /* frames per row/column pass; passes alternate between two streams (0: two passes
+                                once there are 4 or more frames) */
   uint32_t rows_blocks_per_sm; /* 1 or 2 resident row CTAs per SM (2 caps registers at 80 per thread) */
   uint32_t coil_parts;      /* 1 or 2: a row CTA's coil group is split into this many independent list tasks */
   uint32_t column_pass;     /* 0 heuristic, 1 one CTA per (frame, column block), 2 persistent CTAs with a

@@ -235,8 +235,12 @@ ksj_gpu_status make_shape(const ksj_gpu_gridding_desc* d, const ksj_gpu_gridding
     int want = 1;
     while (want < s->channels && want < 32) want <<= 1;
     cg = want;
-    // two row blocks per SM when they fit: (228 KiB - 2 x 1 KiB reserved) / 2
-    while (cg > 1 && rows_smem(cg) > 115712) cg >>= 1;
+    // two row blocks per SM when they fit: (228 KiB - 2 x 1 KiB reserved) / 2;
+    // rows wider than 384 columns run one 512-thread block per SM whatever
+    // the group, and there the whole 32-coil register path wins (grid 512,
+    // 32 coils: 4.8 against 8.6 ms per 16-frame call with a 16-coil group)
+    const size_t per_block = rows_threads_for(s->grid_cols) <= 384 ? 115712 : smem_limit;
+    while (cg > 1 && rows_smem(cg) > per_block) cg >>= 1;
   }
   if (cg < 1 || cg > 32 || (cg & (cg - 1)) != 0 || rows_smem(cg) > smem_limit) return KSJ_GPU_ERROR_INVALID_ARGUMENT;
   // column pass: cb columns x col_group coils per tile (a power of two
@@ -262,7 +266,9 @@ ksj_gpu_status make_shape(const ksj_gpu_gridding_desc* d, const ksj_gpu_gridding
   // struct_size covers them
   auto has = [&](size_t field_end) { return t != nullptr && t->struct_size >= field_end; };
   int fpp = has(offsetof(ksj_gpu_gridding_tuning, frames_per_pass) + 4) ? static_cast<int>(t->frames_per_pass) : 0;
-  if (fpp <= 0) fpp = s->frames;
+  // default: two passes (on two streams, so one pass's last partial wave
+  // overlaps the other) once there are enough frames to split
+  if (fpp <= 0) fpp = s->frames >= 4 ? (s->frames + 1) / 2 : s->frames;
   s->frames_per_pass = std::min(fpp, s->frames);
   int rb = has(offsetof(ksj_gpu_gridding_tuning, rows_blocks_per_sm) + 4) ? static_cast<int>(t->rows_blocks_per_sm) : 0;
   // default: two row CTAs per SM wherever the row kernel fits them (384
@@ -1076,7 +1082,7 @@ __device__ __forceinline__ void chunk_taps_wrapped(float2 (&r)[kChunk], int c0, 
 // the sum, in segment order, of its segments' partial sums, each partial sum
 // in sample order from zero.  Shorter lists are one segment: the cell is its
 // samples' sum in sample order.  Every row kernel uses the same segments.
-constexpr int kSegMin = 64;
+constexpr int kSegMin = 32;
 constexpr int kSegMax = 32;
 
 __host__ __device__ inline int list_segments(int n) {

@@ -97,7 +97,7 @@ def test_allocation_failure_fails_the_firing_and_releases_the_grant(recon, cuda)
 
 @pytest.mark.gpu
 def test_segment_wait_runs_out_and_the_call_returns(native, cuda):
-    """The row pass's per-list segment wait (lists over 64 entries are summed
+    """The row pass's per-list segment wait (lists over 32 entries are summed
     in segments that wait for their predecessors) pointed, by the test-only
     tuning field, at a count that never comes: every later segment gives up
     after 256 polls, KSJ_GPU_FLAG_WAIT_TIMEOUT comes back, the call returns,
