@@ -391,7 +391,7 @@ def width6_leg(g4_tuning_note: str, k, t, traj_h, ksp_h, dev, steps: int, warmup
     return {"kernel_width": 6, "ms_per_step": ms, "value": FRAMES * COILS * traj_h.shape[1] / (ms / 1e3),
             "unit": "samples/s", "accuracy": acc,
             "tuning": {"coil_group": tuning.coil_group, "column_block": tuning.column_block,
-                       "frames_per_pass": tuning.frames_per_pass or FRAMES,
+                       "frames_per_pass": tuning.frames_per_pass or (FRAMES + 1) // 2,
                        "rows_blocks_per_sm": tuning.rows_blocks_per_sm}}
 
 
@@ -492,7 +492,7 @@ def run_ours(args) -> dict | None:
     # pass, so no two of its launches overlap and each launch's events time it alone
     # (the tuned call may run two passes concurrently on two streams)
     tuning_k = gpu.GriddingTuning(ctypes.sizeof(gpu.GriddingTuning), tuning.coil_group, tuning.column_block,
-                                  tuning.list_capacity, 0, tuning.rows_blocks_per_sm, tuning.coil_parts,
+                                  tuning.list_capacity, FRAMES, tuning.rows_blocks_per_sm, tuning.coil_parts,
                                   tuning.column_pass)
     for _ in range(2):
         g.run(k, t, out, ws, tuning=tuning_k)
@@ -618,7 +618,8 @@ def run_ours(args) -> dict | None:
         "dtype": "f32 (complex64 samples, float32 gridding/FFT)", "data": "synthetic",
         "config": workload_config({"parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                                    "tuning": {"coil_group": tuning.coil_group, "column_block": tuning.column_block,
-                                              "frames_per_pass": tuning.frames_per_pass or FRAMES,
+                                              "frames_per_pass": tuning.frames_per_pass or
+                                              ((FRAMES + 1) // 2 if FRAMES >= 4 else FRAMES),
                                               "rows_blocks_per_sm": tuning.rows_blocks_per_sm,
                                               "coil_parts": tuning.coil_parts or 1,
                                               "column_pass": "persistent ring" if tuning.column_pass == 2

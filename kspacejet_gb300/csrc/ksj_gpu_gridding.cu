@@ -1089,6 +1089,10 @@ __host__ __device__ inline int list_segments(int n) {
   return n <= kSegMin ? 1 : ((n + kSegMin - 1) / kSegMin < kSegMax ? (n + kSegMin - 1) / kSegMin : kSegMax);
 }
 static_assert(kSegMin * kSegMax <= (1 << 22), "segment counts are taken from lengths capped at 2^22");
+// First entry (absolute, within the frame's entries) of segment seg of a
+// list starting at `begin` with segments of sl entries.
+__host__ __device__ inline int seg_start(uint32_t begin, int seg, int sl) { return static_cast<int>(begin) + seg * sl; }
+
 __host__ __device__ inline int segment_length(int n) {
   const int sg = list_segments(n);
   return (n + sg - 1) / sg;
@@ -1098,17 +1102,41 @@ __host__ __device__ inline int segment_length(int n) {
 // warp, lane = coil: the chunk's 16 cells stay in registers, summed in entry
 // order from zero.  kWrap admits entries whose taps wrap around the grid
 // inside the chunk.  `meta` is the warp's staging buffer.
+//
+// have_sk: lane i's sk_first already holds the sample index of entry i (of
+// the first batch), loaded ahead by the caller; the first samples are then
+// requested before the batch's entries are staged, so the two loads overlap
+// instead of following each other.  Within the task, each batch loads the
+// next batch's sample indices the same way (one 4-byte load per lane, which
+// also brings the next batch's entries towards L1).
 template <int W, uint32_t kFormat, bool kWrap, int kAR>
 __device__ __forceinline__ void grid_entries_regs(float2 (&r)[kChunk], const RowsArgs& a, size_t sample_base,
                                                   bool coil_ok, int lane, int col_lo, const float4* xent, int n,
-                                                  float4* meta) {
+                                                  float4* meta, bool have_sk = false, uint32_t sk_first = 0u) {
   constexpr int kMV = meta_vecs(W);
   constexpr int kBatch = meta_batch(W);
   const void* ks = a.samples_t;
 #pragma unroll
   for (int t = 0; t < kChunk; ++t) r[t] = make_float2(0.0f, 0.0f);
+  uint32_t sk_batch = sk_first;
+  bool sk_ready = have_sk;
   for (int base = 0; base < n; base += kBatch) {
     const int cnt = min(kBatch, n - base);
+    float2 yv[kAR];
+    const bool pre = sk_ready;
+    if (pre) {
+#pragma unroll
+      for (int k = 0; k < kAR; ++k) {
+        const uint32_t sk = __shfl_sync(0xffffffffu, sk_batch, k);
+        yv[k] = (coil_ok && k < cnt) ? load_sample<kFormat>(ks, sample_base + static_cast<size_t>(sk) * a.channels)
+                                     : make_float2(0.0f, 0.0f);
+      }
+    }
+    if (have_sk && base + kBatch < n) {
+      const int nb = base + kBatch;
+      sk_batch = lane < min(kBatch, n - nb) ? __float_as_uint(__ldg(&xent[static_cast<size_t>(nb + lane) * kMV].y)) : 0u;
+      sk_ready = true;
+    }
     __syncwarp();  // the previous batch is read by every lane before it is replaced
     if (lane < cnt) {
       const float4* src = xent + static_cast<size_t>(base + lane) * kMV;
@@ -1121,9 +1149,10 @@ __device__ __forceinline__ void grid_entries_regs(float2 (&r)[kChunk], const Row
       const uint32_t sk = __float_as_uint(meta[i * kMV].y);
       return load_sample<kFormat>(ks, sample_base + static_cast<size_t>(sk) * a.channels);
     };
-    float2 yv[kAR];
+    if (!pre) {
 #pragma unroll
-    for (int k = 0; k < kAR; ++k) yv[k] = (coil_ok && k < cnt) ? fetch(k) : make_float2(0.0f, 0.0f);
+      for (int k = 0; k < kAR; ++k) yv[k] = (coil_ok && k < cnt) ? fetch(k) : make_float2(0.0f, 0.0f);
+    }
     for (int i0 = 0; i0 < cnt; i0 += kAR) {
 #pragma unroll
       for (int k = 0; k < kAR; ++k) {
@@ -1240,24 +1269,61 @@ __device__ __forceinline__ void rows_grid_regs(const RowsArgs& a, int f, int cgi
   const bool coil_ok = coil_global < a.channels;
   const size_t sample_base = static_cast<size_t>(f) * a.sample_frame_stride + (coil_ok ? coil_global : 0);
   const int ntasks = tasks.base[a.nchunks];
-  for (;;) {
+  constexpr int kBatch = meta_batch(W);
+  // A warp claims its next task before it grids the current one, and loads
+  // that task's first sample indices at once, so their latency hides behind
+  // the current task.  Tasks are claimed in increasing order, so the
+  // smallest unfinished task is always some warp's current one: a segment's
+  // wait for its predecessors always ends.
+  auto claim = [&]() {
     int q = 0;
     if (lane == 0) q = atomicAdd(tasks.next, 1);
-    q = __shfl_sync(0xffffffffu, q, 0);
-    if (q >= ntasks) break;
-    int rank, seg;
-    task_of(tasks, a.nchunks, q, lane, &rank, &seg);
-    const int chunk = tasks.chunk[rank];
-    const uint32_t begin = offs[chunk];
-    const int n = static_cast<int>(offs[chunk + 1] - begin);
-    const int sl = segment_length(n);
-    const int e0 = seg * sl, e1 = min(n, e0 + sl);
-    const float4* xent = a.expanded + (static_cast<size_t>(f) * a.entries_per_frame + begin + e0) * kMV;
+    return __shfl_sync(0xffffffffu, q, 0);
+  };
+  struct Task {
+    int chunk, seg, n, e0, e1;
+  };
+  auto decode = [&](int q) {
+    Task t;
+    int rank;
+    task_of(tasks, a.nchunks, q, lane, &rank, &t.seg);
+    t.chunk = tasks.chunk[rank];
+    const uint32_t begin = offs[t.chunk];
+    t.n = static_cast<int>(offs[t.chunk + 1] - begin);
+    const int sl = segment_length(t.n);
+    t.e0 = seg_start(begin, t.seg, sl);
+    t.e1 = min(static_cast<int>(begin) + t.n, t.e0 + sl);
+    return t;
+  };
+  auto entries_of = [&](const Task& t) {
+    return a.expanded + (static_cast<size_t>(f) * a.entries_per_frame + static_cast<size_t>(t.e0)) * meta_vecs(W);
+  };
+  auto first_sk = [&](const Task& t) {
+    return lane < min(kBatch, t.e1 - t.e0) ? __float_as_uint(__ldg(&entries_of(t)[static_cast<size_t>(lane) * kMV].y))
+                                           : 0u;
+  };
+  int q = claim();
+  if (q >= ntasks) return;
+  Task cur = decode(q);
+  uint32_t sk = first_sk(cur);
+  for (;;) {
+    const int qn = claim();
+    const bool more = qn < ntasks;
+    Task nxt{};
+    uint32_t sk_next = 0u;
+    if (more) {
+      nxt = decode(qn);
+      sk_next = first_sk(nxt);
+    }
     float2 r[kChunk];
-    grid_entries_regs<W, kFormat, kWrap, kAR>(r, a, sample_base, coil_ok, lane, chunk * kChunk, xent, e1 - e0, meta);
-    put_chunk(r, acc + static_cast<size_t>(chunk * kChunk) * 32 + lane, 32, min(kChunk, a.grid_cols - chunk * kChunk),
-              true, seg, list_segments(n) > 1 ? tasks.combined + chunk : nullptr, a.flags, a.wait_limit,
-              a.wait_beyond);
+    grid_entries_regs<W, kFormat, kWrap, kAR>(r, a, sample_base, coil_ok, lane, cur.chunk * kChunk, entries_of(cur),
+                                              cur.e1 - cur.e0, meta, true, sk);
+    put_chunk(r, acc + static_cast<size_t>(cur.chunk * kChunk) * 32 + lane, 32,
+              min(kChunk, a.grid_cols - cur.chunk * kChunk), true, cur.seg,
+              list_segments(cur.n) > 1 ? tasks.combined + cur.chunk : nullptr, a.flags, a.wait_limit, a.wait_beyond);
+    if (!more) break;
+    cur = nxt;
+    sk = sk_next;
   }
 }
 
