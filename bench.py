@@ -563,7 +563,7 @@ def run_ours(args) -> dict | None:
     if rank == 0 and not args.skip_extra:
         del ws
         torch.cuda.empty_cache()
-        srv = run_serve(args, n=64)
+        srv = run_serve(args)
         served = {k2: srv[k2] for k2 in ("value", "serial_value", "vs_serial", "p50_ms", "p99_ms", "serial_p50_ms",
                                          "serial_p99_ms", "poisson_rate_per_s")}
         served.update({"unit": "samples/s", "requests": srv["config"]["requests"],
@@ -571,7 +571,7 @@ def run_ours(args) -> dict | None:
                        "workload": srv["config"]["workload"], "serial": srv["config"]["serial"],
                        "served": srv["config"]["served"],
                        "note": "value = burst throughput of the served loop; p50/p99 under Poisson arrivals at 90 % "
-                               "of the serial path's burst throughput; bench.py --serve runs 160 requests"})
+                               "of the serial path's burst throughput"})
 
     ms, e2e_ms = max_over_ranks(dist, ms, e2e_ms)
     if rank != 0:

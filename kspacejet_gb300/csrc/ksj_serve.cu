@@ -62,6 +62,8 @@ struct Buffer {
 struct Slot {
   cudaStream_t stream = nullptr;
   cudaEvent_t start = nullptr, copied = nullptr, computed = nullptr, done = nullptr;  // timing events of a batch
+  cudaStream_t copy2 = nullptr;     // second input-copy stream (every other request), for a second copy engine
+  cudaEvent_t copy2_done = nullptr;
   Buffer kspace, out, workspace, counts;  // device: copied inputs (packed), images, workspace, per-frame table
   Buffer pin_in, pin_out, pin_meta;             // pinned host: pageable inputs, pageable outputs, counts + flags
   std::vector<Ticket*> batch;                    // in frame order; empty = free
@@ -232,9 +234,15 @@ bool ksj_serve::launch(Slot& slot, const std::vector<Ticket*>& batch, uint32_t c
   uint32_t* counts = static_cast<uint32_t*>(slot.pin_meta.p);
   uint64_t* addr = reinterpret_cast<uint64_t*>(static_cast<char*>(slot.pin_meta.p) + ((size_t{nf} * 8 + 15) & ~size_t{15}));
   uint32_t* flags = reinterpret_cast<uint32_t*>(addr + 2 * nf);
-  if (cudaEventRecord(slot.start, slot.stream) != cudaSuccess) return false;
+  // the requests' input copies alternate between the slot's stream and a
+  // second copy stream (which first waits for the slot's earlier work), so
+  // two copy engines carry them; the reconstruction waits for both
+  if (cudaEventRecord(slot.start, slot.stream) != cudaSuccess ||
+      cudaStreamWaitEvent(slot.copy2, slot.start, 0) != cudaSuccess)
+    return false;
   char* stage = static_cast<char*>(slot.pin_in.p);
   char* dev = static_cast<char*>(slot.kspace.p);
+  cudaStream_t cs = slot.stream;
   auto place = [&](const void* src, size_t bytes, const void* in_place_addr) -> const void* {
     if (in_place_addr != nullptr) return in_place_addr;
     const void* from = src;
@@ -244,7 +252,7 @@ bool ksj_serve::launch(Slot& slot, const std::vector<Ticket*>& batch, uint32_t c
       stage += (bytes + 15) & ~size_t{15};
       if (in_place) return device_address(from);
     }
-    if (cudaMemcpyAsync(dev, from, bytes, cudaMemcpyHostToDevice, slot.stream) != cudaSuccess) return nullptr;
+    if (cudaMemcpyAsync(dev, from, bytes, cudaMemcpyHostToDevice, cs) != cudaSuccess) return nullptr;
     const void* at = dev;
     dev += (bytes + 255) & ~size_t{255};
     return at;
@@ -254,6 +262,7 @@ bool ksj_serve::launch(Slot& slot, const std::vector<Ticket*>& batch, uint32_t c
     const size_t kb = size_t{r.channels} * r.samples * 8, tb = size_t{r.samples} * 8;
     counts[f] = r.channels;
     counts[nf + f] = r.samples;
+    cs = (f & 1) ? slot.copy2 : slot.stream;
     const void* k_at = place(r.kspace, kb, k_dev[f]);
     if (k_at == nullptr) return false;
     const void* t_at = nullptr;
@@ -284,7 +293,9 @@ bool ksj_serve::launch(Slot& slot, const std::vector<Ticket*>& batch, uint32_t c
     addr[nf + f] = reinterpret_cast<uint64_t>(t_at);
   }
   const size_t addr_off = reinterpret_cast<char*>(addr) - static_cast<char*>(slot.pin_meta.p);
-  if (cudaMemcpyAsync(slot.counts.p, slot.pin_meta.p, addr_off + size_t{nf} * 16, cudaMemcpyHostToDevice,
+  if (cudaEventRecord(slot.copy2_done, slot.copy2) != cudaSuccess ||
+      cudaStreamWaitEvent(slot.stream, slot.copy2_done, 0) != cudaSuccess ||
+      cudaMemcpyAsync(slot.counts.p, slot.pin_meta.p, addr_off + size_t{nf} * 16, cudaMemcpyHostToDevice,
                       slot.stream) != cudaSuccess)
     return false;
   const uint32_t* d_counts = static_cast<const uint32_t*>(slot.counts.p);
@@ -375,6 +386,8 @@ void ksj_serve::run() {
   slots.resize(cfg.slots);
   for (Slot& s : slots) {
     if (cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&s.copy2, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&s.copy2_done, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreate(&s.start) != cudaSuccess || cudaEventCreate(&s.copied) != cudaSuccess ||
         cudaEventCreate(&s.computed) != cudaSuccess || cudaEventCreate(&s.done) != cudaSuccess)
       return;
@@ -434,6 +447,7 @@ void ksj_serve::run() {
         in_flight_bytes -= bytes;
         free_slot->bytes = 0;
         cudaStreamSynchronize(free_slot->stream);
+        cudaStreamSynchronize(free_slot->copy2);
         cudaGetLastError();
         fail_batch(batch, KSJ_GPU_ERROR_CUDA);
       } else {
@@ -457,9 +471,11 @@ void ksj_serve::run() {
       if (b->p) cudaFree(b->p);
     for (Buffer* b : {&s.pin_in, &s.pin_out, &s.pin_meta})
       if (b->p) cudaFreeHost(b->p);
-    for (cudaEvent_t e : {s.start, s.copied, s.computed, s.done})
+    if (s.copy2) cudaStreamSynchronize(s.copy2);
+    for (cudaEvent_t e : {s.start, s.copied, s.computed, s.done, s.copy2_done})
       if (e) cudaEventDestroy(e);
     if (s.stream) cudaStreamDestroy(s.stream);
+    if (s.copy2) cudaStreamDestroy(s.copy2);
   }
   for (auto& kv : trajectories) {
     cudaFree(kv.second.d);
