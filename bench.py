@@ -570,8 +570,8 @@ def run_ours(args) -> dict | None:
                        "batches": srv["results"]["served"]["burst"]["batches"],
                        "workload": srv["config"]["workload"], "serial": srv["config"]["serial"],
                        "served": srv["config"]["served"],
-                       "note": "value = burst throughput of the served loop; p50/p99 under Poisson arrivals at 90 % "
-                               "of the serial path's burst throughput"})
+                       "note": "value = burst throughput of the served loop (median of 3 bursts); p50/p99 under "
+                               "Poisson arrivals at 90 % of the serial path's burst throughput"})
 
     ms, e2e_ms = max_over_ranks(dist, ms, e2e_ms)
     if rank != 0:
@@ -725,8 +725,9 @@ def run_serve(args, n: int | None = None) -> dict:
     """The served stream: `n` requests through the request loop, once as the
     plain serial GPU path (one slot, batches of one request: each request is
     its own one-frame call) and once served (slots, ragged batches of up to
-    --serve-batch requests), each as a burst (all submitted at once) and as
-    Poisson arrivals at 90 % of the serial path's burst throughput."""
+    --serve-batch requests), each as a burst (all submitted at once; the
+    median of three bursts) and as Poisson arrivals at 90 % of the serial
+    path's burst throughput."""
     import torch
     from kspacejet_gb300 import serve
 
@@ -753,7 +754,8 @@ def run_serve(args, n: int | None = None) -> dict:
                           coil_split=split) as s:
             serve_pass(s, warm)
             serve_pass(s, reqs)  # first pass uploads and caches the trajectories
-            results[name] = {"burst": serve_pass(s, reqs)}
+            bursts = sorted((serve_pass(s, reqs) for _ in range(3)), key=lambda b: b["wall_seconds"])
+            results[name] = {"burst": bursts[1]}  # the median of three bursts
     # Poisson arrivals at 90% of the serial path's burst throughput
     rate = 0.9 * n / results["serial"]["burst"]["wall_seconds"]
     rng = np.random.default_rng(13)
