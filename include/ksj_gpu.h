@@ -456,9 +456,11 @@ KSJ_GPU_API ksj_gpu_status ksj_gpu_aggregate_acquisitions(uint32_t acquisitions,
  * d_kspace complex64 [frame][channel][row][col] (channel-major, as the
  * reference's ksj.kspace-frame) -> d_out per `output`: KSJ_GPU_OUTPUT_COIL_LAST
  * complex64 [frame][row][col][channel] (the reference's coil-image frame) or
- * KSJ_GPU_OUTPUT_RSS float32 [frame][row][col].  rows and cols 2^a or 3 * 2^a
- * up to 512 (the reference also takes other lengths: KSJ_GPU_ERROR_UNSUPPORTED
- * here), channels 1..64.  Workspace: ksj_gpu_cartesian_workspace_bytes. */
+ * KSJ_GPU_OUTPUT_RSS float32 [frame][row][col].  rows and cols 2..512, every
+ * length the reference takes: lengths 2^a 3^b 5^c 7^d by mixed-radix FFTs,
+ * lengths with a larger prime factor by a direct DFT along that axis (larger
+ * lengths: KSJ_GPU_ERROR_UNSUPPORTED); channels 1..64.  Workspace:
+ * ksj_gpu_cartesian_workspace_bytes. */
 KSJ_GPU_API size_t ksj_gpu_cartesian_workspace_bytes(uint32_t rows, uint32_t cols, uint32_t channels,
                                                      uint32_t frames);
 KSJ_GPU_API ksj_gpu_status ksj_gpu_cartesian_ifft2(uint32_t rows, uint32_t cols, uint32_t channels, uint32_t frames,

@@ -3200,8 +3200,52 @@ ksj_gpu_status dispatch_width(const Shape& s, const Layout& l, const ksj_gpu_gri
 // [frame][pixel][channel] (k_transpose), the row transform per (frame, row,
 // coil group) (k_cart_rows), then the column pass k_cols with its
 // deapodisation factors set to 1/rows and 1/cols and no crop or shift.
+// An axis whose length has a prime factor above 7 (no mixed-radix plan; the
+// reference's transform takes every length 2..512) is transformed by a
+// direct DFT instead: the row form of k_cart_rows, and k_cart_cols_direct
+// for the columns (coil-last output, then k_rss for the RSS form).
 
 constexpr int kCartThreads = 256;
+
+// Direct inverse DFT of 2^lg lines of length n held line-contiguous in
+// shared memory (element (j, line) at x[(j << lg) + line]): output k of a
+// line is sum_j x[j] w^(jk), w = exp(2 pi i / n), with jk reduced mod n
+// exactly in integers (tw[t] = w^t) and eight interleaved partial sums
+// (rounding error ~ sqrt(n / 8) ulp instead of sqrt(n)).  emit(k, line, v).
+template <class Emit>
+__device__ __forceinline__ void dft_direct_lines(const float2* x, int lg, int n, const float2* tw, int tid,
+                                                 int nthreads, Emit emit) {
+  const int lines = 1 << lg;
+  for (int o = tid; o < n * lines; o += nthreads) {
+    const int k = o >> lg, line = o & (lines - 1);
+    float2 s[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) s[u] = make_float2(0.0f, 0.0f);
+    int e = 0, j = 0;
+    for (; j + 8 <= n; j += 8) {
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const float2 v = x[((j + u) << lg) + line];
+        const float2 w = tw[e];
+        s[u].x = fmaf(v.x, w.x, fmaf(-v.y, w.y, s[u].x));
+        s[u].y = fmaf(v.x, w.y, fmaf(v.y, w.x, s[u].y));
+        e += k;
+        if (e >= n) e -= n;
+      }
+    }
+    for (int u = 0; j < n; ++j, ++u) {
+      const float2 v = x[(j << lg) + line];
+      const float2 w = tw[e];
+      s[u].x = fmaf(v.x, w.x, fmaf(-v.y, w.y, s[u].x));
+      s[u].y = fmaf(v.x, w.y, fmaf(v.y, w.x, s[u].y));
+      e += k;
+      if (e >= n) e -= n;
+    }
+    const float re = ((s[0].x + s[1].x) + (s[2].x + s[3].x)) + ((s[4].x + s[5].x) + (s[6].x + s[7].x));
+    const float im = ((s[0].y + s[1].y) + (s[2].y + s[3].y)) + ((s[4].y + s[5].y) + (s[6].y + s[7].y));
+    emit(k, line, make_float2(re, im));
+  }
+}
 
 // Twiddles, the normalisation factors and the position of output k of each
 // axis's transform (two-step slot or digit-reversed position).
@@ -3222,7 +3266,8 @@ __global__ void k_cart_tables(float2* tw_rows, int rows, float2* tw_cols, int co
 
 // One block per (frame, row, coil group of cg): the row's cg coil lines
 // [column][coil] from the coil-last samples, transformed along the row; every
-// column written to [frame][row][column][cpitch].
+// column written to [frame][row][column][cpitch].  kN > 0: the two-step
+// transform of that length; 0: the mixed-radix plan; -1: the direct DFT.
 template <int kN>
 __global__ void __launch_bounds__(kCartThreads) k_cart_rows(const float2* __restrict__ coil_last, float2* inter,
                                                             const float2* __restrict__ tw_cols,
@@ -3245,8 +3290,10 @@ __global__ void __launch_bounds__(kCartThreads) k_cart_rows(const float2* __rest
   auto emit = [&](int k, int line, float2 v) {
     if (line < live) dst[static_cast<size_t>(k) * cpitch + line] = v;
   };
-  if constexpr (kN != 0) {
+  if constexpr (kN > 0) {
     fft_two_step<16, kN / 16>(acc, lg, tw, threadIdx.x, blockDim.x, emit);
+  } else if constexpr (kN < 0) {
+    dft_direct_lines(acc, lg, cols, tw, threadIdx.x, blockDim.x, emit);
   } else {
     dif_lines(acc, lg, plan, tw, threadIdx.x, blockDim.x);
     const int c = threadIdx.x & (cg - 1);
@@ -3259,6 +3306,7 @@ __global__ void __launch_bounds__(kCartThreads) k_cart_rows(const float2* __rest
 using CartRowsKernel = void (*)(const float2*, float2*, const float2*, const int*, DifPlan, int, int, int, int, int);
 
 CartRowsKernel cart_rows_for(int n) {
+  if (!is_fft_size(static_cast<uint32_t>(n))) return k_cart_rows<-1>;
   switch (n) {
     case 128: return k_cart_rows<128>;
     case 192: return k_cart_rows<192>;
@@ -3267,6 +3315,33 @@ CartRowsKernel cart_rows_for(int n) {
     case 512: return k_cart_rows<512>;
     default: return k_cart_rows<0>;
   }
+}
+
+// Columns of an axis without a mixed-radix plan: one block per (frame,
+// column, coil group of cg): the column's rows x cg lines from the
+// row-transformed grid [frame][row][column][cpitch] into shared memory, the
+// direct DFT along the rows, each output scaled by (1/rows)(1/cols) and
+// written coil-last [frame][row][column][channel].
+__global__ void __launch_bounds__(kCartThreads) k_cart_cols_direct(const float2* __restrict__ inter, float2* out,
+                                                                   const float2* __restrict__ tw_rows, int rows,
+                                                                   int cols, int channels, int cg, int cpitch) {
+  extern __shared__ __align__(16) float2 cart_smem[];
+  float2* acc = cart_smem;
+  float2* tw = cart_smem + static_cast<size_t>(rows) * cg;
+  const int col = blockIdx.x, cgi = blockIdx.y, f = blockIdx.z;
+  const int lg = ilog2(cg);
+  const float2* src = inter + (static_cast<size_t>(f) * rows * cols + col) * cpitch + cgi * cg;
+  for (int i = threadIdx.x; i < rows * cg; i += blockDim.x)
+    acc[i] = __ldg(src + static_cast<size_t>(i >> lg) * cols * cpitch + (i & (cg - 1)));
+  for (int i = threadIdx.x; i < rows; i += blockDim.x) tw[i] = tw_rows[i];
+  __syncthreads();
+  const float scale = (1.0f / static_cast<float>(rows)) * (1.0f / static_cast<float>(cols));
+  const int live = min(cg, channels - cgi * cg);
+  float2* dst = out + static_cast<size_t>(f) * rows * cols * channels + static_cast<size_t>(col) * channels + cgi * cg;
+  dft_direct_lines(acc, lg, rows, tw, threadIdx.x, blockDim.x, [&](int k, int line, float2 v) {
+    if (line < live)
+      dst[static_cast<size_t>(k) * cols * channels + line] = make_float2(v.x * scale, v.y * scale);
+  });
 }
 
 // The shape of a Cartesian call as the column pass reads it.
@@ -3278,7 +3353,7 @@ struct CartShape {
 
 ksj_gpu_status make_cart_shape(uint32_t rows, uint32_t cols, uint32_t channels, uint32_t frames, CartShape* c) {
   if (rows < 2 || cols < 2 || channels == 0 || channels > 64 || frames == 0) return KSJ_GPU_ERROR_INVALID_ARGUMENT;
-  if (!is_fft_size(rows) || !is_fft_size(cols)) return KSJ_GPU_ERROR_UNSUPPORTED;
+  if (rows > kMaxGrid || cols > kMaxGrid) return KSJ_GPU_ERROR_UNSUPPORTED;
   Shape& s = c->s;
   s = Shape{};
   s.frames = static_cast<int>(frames);
@@ -3293,12 +3368,17 @@ ksj_gpu_status make_cart_shape(uint32_t rows, uint32_t cols, uint32_t channels, 
     return static_cast<size_t>(s.grid_rows) * b * s.col_group * sizeof(float2) * (cgroups > 1 ? 2 : 1);
   };
   int cb = std::max(1, 32 / s.col_group);
-  while (cb > 1 && (tile(cb) > 110 * 1024 || cb > s.out_cols)) cb >>= 1;
-  if (tile(cb) > 200 * 1024) return KSJ_GPU_ERROR_UNSUPPORTED;
+  if (is_fft_size(rows)) {  // the column pass k_cols and its tile
+    while (cb > 1 && (tile(cb) > 110 * 1024 || cb > s.out_cols)) cb >>= 1;
+    if (tile(cb) > 200 * 1024) return KSJ_GPU_ERROR_UNSUPPORTED;
+  } else {
+    cb = 1;
+  }
   s.column_block = cb;
   s.frames_per_pass = s.frames;
-  make_dif_plan(s.grid_rows, &s.plan_rows);
-  make_dif_plan(s.grid_cols, &s.plan_cols);
+  // an axis without a mixed-radix plan (direct DFT) keeps an empty plan
+  if (!make_dif_plan(s.grid_rows, &s.plan_rows)) s.plan_rows = DifPlan{s.grid_rows, 0, {}, {}, {}, {}, {}};
+  if (!make_dif_plan(s.grid_cols, &s.plan_cols)) s.plan_cols = DifPlan{s.grid_cols, 0, {}, {}, {}, {}, {}};
   c->cg = s.col_group;
   size_t off = 0;
   auto take = [&](size_t bytes) {
@@ -3816,6 +3896,29 @@ extern "C" ksj_gpu_status ksj_gpu_cartesian_ifft2(uint32_t rows, uint32_t cols, 
     LaunchScope scope("k_cart_rows", cstream);
     rk<<<grid, kCartThreads, smem, cstream>>>(coil_last, inter, tw_cols, pos_cols, s.plan_cols, static_cast<int>(rows),
                                              static_cast<int>(cols), static_cast<int>(channels), cs.cg, s.cpitch);
+  }
+  if (!is_fft_size(rows)) {
+    // direct DFT along the columns, coil-last into the output (or into the
+    // consumed coil-last buffer, then its RSS)
+    float2* dst = output == KSJ_GPU_OUTPUT_COIL_LAST ? static_cast<float2*>(d_out) : coil_last;
+    const size_t smem = (static_cast<size_t>(rows) * cs.cg + rows) * sizeof(float2);
+    if (cudaFuncSetAttribute(k_cart_cols_direct, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(smem)) != cudaSuccess)
+      return KSJ_GPU_ERROR_CUDA;
+    {
+      const dim3 grid(cols, (channels + cs.cg - 1) / cs.cg, frames);
+      LaunchScope scope("k_cart_cols_direct", cstream);
+      k_cart_cols_direct<<<grid, kCartThreads, smem, cstream>>>(inter, dst, tw_rows, static_cast<int>(rows),
+                                                               static_cast<int>(cols), static_cast<int>(channels),
+                                                               cs.cg, s.cpitch);
+    }
+    if (output == KSJ_GPU_OUTPUT_RSS) {
+      const ksj_gpu_status rs = check_launch();
+      if (rs != KSJ_GPU_OK) return rs;
+      return ksj_gpu_rss_coil_last(static_cast<uint64_t>(frames) * rows * cols, channels, coil_last,
+                                   static_cast<float*>(d_out), stream);
+    }
+    return check_launch();
   }
   ColsArgs c{};
   c.tw_rows = tw_rows;

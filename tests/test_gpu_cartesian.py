@@ -8,7 +8,7 @@ import oracle
 
 pytestmark = pytest.mark.gpu
 
-TOL = 3e-6  # rel L2 per coil against FP64 (float transforms of <= 512 points per axis)
+TOL = 3e-6  # rel L2 per coil against FP64 (float transforms of <= 512 points per axis, FFT or direct DFT)
 
 
 def test_cartesian_reference_known_answer(native, cuda):
@@ -27,7 +27,11 @@ def test_cartesian_reference_known_answer(native, cuda):
                                                       # lengths with factors 5, 7 and 3^2 (matrices such as
                                                       # 160, 240, 320, 448 common in MRI)
                                                       (1, 8, 160, 240), (1, 4, 320, 448), (2, 3, 100, 36),
-                                                      (1, 2, 210, 98), (1, 16, 7, 5), (1, 32, 288, 144)])
+                                                      (1, 2, 210, 98), (1, 16, 7, 5), (1, 32, 288, 144),
+                                                      # lengths with a prime factor above 7 (direct DFT on that
+                                                      # axis): 110 = 2 x 5 x 11, 121 = 11^2, 509 and 13 prime
+                                                      (1, 8, 110, 121), (2, 3, 509, 13), (1, 40, 127, 64),
+                                                      (1, 6, 96, 11), (1, 4, 2, 17)])
 def test_cartesian_matches_fp64(native, cuda, orc, frames, channels, rows, cols):
     import torch
     from kspacejet_gb300 import gpu
@@ -51,7 +55,7 @@ def test_cartesian_rejects(native, cuda):
     from kspacejet_gb300 import gpu
 
     with pytest.raises(gpu.GpuError):
-        # 110 = 2 x 5 x 11: a prime factor above 7 (the reference's FFT takes it; here it is refused)
-        gpu.cartesian_ifft2(torch.zeros((2, 110, 110), dtype=torch.complex64, device=cuda))
+        # an axis above the 512 points of the envelope
+        gpu.cartesian_ifft2(torch.zeros((2, 520, 64), dtype=torch.complex64, device=cuda))
     with pytest.raises(gpu.GpuError):
         gpu.cartesian_ifft2(torch.zeros((65, 8, 8), dtype=torch.complex64, device=cuda))
