@@ -195,27 +195,40 @@ constexpr int kCovThreads = 128;
 constexpr uint32_t kCovWaitLimit = 1u << 22;
 constexpr int kCovMaxBlocks = 304;
 
+// Four consecutive samples of one coil per thread: four 8-byte loads (a
+// warp reads 1 KiB contiguous) and one 8-byte store per operand row.
+constexpr int kSplitPerThread = 4;
+static_assert(kCovKTile % kSplitPerThread == 0, "padded sample count is a multiple of the per-thread samples");
+
 __global__ void __launch_bounds__(256) k_cov_split(const float2* __restrict__ x, uint16_t* a, int channels,
                                                    int samples, int kpad) {
   const size_t idx = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (idx >= static_cast<size_t>(32) * kpad) return;
-  const int c = static_cast<int>(idx / kpad);
-  const int s = static_cast<int>(idx - static_cast<size_t>(c) * kpad);
-  float re = 0.0f, im = 0.0f;
-  if (c < channels && s < samples) {
-    const float2 v = x[static_cast<size_t>(c) * samples + s];
-    re = v.x;
-    im = v.y;
+  const int quads = kpad / kSplitPerThread;
+  if (idx >= static_cast<size_t>(32) * quads) return;
+  const int c = static_cast<int>(idx / quads);
+  const int s0 = static_cast<int>(idx - static_cast<size_t>(c) * quads) * kSplitPerThread;
+  uint16_t h[2][kSplitPerThread], l[2][kSplitPerThread];
+#pragma unroll
+  for (int i = 0; i < kSplitPerThread; ++i) {
+    const int sm = s0 + i;
+    float2 v = make_float2(0.0f, 0.0f);
+    if (c < channels && sm < samples) v = __ldg(x + static_cast<size_t>(c) * samples + sm);
+    const __nv_bfloat16 hr = __float2bfloat16_rn(v.x);
+    const __nv_bfloat16 hi = __float2bfloat16_rn(v.y);
+    h[0][i] = __bfloat16_as_ushort(hr);
+    h[1][i] = __bfloat16_as_ushort(hi);
+    l[0][i] = __bfloat16_as_ushort(__float2bfloat16_rn(v.x - __bfloat162float(hr)));
+    l[1][i] = __bfloat16_as_ushort(__float2bfloat16_rn(v.y - __bfloat162float(hi)));
   }
-  const __nv_bfloat16 hr = __float2bfloat16_rn(re);
-  const __nv_bfloat16 hi = __float2bfloat16_rn(im);
-  const __nv_bfloat16 lr = __float2bfloat16_rn(re - __bfloat162float(hr));
-  const __nv_bfloat16 li = __float2bfloat16_rn(im - __bfloat162float(hi));
+  auto pack = [](const uint16_t (&v)[kSplitPerThread]) {
+    return make_uint2(static_cast<uint32_t>(v[0]) | (static_cast<uint32_t>(v[1]) << 16),
+                      static_cast<uint32_t>(v[2]) | (static_cast<uint32_t>(v[3]) << 16));
+  };
   const size_t k = static_cast<size_t>(kpad);
-  a[static_cast<size_t>(c) * k + s] = __bfloat16_as_ushort(hr);
-  a[static_cast<size_t>(32 + c) * k + s] = __bfloat16_as_ushort(hi);
-  a[static_cast<size_t>(64 + c) * k + s] = __bfloat16_as_ushort(lr);
-  a[static_cast<size_t>(96 + c) * k + s] = __bfloat16_as_ushort(li);
+  *reinterpret_cast<uint2*>(a + static_cast<size_t>(c) * k + s0) = pack(h[0]);
+  *reinterpret_cast<uint2*>(a + static_cast<size_t>(32 + c) * k + s0) = pack(h[1]);
+  *reinterpret_cast<uint2*>(a + static_cast<size_t>(64 + c) * k + s0) = pack(l[0]);
+  *reinterpret_cast<uint2*>(a + static_cast<size_t>(96 + c) * k + s0) = pack(l[1]);
 }
 
 // Shared-memory matrix descriptor of a K-major operand in the 128-byte swizzle
@@ -519,7 +532,7 @@ ksj_gpu_status covariance_run(uint32_t channels, uint32_t samples, const void* d
   float* partials = reinterpret_cast<float*>(ws + l.partials);
   if (cudaMemsetAsync(flags, 0, 16, cs) != cudaSuccess) return KSJ_GPU_ERROR_CUDA;
   {
-    const size_t n = static_cast<size_t>(32) * l.kpad;
+    const size_t n = static_cast<size_t>(32) * (l.kpad / kSplitPerThread);
     LaunchScope scope("k_cov_split", cs);
     k_cov_split<<<static_cast<unsigned>((n + 255) / 256), 256, 0, cs>>>(static_cast<const float2*>(d_kspace),
                                                                         operand, static_cast<int>(channels),

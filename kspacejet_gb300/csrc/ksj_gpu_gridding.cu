@@ -2413,36 +2413,93 @@ __global__ void __launch_bounds__(256) k_pm_prepare(const float* traj, PmRecord<
   w[idx] = ok ? 1.0 : 0.0;
 }
 
-// One half-warp per list; lane l % 16 is the list's column chunk * 16 + l % 16.
-// Every cell of the grid belongs to exactly one list, so every cell is written.
-template <int W>
-__global__ void __launch_bounds__(256) k_pm_grid(const uint32_t* offsets, const uint32_t* entries,
-                                                 const PmRecord<W>* pm, const double* w, double* grid, int frames,
-                                                 int samples, int grid_rows, int grid_cols, int nchunks,
-                                                 int lists_per_frame, size_t entries_per_frame) {
-  const size_t hw = (static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 4;
-  const int sub = threadIdx.x & 15;
-  if (hw >= static_cast<size_t>(frames) * lists_per_frame) return;
-  const int f = static_cast<int>(hw / lists_per_frame);
-  const int l = static_cast<int>(hw - static_cast<size_t>(f) * lists_per_frame);
-  const int row = l / nchunks;
-  const int col = (l - row * nchunks) * kChunk + sub;
-  const uint32_t* off = offsets + static_cast<size_t>(f) * (lists_per_frame + 1);
-  const uint32_t begin = off[l], end = off[l + 1];
-  const uint32_t* ent = entries + static_cast<size_t>(f) * entries_per_frame;
-  const PmRecord<W>* rec = pm + static_cast<size_t>(f) * samples;
-  const double* wf = w + static_cast<size_t>(f) * samples;
-  double acc = 0.0;
-  for (uint32_t e = begin; e < end; ++e) {
-    const uint32_t sidx = __ldg(ent + e);
-    const PmRecord<W>& r = rec[sidx];
-    int dc = col - r.c0;
-    if (dc < 0) dc += grid_cols;
-    int dr = row - r.r0;
-    if (dr < 0) dr += grid_rows;
-    if (dc < W && dr < W) acc += wf[sidx] * (r.wr[dr] * r.wc[dc]);
+// The grid step, kPmLanes lanes per list: lane q takes the list's entries q,
+// q + kPmLanes, ... in order and, for every column tap of an entry that lands
+// in the list's 16-column chunk, adds u * wc[k] (u = w times the entry's row,
+// and plane, weights) to its own 16 cells in shared memory (cell t of thread
+// i at cells[t * kPmThreads + i]: the lanes of a warp always touch distinct
+// banks).  Then lane q sums cells 4q .. 4q+3 over the list's lanes, each cell
+// in a fixed order (starting at lane q), and writes them.  Every FP64
+// operation a lane issues is one a cell needs; with a lane per column
+// instead, 12 of every 16 lanes multiplied by taps outside their column, and
+// this step is bound by the FP64 pipe.  Lists are kPmLanes consecutive lanes
+// of one warp, so a warp barrier orders the two phases.
+constexpr int kPmLanes = 4;
+constexpr int kPmThreads = 256;
+constexpr int kPmCellsPerLane = kChunk / kPmLanes;
+static_assert(kChunk == 16 && (kPmLanes & (kPmLanes - 1)) == 0 && 32 % kPmLanes == 0, "lanes of a list");
+
+// One lane's share of the list's entries [e0, e1) (every `step`-th), added to
+// its cells (cell[t * kPmThreads], t = column - lo).  `weight(r, sidx, &u)`
+// gives the entry's u, or false when its row (and plane) taps miss the list.
+template <int W, class Rec, class Weight>
+__device__ __forceinline__ void pm_accumulate(const uint32_t* entries, uint32_t e0, uint32_t e1, uint32_t step,
+                                              const Rec* rec, int lo, int grid_cols, double* cell, Weight weight) {
+  for (uint32_t e = e0; e < e1; e += step) {
+    const uint32_t sidx = __ldg(entries + e);
+    const Rec& r = rec[sidx];
+    double u;
+    if (!weight(r, sidx, &u)) continue;
+    int col = r.c0;
+#pragma unroll
+    for (int k = 0; k < W; ++k) {
+      const int t = col - lo;
+      if (t >= 0 && t < kChunk) cell[t * kPmThreads] = fma(u, r.wc[k], cell[t * kPmThreads]);
+      if (++col == grid_cols) col = 0;
+    }
   }
-  if (col < grid_cols) grid[(static_cast<size_t>(f) * grid_rows + row) * grid_cols + col] = acc;
+}
+
+// Lane q of a list (its lane 0 is thread `lane0`): cells 4q .. 4q+3 summed
+// over the list's lanes, starting at lane q, written to row[lo + t] inside
+// the grid.
+__device__ __forceinline__ void pm_reduce_store(const double* cells, int lane0, int q, double* row, int lo,
+                                                int grid_cols) {
+#pragma unroll
+  for (int i = 0; i < kPmCellsPerLane; ++i) {
+    const int t = q * kPmCellsPerLane + i;
+    const double* c = cells + t * kPmThreads + lane0;
+    double acc = c[q];
+#pragma unroll
+    for (int j = 1; j < kPmLanes; ++j) acc += c[(q + j) & (kPmLanes - 1)];
+    if (lo + t < grid_cols) row[lo + t] = acc;
+  }
+}
+
+template <int W>
+__global__ void __launch_bounds__(kPmThreads) k_pm_grid(const uint32_t* offsets, const uint32_t* entries,
+                                                        const PmRecord<W>* pm, const double* w, double* grid,
+                                                        int frames, int samples, int grid_rows, int grid_cols,
+                                                        int nchunks, int lists_per_frame, size_t entries_per_frame) {
+  __shared__ double cells[kChunk * kPmThreads];
+  const size_t list = (static_cast<size_t>(blockIdx.x) * kPmThreads + threadIdx.x) / kPmLanes;
+  const int q = threadIdx.x & (kPmLanes - 1);
+  double* cell = cells + threadIdx.x;
+#pragma unroll
+  for (int t = 0; t < kChunk; ++t) cell[t * kPmThreads] = 0.0;
+  const bool active = list < static_cast<size_t>(frames) * lists_per_frame;
+  int f = 0, row = 0, lo = 0;
+  if (active) {
+    f = static_cast<int>(list / lists_per_frame);
+    const int l = static_cast<int>(list - static_cast<size_t>(f) * lists_per_frame);
+    row = l / nchunks;
+    lo = (l - row * nchunks) * kChunk;
+    const uint32_t* off = offsets + static_cast<size_t>(f) * (lists_per_frame + 1);
+    const PmRecord<W>* rec = pm + static_cast<size_t>(f) * samples;
+    const double* wf = w + static_cast<size_t>(f) * samples;
+    pm_accumulate<W>(entries + static_cast<size_t>(f) * entries_per_frame, off[l] + q, off[l + 1], kPmLanes, rec, lo,
+                     grid_cols, cell, [&](const PmRecord<W>& r, uint32_t sidx, double* u) {
+                       int dr = row - r.r0;
+                       if (dr < 0) dr += grid_rows;
+                       if (dr >= W) return false;
+                       *u = wf[sidx] * r.wr[dr];
+                       return true;
+                     });
+  }
+  __syncwarp();
+  if (active)
+    pm_reduce_store(cells, threadIdx.x - q, q, grid + (static_cast<size_t>(f) * grid_rows + row) * grid_cols, lo,
+                    grid_cols);
 }
 
 // Per sample: d = the grid read back through the sample's taps (row-major),
@@ -2526,11 +2583,11 @@ ksj_gpu_status launch_pipe_menon(const Shape& s, const PmLayout& l, const ksj_gp
     k_pm_prepare<W><<<static_cast<unsigned>((fm + 255) / 256), 256, 0, stream>>>(
         d_traj, pm, w, fm, s.grid_rows, s.grid_cols, beta, 1.0 / std::cyl_bessel_i(0.0, beta), d->require_nyquist);
   }
-  const size_t half_warps = static_cast<size_t>(s.frames) * s.lists_per_frame;
+  const size_t lists = static_cast<size_t>(s.frames) * s.lists_per_frame;
   for (uint32_t it = 0; it < iterations; ++it) {
     {
       LaunchScope scope("k_pm_grid", stream);
-      k_pm_grid<W><<<static_cast<unsigned>((half_warps * 16 + 255) / 256), 256, 0, stream>>>(
+      k_pm_grid<W><<<static_cast<unsigned>((lists * kPmLanes + kPmThreads - 1) / kPmThreads), kPmThreads, 0, stream>>>(
           reinterpret_cast<const uint32_t*>(ws + l.offsets), reinterpret_cast<const uint32_t*>(ws + l.entries), pm,
           w, grid, s.frames, s.samples, s.grid_rows, s.grid_cols, s.nchunks, s.lists_per_frame,
           s.entries_per_frame);
@@ -2986,80 +3043,94 @@ __global__ void __launch_bounds__(256) k_pm_prepare3(const float* traj, PmRecord
   w[idx] = ok ? 1.0 : 0.0;
 }
 
-// Cell (plane, row, col)'s sum over list entries [e0, e1), in entry order
-// from `acc`.
+// The 3-D grid step: the lanes-per-list form of k_pm_grid, with the entry's
+// plane weight in u.  Lists longer than `capacity` entries (queued by the
+// list sort) are left to k_pm_long3.
 template <int W>
-__device__ __forceinline__ double pm_cell3(const uint32_t* entries, uint32_t e0, uint32_t e1, const PmRecord3<W>* pm,
-                                           const double* w, int plane, int row, int col, int g, double acc) {
-  for (uint32_t e = e0; e < e1; ++e) {
-    const uint32_t sidx = __ldg(entries + e);
-    const PmRecord3<W>& r = pm[sidx];
-    int dz = plane - r.z0;
-    if (dz < 0) dz += g;
-    int dr = row - r.r0;
-    if (dr < 0) dr += g;
-    int dc = col - r.c0;
-    if (dc < 0) dc += g;
-    if (dz < W && dr < W && dc < W) acc += w[sidx] * ((r.wz[dz] * r.wr[dr]) * r.wc[dc]);
+__global__ void __launch_bounds__(kPmThreads) k_pm_grid3(const uint32_t* offsets, const uint32_t* entries,
+                                                         const PmRecord3<W>* pm, const double* w, double* grid, int g,
+                                                         int nchunks, int lists_per_plane, int capacity) {
+  __shared__ double cells[kChunk * kPmThreads];
+  const size_t list = (static_cast<size_t>(blockIdx.x) * kPmThreads + threadIdx.x) / kPmLanes;
+  const int q = threadIdx.x & (kPmLanes - 1);
+  double* cell = cells + threadIdx.x;
+#pragma unroll
+  for (int t = 0; t < kChunk; ++t) cell[t * kPmThreads] = 0.0;
+  bool active = list < static_cast<size_t>(g) * lists_per_plane;
+  int plane = 0, row = 0, lo = 0;
+  if (active) {
+    plane = static_cast<int>(list / lists_per_plane);
+    const int l = static_cast<int>(list - static_cast<size_t>(plane) * lists_per_plane);
+    row = l / nchunks;
+    lo = (l - row * nchunks) * kChunk;
+    const uint32_t* off = offsets + static_cast<size_t>(plane) * (lists_per_plane + 1);
+    const uint32_t begin = off[l], end = off[l + 1];
+    active = static_cast<int>(end - begin) <= capacity;
+    if (active)
+      pm_accumulate<W>(entries, begin + q, end, kPmLanes, pm, lo, g, cell,
+                       [&](const PmRecord3<W>& r, uint32_t sidx, double* u) {
+                         int dz = plane - r.z0;
+                         if (dz < 0) dz += g;
+                         int dr = row - r.r0;
+                         if (dr < 0) dr += g;
+                         if (dz >= W || dr >= W) return false;
+                         *u = w[sidx] * (r.wz[dz] * r.wr[dr]);
+                         return true;
+                       });
   }
-  return acc;
-}
-
-// One half-warp per (plane, row, chunk) list; lane l % 16 is a column.
-// Lists longer than `capacity` entries (queued by the list sort) are left to
-// k_pm_long3.
-template <int W>
-__global__ void __launch_bounds__(256) k_pm_grid3(const uint32_t* offsets, const uint32_t* entries,
-                                                  const PmRecord3<W>* pm, const double* w, double* grid, int g,
-                                                  int nchunks, int lists_per_plane, int capacity) {
-  const size_t hw = (static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 4;
-  const int sub = threadIdx.x & 15;
-  if (hw >= static_cast<size_t>(g) * lists_per_plane) return;
-  const int plane = static_cast<int>(hw / lists_per_plane);
-  const int l = static_cast<int>(hw - static_cast<size_t>(plane) * lists_per_plane);
-  const int row = l / nchunks;
-  const int col = (l - row * nchunks) * kChunk + sub;
-  const uint32_t* off = offsets + static_cast<size_t>(plane) * (lists_per_plane + 1);
-  const uint32_t begin = off[l], end = off[l + 1];
-  if (static_cast<int>(end - begin) > capacity) return;
-  const double acc = pm_cell3<W>(entries, begin, end, pm, w, plane, row, col, g, 0.0);
-  if (col < g) grid[(static_cast<size_t>(plane) * g + row) * g + col] = acc;
+  __syncwarp();
+  if (active) pm_reduce_store(cells, threadIdx.x - q, q, grid + (static_cast<size_t>(plane) * g + row) * g, lo, g);
 }
 
 // The queued long lists (count at long_lists[0], global list ids after it),
-// one block per list at a time: half-warp h sums the h-th of kPmLongSegs
-// consecutive segments of the list for its 16 columns (in entry order from
-// zero), then the block's first 16 threads add the segments' partial sums in
-// segment order.  The kooshball centre's lists hold up to ~10^5 entries, which
-// one half-warp walks one dependent record load at a time.
-constexpr int kPmLongThreads = 512;
-constexpr int kPmLongSegs = kPmLongThreads / 16;
-
+// one block per list at a time: thread i takes the list's entries i,
+// i + kPmThreads, ... into its own 16 cells (as in k_pm_grid3); then cell t
+// is summed over the block in a fixed order: 16 groups of 16 threads each
+// (within a group starting at a rotation by t), then the groups in order.
+// The kooshball centre's lists hold up to ~10^5 entries.
 template <int W>
-__global__ void __launch_bounds__(kPmLongThreads) k_pm_long3(const uint32_t* long_lists, const uint32_t* offsets,
-                                                             const uint32_t* entries, const PmRecord3<W>* pm,
-                                                             const double* w, double* grid, int g, int nchunks,
-                                                             int lists_per_plane) {
-  __shared__ double part[kPmLongSegs][16];
+__global__ void __launch_bounds__(kPmThreads) k_pm_long3(const uint32_t* long_lists, const uint32_t* offsets,
+                                                         const uint32_t* entries, const PmRecord3<W>* pm,
+                                                         const double* w, double* grid, int g, int nchunks,
+                                                         int lists_per_plane) {
+  constexpr int kGroups = kPmThreads / kChunk;
+  __shared__ double cells[kChunk * kPmThreads];
+  __shared__ double part[kGroups][kChunk];
   const uint32_t queued = long_lists[0];
-  const int h = threadIdx.x >> 4, sub = threadIdx.x & 15;
-  for (uint32_t q = blockIdx.x; q < queued; q += gridDim.x) {
-    const uint32_t gl = long_lists[1 + q];
+  double* cell = cells + threadIdx.x;
+  const int c = threadIdx.x & (kChunk - 1), grp = threadIdx.x / kChunk;
+  for (uint32_t qd = blockIdx.x; qd < queued; qd += gridDim.x) {
+    const uint32_t gl = long_lists[1 + qd];
     const int plane = static_cast<int>(gl / static_cast<uint32_t>(lists_per_plane));
     const int l = static_cast<int>(gl - static_cast<uint32_t>(plane) * lists_per_plane);
     const int row = l / nchunks;
-    const int col = (l - row * nchunks) * kChunk + sub;
+    const int lo = (l - row * nchunks) * kChunk;
     const uint32_t* off = offsets + static_cast<size_t>(plane) * (lists_per_plane + 1);
-    const uint32_t begin = off[l], n = off[l + 1] - begin;
-    const uint32_t seg = (n + kPmLongSegs - 1) / kPmLongSegs;
-    const uint32_t e0 = begin + min(n, static_cast<uint32_t>(h) * seg);
-    const uint32_t e1 = begin + min(n, static_cast<uint32_t>(h + 1) * seg);
-    part[h][sub] = pm_cell3<W>(entries, e0, e1, pm, w, plane, row, col, g, 0.0);
+#pragma unroll
+    for (int t = 0; t < kChunk; ++t) cell[t * kPmThreads] = 0.0;
+    pm_accumulate<W>(entries, off[l] + threadIdx.x, off[l + 1], kPmThreads, pm, lo, g, cell,
+                     [&](const PmRecord3<W>& r, uint32_t sidx, double* u) {
+                       int dz = plane - r.z0;
+                       if (dz < 0) dz += g;
+                       int dr = row - r.r0;
+                       if (dr < 0) dr += g;
+                       if (dz >= W || dr >= W) return false;
+                       *u = w[sidx] * (r.wz[dz] * r.wr[dr]);
+                       return true;
+                     });
     __syncthreads();
-    if (threadIdx.x < 16) {
-      double acc = part[0][sub];
-      for (int k = 1; k < kPmLongSegs; ++k) acc += part[k][sub];
-      if (col < g) grid[(static_cast<size_t>(plane) * g + row) * g + col] = acc;
+    {
+      const double* src = cells + c * kPmThreads + grp * kChunk;
+      double acc = src[c];
+#pragma unroll
+      for (int j = 1; j < kChunk; ++j) acc += src[(c + j) & (kChunk - 1)];
+      part[grp][c] = acc;
+    }
+    __syncthreads();
+    if (threadIdx.x < kChunk) {
+      double acc = part[0][c];
+      for (int k = 1; k < kGroups; ++k) acc += part[k][c];
+      if (lo + c < g) grid[(static_cast<size_t>(plane) * g + row) * g + lo + c] = acc;
     }
     __syncthreads();
   }
@@ -3144,19 +3215,20 @@ ksj_gpu_status launch_pipe_menon3(const Shape& s, const PmLayout3& l, uint32_t i
     k_pm_prepare3<W><<<(s.samples + 255) / 256, 256, 0, stream>>>(d_traj, pm, w, s.samples, g, s.beta,
                                                                  1.0 / std::cyl_bessel_i(0.0, static_cast<double>(s.beta)));
   }
-  const size_t half_warps = static_cast<size_t>(g) * s.lists_per_frame;
+  const size_t lists = static_cast<size_t>(g) * s.lists_per_frame;
   // at most this many lists exceed the capacity
   const size_t long_blocks = std::max<size_t>(1, l.entries_total / (static_cast<size_t>(s.list_capacity) + 1));
   for (uint32_t it = 0; it < iterations; ++it) {
     {
       LaunchScope scope("k_pm_grid3", stream);
-      k_pm_grid3<W><<<static_cast<unsigned>((half_warps * 16 + 255) / 256), 256, 0, stream>>>(
+      k_pm_grid3<W><<<static_cast<unsigned>((lists * kPmLanes + kPmThreads - 1) / kPmThreads), kPmThreads, 0,
+                      stream>>>(
           reinterpret_cast<const uint32_t*>(ws + l.offsets), reinterpret_cast<const uint32_t*>(ws + l.entries), pm, w,
           grid, g, s.nchunks, s.lists_per_frame, s.list_capacity);
     }
     {
       LaunchScope scope("k_pm_long3", stream);
-      k_pm_long3<W><<<static_cast<unsigned>(std::min<size_t>(long_blocks, 1216)), kPmLongThreads, 0, stream>>>(
+      k_pm_long3<W><<<static_cast<unsigned>(std::min<size_t>(long_blocks, 1216)), kPmThreads, 0, stream>>>(
           reinterpret_cast<const uint32_t*>(ws + l.long_lists), reinterpret_cast<const uint32_t*>(ws + l.offsets),
           reinterpret_cast<const uint32_t*>(ws + l.entries), pm, w, grid, g, s.nchunks, s.lists_per_frame);
     }
