@@ -2513,17 +2513,24 @@ __global__ void __launch_bounds__(256) k_pm_update(const PmRecord<W>* pm, const 
   const size_t f = idx / samples;
   const PmRecord<W> r = pm[idx];
   const double* g = grid + f * grid_rows * grid_cols;
+  // separable taps: d = sum_a wr[a] (sum_b wc[b] grid[a][b]), W + 1 FP64
+  // operations per row of taps instead of 2W
+  int cols[W];
+#pragma unroll
+  for (int b = 0; b < W; ++b) {
+    cols[b] = r.c0 + b;
+    if (cols[b] >= grid_cols) cols[b] -= grid_cols;
+  }
   double d = 0.0;
 #pragma unroll
   for (int a = 0; a < W; ++a) {
     int rr = r.r0 + a;
     if (rr >= grid_rows) rr -= grid_rows;
+    const double* line = g + static_cast<size_t>(rr) * grid_cols;
+    double t = 0.0;
 #pragma unroll
-    for (int b = 0; b < W; ++b) {
-      int cc = r.c0 + b;
-      if (cc >= grid_cols) cc -= grid_cols;
-      d += g[static_cast<size_t>(rr) * grid_cols + cc] * (r.wr[a] * r.wc[b]);
-    }
+    for (int b = 0; b < W; ++b) t = fma(line[cols[b]], r.wc[b], t);
+    d = fma(r.wr[a], t, d);
   }
   const double nw = d > 0.0 ? w[idx] / d : 0.0;
   w[idx] = nw;
@@ -3043,9 +3050,26 @@ __global__ void __launch_bounds__(256) k_pm_prepare3(const float* traj, PmRecord
   w[idx] = ok ? 1.0 : 0.0;
 }
 
-// The 3-D grid step: the lanes-per-list form of k_pm_grid, with the entry's
-// plane weight in u.  Lists longer than `capacity` entries (queued by the
-// list sort) are left to k_pm_long3.
+// u of a 3-D entry in the list (plane, row): w times its plane and row tap
+// weights, or false when its taps miss the list's plane or row.
+template <int W>
+struct Pm3Weight {
+  const double* w;
+  int plane, row, g;
+  __device__ __forceinline__ bool operator()(const PmRecord3<W>& r, uint32_t sidx, double* u) const {
+    int dz = plane - r.z0;
+    if (dz < 0) dz += g;
+    int dr = row - r.r0;
+    if (dr < 0) dr += g;
+    if (dz >= W || dr >= W) return false;
+    *u = w[sidx] * (r.wz[dz] * r.wr[dr]);
+    return true;
+  }
+};
+
+// The 3-D grid step for lists of at most `capacity` entries: the
+// lanes-per-list form of k_pm_grid, with the entry's plane weight in u.
+// Longer lists (queued by the list sort) are left to k_pm_long3.
 template <int W>
 __global__ void __launch_bounds__(kPmThreads) k_pm_grid3(const uint32_t* offsets, const uint32_t* entries,
                                                          const PmRecord3<W>* pm, const double* w, double* grid, int g,
@@ -3067,72 +3091,137 @@ __global__ void __launch_bounds__(kPmThreads) k_pm_grid3(const uint32_t* offsets
     const uint32_t begin = off[l], end = off[l + 1];
     active = static_cast<int>(end - begin) <= capacity;
     if (active)
-      pm_accumulate<W>(entries, begin + q, end, kPmLanes, pm, lo, g, cell,
-                       [&](const PmRecord3<W>& r, uint32_t sidx, double* u) {
-                         int dz = plane - r.z0;
-                         if (dz < 0) dz += g;
-                         int dr = row - r.r0;
-                         if (dr < 0) dr += g;
-                         if (dz >= W || dr >= W) return false;
-                         *u = w[sidx] * (r.wz[dz] * r.wr[dr]);
-                         return true;
-                       });
+      pm_accumulate<W>(entries, begin + q, end, kPmLanes, pm, lo, g, cell, Pm3Weight<W>{w, plane, row, g});
   }
   __syncwarp();
   if (active) pm_reduce_store(cells, threadIdx.x - q, q, grid + (static_cast<size_t>(plane) * g + row) * g, lo, g);
 }
 
-// The queued long lists (count at long_lists[0], global list ids after it),
-// one block per list at a time: thread i takes the list's entries i,
-// i + kPmThreads, ... into its own 16 cells (as in k_pm_grid3); then cell t
-// is summed over the block in a fixed order: 16 groups of 16 threads each
-// (within a group starting at a rotation by t), then the groups in order.
-// The kooshball centre's lists hold up to ~10^5 entries.
-template <int W>
-__global__ void __launch_bounds__(kPmThreads) k_pm_long3(const uint32_t* long_lists, const uint32_t* offsets,
-                                                         const uint32_t* entries, const PmRecord3<W>* pm,
-                                                         const double* w, double* grid, int g, int nchunks,
-                                                         int lists_per_plane) {
-  constexpr int kGroups = kPmThreads / kChunk;
-  __shared__ double cells[kChunk * kPmThreads];
-  __shared__ double part[kGroups][kChunk];
+// The queued long lists (count at long_lists[0], global list ids after it)
+// are cut into parts of kPmPart entries: part_base[i] is the first part of
+// queued list i (an exclusive scan, the total at part_base[count]).
+constexpr uint32_t kPmPart = 512;
+
+__global__ void __launch_bounds__(1024) k_pm_long_parts(const uint32_t* long_lists, const uint32_t* offsets,
+                                                        int lists_per_plane, uint32_t* part_base) {
+  __shared__ uint32_t warp_sums[32];
+  __shared__ uint32_t carry;
   const uint32_t queued = long_lists[0];
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (uint32_t i0 = 0; i0 < queued; i0 += 1024) {
+    const uint32_t i = i0 + threadIdx.x;
+    uint32_t parts = 0;
+    if (i < queued) {
+      const uint32_t gl = long_lists[1 + i];
+      const uint32_t plane = gl / static_cast<uint32_t>(lists_per_plane);
+      const uint32_t l = gl - plane * static_cast<uint32_t>(lists_per_plane);
+      const uint32_t* off = offsets + static_cast<size_t>(plane) * (lists_per_plane + 1);
+      parts = (off[l + 1] - off[l] + kPmPart - 1) / kPmPart;
+    }
+    uint32_t incl = parts;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint32_t v = __shfl_up_sync(0xffffffffu, incl, d);
+      if (lane >= d) incl += v;
+    }
+    if (lane == 31) warp_sums[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+      uint32_t ws = warp_sums[lane];
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t v = __shfl_up_sync(0xffffffffu, ws, d);
+        if (lane >= d) ws += v;
+      }
+      warp_sums[lane] = ws;  // inclusive over warps
+    }
+    __syncthreads();
+    const uint32_t before = carry + (warp > 0 ? warp_sums[warp - 1] : 0u) + incl - parts;
+    if (i < queued) part_base[i] = before;
+    __syncthreads();
+    if (threadIdx.x == 1023) carry = before + parts;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part_base[queued] = carry;
+}
+
+// The long lists' parts, kPmLanes lanes per part (as in k_pm_grid3; every
+// part the same work however long its list).  Each part's sums go to
+// partial[part]; the part that completes its list's count (the counters grow
+// by the list's part count every iteration, zeroed once per call) adds the
+// list's parts in part order and writes the cells -- deterministic, and no
+// part waits for another.  Groups stride over the parts.
+template <int W>
+__global__ void __launch_bounds__(kPmThreads) k_pm_long3(const uint32_t* long_lists, const uint32_t* part_base,
+                                                         const uint32_t* offsets, const uint32_t* entries,
+                                                         const PmRecord3<W>* pm, const double* w, double* grid, int g,
+                                                         int nchunks, int lists_per_plane, double* partial,
+                                                         uint32_t* counters) {
+  __shared__ double cells[kChunk * kPmThreads];
+  const int q = threadIdx.x & (kPmLanes - 1);
+  const int lane0 = (threadIdx.x & 31) & ~(kPmLanes - 1);
+  const unsigned gmask = ((1u << kPmLanes) - 1u) << lane0;
+  const uint32_t queued = long_lists[0];
+  const uint32_t total_parts = part_base[queued];
+  const uint32_t groups = gridDim.x * (kPmThreads / kPmLanes);
   double* cell = cells + threadIdx.x;
-  const int c = threadIdx.x & (kChunk - 1), grp = threadIdx.x / kChunk;
-  for (uint32_t qd = blockIdx.x; qd < queued; qd += gridDim.x) {
-    const uint32_t gl = long_lists[1 + qd];
+  for (uint32_t part = (blockIdx.x * kPmThreads + threadIdx.x) / kPmLanes; part < total_parts; part += groups) {
+    // the queued list holding this part: the last i with part_base[i] <= part
+    uint32_t lo_i = 0, hi_i = queued;  // part_base[lo_i] <= part < part_base[hi_i]
+    while (hi_i - lo_i > 1) {
+      const uint32_t mid = (lo_i + hi_i) / 2;
+      if (__ldg(part_base + mid) <= part)
+        lo_i = mid;
+      else
+        hi_i = mid;
+    }
+    const uint32_t first = __ldg(part_base + lo_i), parts = __ldg(part_base + lo_i + 1) - first;
+    const uint32_t gl = __ldg(long_lists + 1 + lo_i);
     const int plane = static_cast<int>(gl / static_cast<uint32_t>(lists_per_plane));
     const int l = static_cast<int>(gl - static_cast<uint32_t>(plane) * lists_per_plane);
     const int row = l / nchunks;
     const int lo = (l - row * nchunks) * kChunk;
     const uint32_t* off = offsets + static_cast<size_t>(plane) * (lists_per_plane + 1);
+    const uint32_t e0 = off[l] + (part - first) * kPmPart, e1 = min(off[l + 1], e0 + kPmPart);
 #pragma unroll
     for (int t = 0; t < kChunk; ++t) cell[t * kPmThreads] = 0.0;
-    pm_accumulate<W>(entries, off[l] + threadIdx.x, off[l + 1], kPmThreads, pm, lo, g, cell,
-                     [&](const PmRecord3<W>& r, uint32_t sidx, double* u) {
-                       int dz = plane - r.z0;
-                       if (dz < 0) dz += g;
-                       int dr = row - r.r0;
-                       if (dr < 0) dr += g;
-                       if (dz >= W || dr >= W) return false;
-                       *u = w[sidx] * (r.wz[dz] * r.wr[dr]);
-                       return true;
-                     });
-    __syncthreads();
-    {
-      const double* src = cells + c * kPmThreads + grp * kChunk;
-      double acc = src[c];
+    pm_accumulate<W>(entries, e0 + q, e1, kPmLanes, pm, lo, g, cell, Pm3Weight<W>{w, plane, row, g});
+    __syncwarp(gmask);
+    // this part's sums (cells 4q .. 4q+3 over the group's lanes)
+    double* mine = partial + static_cast<size_t>(part) * kChunk + q * kPmCellsPerLane;
 #pragma unroll
-      for (int j = 1; j < kChunk; ++j) acc += src[(c + j) & (kChunk - 1)];
-      part[grp][c] = acc;
+    for (int i = 0; i < kPmCellsPerLane; ++i) {
+      const double* c = cells + (q * kPmCellsPerLane + i) * kPmThreads + (threadIdx.x - q);
+      double acc = c[q];
+#pragma unroll
+      for (int j = 1; j < kPmLanes; ++j) acc += c[(q + j) & (kPmLanes - 1)];
+      mine[i] = acc;
     }
-    __syncthreads();
-    if (threadIdx.x < kChunk) {
-      double acc = part[0][c];
-      for (int k = 1; k < kGroups; ++k) acc += part[k][c];
-      if (lo + c < g) grid[(static_cast<size_t>(plane) * g + row) * g + lo + c] = acc;
+    __threadfence();
+    __syncwarp(gmask);
+    uint32_t old = 0;
+    if (q == 0) old = atomicAdd(counters + lo_i, 1u);
+    old = __shfl_sync(gmask, old, lane0);
+    if ((old + 1) % parts == 0) {
+      __threadfence();
+      double acc[kPmCellsPerLane];
+#pragma unroll
+      for (int i = 0; i < kPmCellsPerLane; ++i) acc[i] = 0.0;
+      for (uint32_t p = first; p < first + parts; ++p) {
+        const double* src = partial + static_cast<size_t>(p) * kChunk + q * kPmCellsPerLane;
+#pragma unroll
+        for (int i = 0; i < kPmCellsPerLane; ++i) acc[i] += __ldcg(src + i);
+      }
+      double* out_row = grid + (static_cast<size_t>(plane) * g + row) * g;
+#pragma unroll
+      for (int i = 0; i < kPmCellsPerLane; ++i) {
+        const int col = lo + q * kPmCellsPerLane + i;
+        if (col < g) out_row[col] = acc[i];
+      }
     }
-    __syncthreads();
+    __syncwarp(gmask);  // the cells are read before the next part clears them
   }
 }
 
@@ -3142,22 +3231,30 @@ __global__ void __launch_bounds__(256) k_pm_update3(const PmRecord3<W>* pm, cons
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= samples) return;
   const PmRecord3<W> r = pm[idx];
+  // separable taps: d = sum_a wz[a] sum_b wr[b] (sum_c wc[c] grid[a][b][c]):
+  // W^3 + W^2 + W FP64 operations instead of 2 W^3 + W^2
+  int cols[W];
+#pragma unroll
+  for (int c = 0; c < W; ++c) {
+    cols[c] = r.c0 + c;
+    if (cols[c] >= g) cols[c] -= g;
+  }
   double d = 0.0;
   for (int a = 0; a < W; ++a) {
     int zz = r.z0 + a;
     if (zz >= g) zz -= g;
+    double plane = 0.0;
+#pragma unroll
     for (int b = 0; b < W; ++b) {
       int yy = r.r0 + b;
       if (yy >= g) yy -= g;
-      const double wzy = r.wz[a] * r.wr[b];
       const double* line = grid + (static_cast<size_t>(zz) * g + yy) * g;
+      double t = 0.0;
 #pragma unroll
-      for (int c = 0; c < W; ++c) {
-        int xx = r.c0 + c;
-        if (xx >= g) xx -= g;
-        d += line[xx] * (wzy * r.wc[c]);
-      }
+      for (int c = 0; c < W; ++c) t = fma(line[cols[c]], r.wc[c], t);
+      plane = fma(r.wr[b], t, plane);
     }
+    d = fma(r.wz[a], plane, d);
   }
   const double nw = d > 0.0 ? w[idx] / d : 0.0;
   w[idx] = nw;
@@ -3165,7 +3262,8 @@ __global__ void __launch_bounds__(256) k_pm_update3(const PmRecord3<W>* pm, cons
 }
 
 struct PmLayout3 {
-  size_t flags, records, counts, cursor, offsets, bases, entries, long_lists, pm, w, grid, total, entries_total;
+  size_t flags, records, counts, cursor, offsets, bases, entries, long_lists, pm, w, grid, part_base, partial, counters,
+      total, entries_total, max_long;
 };
 
 PmLayout3 make_pm_layout3(const Shape& s) {
@@ -3190,6 +3288,12 @@ PmLayout3 make_pm_layout3(const Shape& s) {
   l.pm = take(static_cast<size_t>(s.samples) * (16 + 24 * static_cast<size_t>(s.width)));
   l.w = take(static_cast<size_t>(s.samples) * sizeof(double));
   l.grid = take(g * g * g * sizeof(double));
+  // the long lists' parts of kPmPart entries: first part of each list, the
+  // parts' sums, one counter per list
+  l.max_long = l.entries_total / (static_cast<size_t>(s.list_capacity) + 1) + 2;
+  l.part_base = take((l.max_long + 1) * 4);
+  l.partial = take((l.entries_total / kPmPart + l.max_long) * kChunk * sizeof(double));
+  l.counters = take(l.max_long * 4);
   l.total = off;
   return l;
 }
@@ -3215,22 +3319,29 @@ ksj_gpu_status launch_pipe_menon3(const Shape& s, const PmLayout3& l, uint32_t i
     k_pm_prepare3<W><<<(s.samples + 255) / 256, 256, 0, stream>>>(d_traj, pm, w, s.samples, g, s.beta,
                                                                  1.0 / std::cyl_bessel_i(0.0, static_cast<double>(s.beta)));
   }
+  const uint32_t* offsets = reinterpret_cast<const uint32_t*>(ws + l.offsets);
+  const uint32_t* entries = reinterpret_cast<const uint32_t*>(ws + l.entries);
+  const uint32_t* long_lists = reinterpret_cast<const uint32_t*>(ws + l.long_lists);
+  uint32_t* part_base = reinterpret_cast<uint32_t*>(ws + l.part_base);
+  uint32_t* counters = reinterpret_cast<uint32_t*>(ws + l.counters);
+  double* partial = reinterpret_cast<double*>(ws + l.partial);
+  if (cudaMemsetAsync(counters, 0, l.max_long * 4, stream) != cudaSuccess) return KSJ_GPU_ERROR_CUDA;
+  {
+    LaunchScope scope("k_pm_long_parts", stream);
+    k_pm_long_parts<<<1, 1024, 0, stream>>>(long_lists, offsets, s.lists_per_frame, part_base);
+  }
   const size_t lists = static_cast<size_t>(g) * s.lists_per_frame;
-  // at most this many lists exceed the capacity
-  const size_t long_blocks = std::max<size_t>(1, l.entries_total / (static_cast<size_t>(s.list_capacity) + 1));
+  const unsigned grid_blocks = static_cast<unsigned>((lists * kPmLanes + kPmThreads - 1) / kPmThreads);
   for (uint32_t it = 0; it < iterations; ++it) {
     {
       LaunchScope scope("k_pm_grid3", stream);
-      k_pm_grid3<W><<<static_cast<unsigned>((lists * kPmLanes + kPmThreads - 1) / kPmThreads), kPmThreads, 0,
-                      stream>>>(
-          reinterpret_cast<const uint32_t*>(ws + l.offsets), reinterpret_cast<const uint32_t*>(ws + l.entries), pm, w,
-          grid, g, s.nchunks, s.lists_per_frame, s.list_capacity);
+      k_pm_grid3<W><<<grid_blocks, kPmThreads, 0, stream>>>(offsets, entries, pm, w, grid, g, s.nchunks,
+                                                            s.lists_per_frame, s.list_capacity);
     }
     {
       LaunchScope scope("k_pm_long3", stream);
-      k_pm_long3<W><<<static_cast<unsigned>(std::min<size_t>(long_blocks, 1216)), kPmThreads, 0, stream>>>(
-          reinterpret_cast<const uint32_t*>(ws + l.long_lists), reinterpret_cast<const uint32_t*>(ws + l.offsets),
-          reinterpret_cast<const uint32_t*>(ws + l.entries), pm, w, grid, g, s.nchunks, s.lists_per_frame);
+      k_pm_long3<W><<<152 * 6, kPmThreads, 0, stream>>>(long_lists, part_base, offsets, entries, pm, w, grid, g,
+                                                        s.nchunks, s.lists_per_frame, partial, counters);
     }
     LaunchScope scope("k_pm_update3", stream);
     k_pm_update3<W><<<(s.samples + 255) / 256, 256, 0, stream>>>(pm, grid, w, it + 1 == iterations ? d_dcf : nullptr,

@@ -1,10 +1,12 @@
 """Pipe-Menon density weights (ksj_gpu_pipe_menon_dcf) against the FP64
 oracle restatement of the same grid-based iteration.  Both run in double
-precision with the same tap sets and per-cell summation order (except the
-3-D lists above 512 entries, summed in segments); they differ only in the
-Bessel I0 evaluation, fused multiply-adds and those segment sums (~1e-15); the
-output is float32, so the bound is 1e-7 relative L2 (float32 rounding of the
-weights alone is ~3e-8)."""
+precision with the same tap sets; the GPU sums each cell in a fixed order of
+its own (a few lanes per list take entries in turn and their sums are added
+in lane order; in 3-D, lists split over 512-entry tasks add the tasks' parts
+in task order), the oracle in sample order.  They differ in that order, the
+Bessel I0 evaluation and fused multiply-adds (~1e-15); the output is float32,
+so the bound is 1e-7 relative L2 (float32 rounding of the weights alone is
+~3e-8)."""
 import numpy as np
 import pytest
 
@@ -77,9 +79,9 @@ def _lists3_over(tr, g, width, capacity=512):
 def test_pipe_menon3_matches_fp64_oracle(native, cuda, orc, n, g, width):
     """3-D Pipe-Menon (the kooshball configuration's density weights) against
     the double-precision restatement, 10 iterations.  The oracle gets the
-    float32 kernel shape the GPU path uses.  The centre's lists exceed the
-    512-entry sort capacity, so their cells come from the long-list kernel
-    (32 segments added in segment order; the oracle sums in sample order, a
+    float32 kernel shape the GPU path uses.  The centre's lists exceed 1024
+    entries, so their cells are split over several 512-entry tasks whose
+    parts are added in task order (the oracle sums in sample order, a
     difference of ~1e-16)."""
     import torch
     from kspacejet_gb300 import gpu, synth
