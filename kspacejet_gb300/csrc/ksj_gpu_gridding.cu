@@ -1748,9 +1748,19 @@ __global__ void __launch_bounds__(kColsThreads) k_cols(const __grid_constant__ C
         const int pr = q >> lg_cb;
         const int base = live ? (__ldg(a.pos_rows + pr) << lg_lines) + ((q & (cb - 1)) << lg_cgc) : 0;
         float total = live ? rss[q] : 0.0f;
-        for (int t = 0; t < live_coils + 31; ++t) {
-          const int c = t - lane;
-          if (live && c >= 0 && c < live_coils) total = __fadd_rn(total, tile[base + c].x);
+        if (live_coils == 32) {
+          // fixed trip count: every load of the walk can be issued ahead of
+          // the dependent adds
+#pragma unroll
+          for (int t = 0; t < 63; ++t) {
+            const int c = t - lane;
+            if (live && c >= 0 && c < 32) total = __fadd_rn(total, tile[base + c].x);
+          }
+        } else {
+          for (int t = 0; t < live_coils + 31; ++t) {
+            const int c = t - lane;
+            if (live && c >= 0 && c < live_coils) total = __fadd_rn(total, tile[base + c].x);
+          }
         }
         if (live) rss[q] = total;
       }
