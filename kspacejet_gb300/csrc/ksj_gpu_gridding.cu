@@ -3027,9 +3027,18 @@ struct PmRecord3 {
   double wc[W];
 };
 
+// The column part of a 3-D record, compact: what the grid step gathers per
+// entry after the first iteration (the entry's plane and row weight product
+// is kept per entry then).
 template <int W>
-__global__ void __launch_bounds__(256) k_pm_prepare3(const float* traj, PmRecord3<W>* pm, double* w, int samples,
-                                                     int grid, double beta, double inv_i0_beta) {
+struct PmCol3 {
+  double wc[W];
+  int c0, pad;
+};
+
+template <int W>
+__global__ void __launch_bounds__(256) k_pm_prepare3(const float* traj, PmRecord3<W>* pm, PmCol3<W>* pmc, double* w,
+                                                     int samples, int grid, double beta, double inv_i0_beta) {
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= samples) return;
   float k[3];
@@ -3057,33 +3066,66 @@ __global__ void __launch_bounds__(256) k_pm_prepare3(const float* traj, PmRecord
     r.wc[j] = ok ? kb_weight64(static_cast<double>(t0[2] + j) - u[2], W, beta, inv_i0_beta) : 0.0;
   }
   pm[idx] = r;
+  PmCol3<W> c;
+#pragma unroll
+  for (int j = 0; j < W; ++j) c.wc[j] = r.wc[j];
+  c.c0 = r.c0;
+  c.pad = 0;
+  pmc[idx] = c;
   w[idx] = ok ? 1.0 : 0.0;
 }
 
-// u of a 3-D entry in the list (plane, row): w times its plane and row tap
-// weights, or false when its taps miss the list's plane or row.
-template <int W>
-struct Pm3Weight {
-  const double* w;
-  int plane, row, g;
-  __device__ __forceinline__ bool operator()(const PmRecord3<W>& r, uint32_t sidx, double* u) const {
-    int dz = plane - r.z0;
-    if (dz < 0) dz += g;
-    int dr = row - r.r0;
-    if (dr < 0) dr += g;
-    if (dz >= W || dr >= W) return false;
-    *u = w[sidx] * (r.wz[dz] * r.wr[dr]);
-    return true;
+// One lane's share of a 3-D list's entries (as pm_accumulate).  The first
+// iteration (kFirst) reads each entry's whole record, forms u = w * (wz[dz] *
+// wr[dr]) and keeps the product wz[dz] * wr[dr] per entry (wzr, in entry
+// order); the later iterations gather only w and the compact column record
+// and read the product back in entry order -- under half the bytes per
+// entry, the bound of this step.  The same operations in the same order
+// either way: bit-identical cells.
+template <int W, bool kFirst>
+__device__ __forceinline__ void pm3_accumulate(const uint32_t* entries, uint32_t e0, uint32_t e1, uint32_t step,
+                                               const PmRecord3<W>* pm, const PmCol3<W>* pmc, const double* w,
+                                               double* wzr, int plane, int row, int lo, int g, double* cell) {
+  for (uint32_t e = e0; e < e1; e += step) {
+    const uint32_t sidx = __ldg(entries + e);
+    double f;
+    int col;
+    const double* wc;
+    if constexpr (kFirst) {
+      const PmRecord3<W>& r = pm[sidx];
+      int dz = plane - r.z0;
+      if (dz < 0) dz += g;
+      int dr = row - r.r0;
+      if (dr < 0) dr += g;
+      f = dz < W && dr < W ? r.wz[dz] * r.wr[dr] : 0.0;
+      wzr[e] = f;
+      col = r.c0;
+      wc = r.wc;
+    } else {
+      f = wzr[e];
+      const PmCol3<W>& c = pmc[sidx];
+      col = c.c0;
+      wc = c.wc;
+    }
+    if (f == 0.0) continue;  // taps outside the list's plane or row
+    const double u = w[sidx] * f;
+#pragma unroll
+    for (int k = 0; k < W; ++k) {
+      const int t = col - lo;
+      if (t >= 0 && t < kChunk) cell[t * kPmThreads] = fma(u, wc[k], cell[t * kPmThreads]);
+      if (++col == g) col = 0;
+    }
   }
-};
+}
 
 // The 3-D grid step for lists of at most `capacity` entries: the
 // lanes-per-list form of k_pm_grid, with the entry's plane weight in u.
 // Longer lists (queued by the list sort) are left to k_pm_long3.
-template <int W>
+template <int W, bool kFirst>
 __global__ void __launch_bounds__(kPmThreads) k_pm_grid3(const uint32_t* offsets, const uint32_t* entries,
-                                                         const PmRecord3<W>* pm, const double* w, double* grid, int g,
-                                                         int nchunks, int lists_per_plane, int capacity) {
+                                                         const PmRecord3<W>* pm, const PmCol3<W>* pmc, const double* w,
+                                                         double* wzr, double* grid, int g, int nchunks,
+                                                         int lists_per_plane, int capacity) {
   __shared__ double cells[kChunk * kPmThreads];
   const size_t list = (static_cast<size_t>(blockIdx.x) * kPmThreads + threadIdx.x) / kPmLanes;
   const int q = threadIdx.x & (kPmLanes - 1);
@@ -3101,7 +3143,7 @@ __global__ void __launch_bounds__(kPmThreads) k_pm_grid3(const uint32_t* offsets
     const uint32_t begin = off[l], end = off[l + 1];
     active = static_cast<int>(end - begin) <= capacity;
     if (active)
-      pm_accumulate<W>(entries, begin + q, end, kPmLanes, pm, lo, g, cell, Pm3Weight<W>{w, plane, row, g});
+      pm3_accumulate<W, kFirst>(entries, begin + q, end, kPmLanes, pm, pmc, w, wzr, plane, row, lo, g, cell);
   }
   __syncwarp();
   if (active) pm_reduce_store(cells, threadIdx.x - q, q, grid + (static_cast<size_t>(plane) * g + row) * g, lo, g);
@@ -3163,10 +3205,11 @@ __global__ void __launch_bounds__(1024) k_pm_long_parts(const uint32_t* long_lis
 // by the list's part count every iteration, zeroed once per call) adds the
 // list's parts in part order and writes the cells -- deterministic, and no
 // part waits for another.  Groups stride over the parts.
-template <int W>
+template <int W, bool kFirst>
 __global__ void __launch_bounds__(kPmThreads) k_pm_long3(const uint32_t* long_lists, const uint32_t* part_base,
                                                          const uint32_t* offsets, const uint32_t* entries,
-                                                         const PmRecord3<W>* pm, const double* w, double* grid, int g,
+                                                         const PmRecord3<W>* pm, const PmCol3<W>* pmc,
+                                                         const double* w, double* wzr, double* grid, int g,
                                                          int nchunks, int lists_per_plane, double* partial,
                                                          uint32_t* counters) {
   __shared__ double cells[kChunk * kPmThreads];
@@ -3197,7 +3240,7 @@ __global__ void __launch_bounds__(kPmThreads) k_pm_long3(const uint32_t* long_li
     const uint32_t e0 = off[l] + (part - first) * kPmPart, e1 = min(off[l + 1], e0 + kPmPart);
 #pragma unroll
     for (int t = 0; t < kChunk; ++t) cell[t * kPmThreads] = 0.0;
-    pm_accumulate<W>(entries, e0 + q, e1, kPmLanes, pm, lo, g, cell, Pm3Weight<W>{w, plane, row, g});
+    pm3_accumulate<W, kFirst>(entries, e0 + q, e1, kPmLanes, pm, pmc, w, wzr, plane, row, lo, g, cell);
     __syncwarp(gmask);
     // this part's sums (cells 4q .. 4q+3 over the group's lanes)
     double* mine = partial + static_cast<size_t>(part) * kChunk + q * kPmCellsPerLane;
@@ -3272,8 +3315,8 @@ __global__ void __launch_bounds__(256) k_pm_update3(const PmRecord3<W>* pm, cons
 }
 
 struct PmLayout3 {
-  size_t flags, records, counts, cursor, offsets, bases, entries, long_lists, pm, w, grid, part_base, partial, counters,
-      total, entries_total, max_long;
+  size_t flags, records, counts, cursor, offsets, bases, entries, long_lists, pm, pmc, wzr, w, grid, part_base, partial,
+      counters, total, entries_total, max_long;
 };
 
 PmLayout3 make_pm_layout3(const Shape& s) {
@@ -3296,6 +3339,8 @@ PmLayout3 make_pm_layout3(const Shape& s) {
   l.entries = take(l.entries_total * 4);
   l.long_lists = take((2 + l.entries_total / (s.list_capacity + 1)) * 4);
   l.pm = take(static_cast<size_t>(s.samples) * (16 + 24 * static_cast<size_t>(s.width)));
+  l.pmc = take(static_cast<size_t>(s.samples) * (8 + 8 * static_cast<size_t>(s.width)));
+  l.wzr = take(l.entries_total * sizeof(double));
   l.w = take(static_cast<size_t>(s.samples) * sizeof(double));
   l.grid = take(g * g * g * sizeof(double));
   // the long lists' parts of kPmPart entries: first part of each list, the
@@ -3321,12 +3366,15 @@ ksj_gpu_status launch_pipe_menon3(const Shape& s, const PmLayout3& l, uint32_t i
       reinterpret_cast<uint32_t*>(ws + l.bases), reinterpret_cast<uint32_t*>(ws + l.entries), nullptr,
       reinterpret_cast<uint32_t*>(ws + l.long_lists), l.entries_total, stream);
   if (st != KSJ_GPU_OK) return st;
+  static_assert(sizeof(PmCol3<W>) == 8 + 8 * W, "PmCol3 layout");
   PmRecord3<W>* pm = reinterpret_cast<PmRecord3<W>*>(ws + l.pm);
+  PmCol3<W>* pmc = reinterpret_cast<PmCol3<W>*>(ws + l.pmc);
+  double* wzr = reinterpret_cast<double*>(ws + l.wzr);
   double* w = reinterpret_cast<double*>(ws + l.w);
   double* grid = reinterpret_cast<double*>(ws + l.grid);
   {
     LaunchScope scope("k_pm_prepare3", stream);
-    k_pm_prepare3<W><<<(s.samples + 255) / 256, 256, 0, stream>>>(d_traj, pm, w, s.samples, g, s.beta,
+    k_pm_prepare3<W><<<(s.samples + 255) / 256, 256, 0, stream>>>(d_traj, pm, pmc, w, s.samples, g, s.beta,
                                                                  1.0 / std::cyl_bessel_i(0.0, static_cast<double>(s.beta)));
   }
   const uint32_t* offsets = reinterpret_cast<const uint32_t*>(ws + l.offsets);
@@ -3343,15 +3391,18 @@ ksj_gpu_status launch_pipe_menon3(const Shape& s, const PmLayout3& l, uint32_t i
   const size_t lists = static_cast<size_t>(g) * s.lists_per_frame;
   const unsigned grid_blocks = static_cast<unsigned>((lists * kPmLanes + kPmThreads - 1) / kPmThreads);
   for (uint32_t it = 0; it < iterations; ++it) {
+    // the first iteration keeps each entry's plane-row weight product
     {
       LaunchScope scope("k_pm_grid3", stream);
-      k_pm_grid3<W><<<grid_blocks, kPmThreads, 0, stream>>>(offsets, entries, pm, w, grid, g, s.nchunks,
-                                                            s.lists_per_frame, s.list_capacity);
+      auto kernel = it == 0 ? k_pm_grid3<W, true> : k_pm_grid3<W, false>;
+      kernel<<<grid_blocks, kPmThreads, 0, stream>>>(offsets, entries, pm, pmc, w, wzr, grid, g, s.nchunks,
+                                                     s.lists_per_frame, s.list_capacity);
     }
     {
       LaunchScope scope("k_pm_long3", stream);
-      k_pm_long3<W><<<152 * 6, kPmThreads, 0, stream>>>(long_lists, part_base, offsets, entries, pm, w, grid, g,
-                                                        s.nchunks, s.lists_per_frame, partial, counters);
+      auto kernel = it == 0 ? k_pm_long3<W, true> : k_pm_long3<W, false>;
+      kernel<<<152 * 6, kPmThreads, 0, stream>>>(long_lists, part_base, offsets, entries, pm, pmc, w, wzr, grid, g,
+                                                 s.nchunks, s.lists_per_frame, partial, counters);
     }
     LaunchScope scope("k_pm_update3", stream);
     k_pm_update3<W><<<(s.samples + 255) / 256, 256, 0, stream>>>(pm, grid, w, it + 1 == iterations ? d_dcf : nullptr,
