@@ -3107,7 +3107,9 @@ __device__ __forceinline__ void pm3_accumulate(const uint32_t* entries, uint32_t
       col = c.c0;
       wc = c.wc;
     }
-    if (f == 0.0) continue;  // taps outside the list's plane or row
+    // taps outside the list's plane or row (f >= 0: an integer test keeps
+    // the FP64 pipe, the bound of this step, for the arithmetic)
+    if (__double_as_longlong(f) == 0) continue;
     const double u = w[sidx] * f;
 #pragma unroll
     for (int k = 0; k < W; ++k) {
