@@ -84,9 +84,9 @@ typedef int32_t ksj_gpu_status;
 typedef struct ksj_gpu_gridding_desc {
   uint32_t struct_size;     /* sizeof(ksj_gpu_gridding_desc) */
   uint32_t kernel;          /* KSJ_GPU_KERNEL_* */
-  uint32_t image_rows;      /* output image, 2..1024 */
+  uint32_t image_rows;      /* output image, 2..512 */
   uint32_t image_cols;
-  uint32_t grid_rows;       /* oversampled grid; == image for LINEAR; 2^a * 3^b, a+b >= 1, <= 1024 */
+  uint32_t grid_rows;       /* oversampled grid; == image for LINEAR; 2^a 3^b 5^c 7^d, 2..512 */
   uint32_t grid_cols;
   uint32_t kernel_width;    /* LINEAR: 2.  KAISER_BESSEL: even, 2..8 */
   float kb_beta;            /* KAISER_BESSEL shape; <= 0 selects Beatty et al. 2005 for (width, grid/image) */
@@ -221,7 +221,7 @@ KSJ_GPU_API ksj_gpu_status ksj_gpu_gridding_tune(const ksj_gpu_gridding_desc* de
 /* ------------------------------------------------------ 3-D gridding */
 
 /* 3-D Kaiser-Bessel adjoint gridding on a cube (no counterpart in the
- * reference, which is 2-D only): image n^3, grid g^3 (g = 2^a 3^b <= 512,
+ * reference, which is 2-D only): image n^3, grid g^3 (g = 2^a 3^b 5^c 7^d <= 512,
  * g >= n), origin (n-1)/2 on every axis, taps, weights, crop and
  * deapodisation as the 2-D Kaiser-Bessel path along each axis. */
 typedef struct ksj_gpu_gridding3_desc {
@@ -294,7 +294,7 @@ KSJ_GPU_API ksj_gpu_status ksj_gpu_direct_adjoint(uint32_t rows, uint32_t cols, 
  * weights, phase, crop positions and deapodisation), i.e. the fast
  * approximation of ksj_gpu_direct_forward that the gridding adjoint pairs
  * with.  desc: kernel KAISER_BESSEL, square image and grid (grid <= 512,
- * 2^a or 3 * 2^a), width 2/4/6/8, complex64 samples; dcf_mode and output are
+ * 2^a 3^b 5^c 7^d), width 2/4/6/8, complex64 samples; dcf_mode and output are
  * ignored.  d_image complex64 coil-last [frame][row][col][channel]; d_traj
  * [frame][sample][2]; d_samples complex64 [frame][channel][sample].  A
  * non-finite or far out-of-range coordinate gives 0 and raises

@@ -41,7 +41,7 @@ def _run(cuda, n, g, w, tr, ks, output, dcf_mode=None, sample_format=0, tuning=N
 
 
 @pytest.mark.parametrize("n,g,w,readout,spokes,coils", [(16, 24, 4, 24, 400, 3), (16, 32, 6, 32, 300, 2),
-                                                        (24, 48, 4, 48, 400, 5)])
+                                                        (24, 48, 4, 48, 400, 5), (20, 40, 4, 40, 300, 2)])
 def test_gridding3_matches_fp64_oracle_and_nudft(native, cuda, orc, n, g, w, readout, spokes, coils):
     from kspacejet_gb300 import gpu
 

@@ -23,7 +23,9 @@ def _case(n, g, frames, coils, spokes, seed):
 
 
 @pytest.mark.parametrize("n,g,w,frames,coils", [(32, 64, 4, 2, 3), (48, 96, 6, 1, 2), (64, 128, 4, 2, 33),
-                                                (96, 192, 4, 1, 8), (24, 48, 8, 1, 1)])
+                                                (96, 192, 4, 1, 8), (24, 48, 8, 1, 1),
+                                                # grids with factors 5 and 7 (mixed-radix plans)
+                                                (40, 80, 4, 1, 3), (56, 112, 4, 1, 2)])
 def test_kb_forward_matches_fp64(native, cuda, orc, n, g, w, frames, coils):
     import torch
     from kspacejet_gb300 import gpu
