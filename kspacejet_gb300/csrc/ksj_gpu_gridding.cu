@@ -3392,6 +3392,12 @@ ksj_gpu_status launch_pipe_menon3(const Shape& s, const PmLayout3& l, uint32_t i
   }
   const size_t lists = static_cast<size_t>(g) * s.lists_per_frame;
   const unsigned grid_blocks = static_cast<unsigned>((lists * kPmLanes + kPmThreads - 1) / kPmThreads);
+  // the long-list parts: a grid-stride loop over six 256-thread blocks per SM
+  int device = 0, sms = 0;
+  if (cudaGetDevice(&device) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || sms <= 0)
+    return KSJ_GPU_ERROR_CUDA;
+  const unsigned long_blocks = static_cast<unsigned>(sms) * 6;
   for (uint32_t it = 0; it < iterations; ++it) {
     // the first iteration keeps each entry's plane-row weight product
     {
@@ -3403,7 +3409,7 @@ ksj_gpu_status launch_pipe_menon3(const Shape& s, const PmLayout3& l, uint32_t i
     {
       LaunchScope scope("k_pm_long3", stream);
       auto kernel = it == 0 ? k_pm_long3<W, true> : k_pm_long3<W, false>;
-      kernel<<<152 * 6, kPmThreads, 0, stream>>>(long_lists, part_base, offsets, entries, pm, pmc, w, wzr, grid, g,
+      kernel<<<long_blocks, kPmThreads, 0, stream>>>(long_lists, part_base, offsets, entries, pm, pmc, w, wzr, grid, g,
                                                  s.nchunks, s.lists_per_frame, partial, counters);
     }
     LaunchScope scope("k_pm_update3", stream);
