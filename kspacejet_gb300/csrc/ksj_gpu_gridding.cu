@@ -60,7 +60,7 @@ constexpr int kMaxGrid = 512;
 constexpr int kMaxThreads = 512;
 constexpr int kColsThreads = 256;  // k_cols block size
 constexpr int kAhead = 8;         // coil loads in flight per warp in k_rows
-constexpr int kAheadRegs = 4;     // the same for the register-cell form at 80 registers (a shorter unrolled body)
+constexpr int kAheadRegs = 2;     // the same for the register-cell form (its unrolled body grows with it: 2 measured best)
 constexpr uint32_t kFlagBytes = 256;
 
 // Per (frame, sample) record written by k_prepare, read by k_rows.
