@@ -538,7 +538,7 @@ def run_ours(args) -> dict | None:
     # E2E_WINDOWS windows of exactly `steps` steps each, every one bracketed
     # by a barrier and a synchronize; the median is reported.  Each step
     # issues ~30 host calls (copies, events, launches), so a host-side stall
-    # (one window in ~8 on the GB300 host measured) drains the GPU queue and
+    # (about one window in six on the GB300 host measured) drains the GPU queue and
     # adds ~1 ms per step to that window; the median of five is robust to it
     # and every window is listed in the line.
     e2e_windows = []
