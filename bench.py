@@ -143,6 +143,19 @@ class ClockSampler:
 
 # --------------------------------------------------------- CPU baseline
 
+def _single_thread_rate(task, pairs, budget_s: float = 1.5) -> tuple[float, int]:
+    """Gridded samples/s of `task` run one (frame, coil) image after another
+    on the calling thread for about `budget_s` (at least one image)."""
+    done = samples = 0
+    t0 = time.perf_counter()
+    while done < len(pairs):
+        samples += task(pairs[done])
+        done += 1
+        if time.perf_counter() - t0 >= budget_s:
+            break
+    return samples / (time.perf_counter() - t0), done
+
+
 def cpu_reference_rate(traj: np.ndarray, ksp: np.ndarray, budget_s: float = 2.5, min_pairs: int = 0):
     """Gridded samples/s of the reference's CPU path (ramp DCF + linear
     gridding + separable inverse DFT, one (frame, coil) image per task) on all
@@ -180,7 +193,9 @@ def cpu_reference_rate(traj: np.ndarray, ksp: np.ndarray, budget_s: float = 2.5,
             if (el >= budget_s and done >= min_pairs) or done >= len(pairs):
                 break
     el = time.perf_counter() - t0
+    single, single_n = _single_thread_rate(task, pairs[done:] or pairs)
     return {"value": samples / el, "unit": METRIC, "cores": cores, "kind": kind,
+            "single_thread_value": single, "single_thread_images": single_n,
             "sample": f"{done} (frame, coil) images of the workload ({traj.shape[1]} samples each) through "
                       f"radial_linear_gridding2_adjoint with ramp DCF on a {IMAGE}x{IMAGE} grid (the reference's "
                       f"direct-DFT fallback for a non-power-of-two axis), {cores} threads, {el:.2f} s wall"}
@@ -221,7 +236,9 @@ def cpu_kb_rate(traj: np.ndarray, ksp: np.ndarray, budget_s: float = 3.0, width:
             if el >= budget_s or done >= len(pairs):
                 break
     el = time.perf_counter() - t0
+    single, single_n = _single_thread_rate(task, pairs[done:] or pairs)
     return {"value": samples / el, "unit": METRIC, "cores": cores, "kind": "port",
+            "single_thread_value": single, "single_thread_images": single_n,
             "sample": f"restatement, not reference (the reference has no Kaiser-Bessel path): {done} (frame, coil) "
                       f"images of the workload ({traj.shape[1]} samples each), KB W={width} gridding on the "
                       f"{GRID}^2 grid, FFT of every grid row and of the {IMAGE} kept columns, crop and "
