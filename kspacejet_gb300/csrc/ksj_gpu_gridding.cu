@@ -1094,6 +1094,7 @@ static_assert(kSegMin * kSegMax <= (1 << 22), "segment counts are taken from len
 __host__ __device__ inline int seg_start(uint32_t begin, int seg, int sl) { return static_cast<int>(begin) + seg * sl; }
 
 __host__ __device__ inline int segment_length(int n) {
+  if (n <= kSegMin) return n;  // one segment (most lists): no division
   const int sg = list_segments(n);
   return (n + sg - 1) / sg;
 }
@@ -1197,9 +1198,14 @@ __device__ __forceinline__ void put_chunk(const float2 (&r)[kChunk], float2* dst
                                           int wait_beyond) {
   if (counter == nullptr) {
     if (live) {
+      if (width == kChunk) {  // every chunk of the row but a partial last one
 #pragma unroll
-      for (int t = 0; t < kChunk; ++t)
-        if (t < width) dst[t * stride] = r[t];
+        for (int t = 0; t < kChunk; ++t) dst[t * stride] = r[t];
+      } else {
+#pragma unroll
+        for (int t = 0; t < kChunk; ++t)
+          if (t < width) dst[t * stride] = r[t];
+      }
     }
     return;
   }
