@@ -1116,7 +1116,7 @@ __device__ __forceinline__ void grid_entries_regs(float2 (&r)[kChunk], const Row
                                                   float4* meta, bool have_sk = false, uint32_t sk_first = 0u) {
   constexpr int kMV = meta_vecs(W);
   constexpr int kBatch = meta_batch(W);
-  const void* ks = a.samples_t;
+  const SampleRows<kFormat> sample_row(a.samples_t, sample_base, a.channels);
 #pragma unroll
   for (int t = 0; t < kChunk; ++t) r[t] = make_float2(0.0f, 0.0f);
   uint32_t sk_batch = sk_first;
@@ -1129,8 +1129,7 @@ __device__ __forceinline__ void grid_entries_regs(float2 (&r)[kChunk], const Row
 #pragma unroll
       for (int k = 0; k < kAR; ++k) {
         const uint32_t sk = __shfl_sync(0xffffffffu, sk_batch, k);
-        yv[k] = (coil_ok && k < cnt) ? load_sample<kFormat>(ks, sample_base + static_cast<size_t>(sk) * a.channels)
-                                     : make_float2(0.0f, 0.0f);
+        yv[k] = (coil_ok && k < cnt) ? sample_row(sk) : make_float2(0.0f, 0.0f);
       }
     }
     if (have_sk && base + kBatch < n) {
@@ -1146,10 +1145,7 @@ __device__ __forceinline__ void grid_entries_regs(float2 (&r)[kChunk], const Row
       for (int v = 0; v < kMV; ++v) m[v] = __ldg(src + v);
     }
     __syncwarp();
-    auto fetch = [&](int i) {
-      const uint32_t sk = __float_as_uint(meta[i * kMV].y);
-      return load_sample<kFormat>(ks, sample_base + static_cast<size_t>(sk) * a.channels);
-    };
+    auto fetch = [&](int i) { return sample_row(__float_as_uint(meta[i * kMV].y)); };
     if (!pre) {
 #pragma unroll
       for (int k = 0; k < kAR; ++k) yv[k] = (coil_ok && k < cnt) ? fetch(k) : make_float2(0.0f, 0.0f);

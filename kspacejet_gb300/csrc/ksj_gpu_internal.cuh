@@ -218,6 +218,23 @@ __device__ __forceinline__ float2 load_sample<KSJ_GPU_SAMPLES_BF16>(const void* 
                      bf16_to_float(static_cast<uint16_t>(packed >> 16)));
 }
 
+// A sample by row index from a lane's own base: `lane_base` points at this
+// lane's coil of sample 0 and `row_bytes` is one sample row (channels x
+// element bytes, < 2^32), so the address is one 32 x 32 -> 64-bit
+// multiply-add per load.
+template <uint32_t kFormat>
+struct SampleRows {
+  static constexpr uint32_t kBytes = kFormat == KSJ_GPU_SAMPLES_BF16 ? 4u : 8u;
+  const unsigned char* lane_base;
+  uint32_t row_bytes;
+  __device__ __forceinline__ SampleRows(const void* samples, size_t lane_index, int channels)
+      : lane_base(static_cast<const unsigned char*>(samples) + lane_index * kBytes),
+        row_bytes(static_cast<uint32_t>(channels) * kBytes) {}
+  __device__ __forceinline__ float2 operator()(uint32_t row) const {
+    return load_sample<kFormat>(lane_base + static_cast<uint64_t>(row) * row_bytes, 0);
+  }
+};
+
 // -------------------------------------------------------------------- FFT
 
 // In-place R-point inverse DFT (exp(+2 pi i j k / R)) on registers.
